@@ -1,0 +1,408 @@
+"""Lanczos throughput on one GB300 (or N independent replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload m573_n50k] [--precision mixed|fp64]
+
+A step is one bi-Lanczos step of run_FT (two operator applications, L and
+L^T, plus the float64 recurrence) on a seeded synthetic ensemble with the
+shapes of the named workload (default: 573 modes, 50 000 configurations, no
+symmetry images, log-normal weights sigma 0.1).  W steps are run untimed,
+then K steps are timed with CUDA events on the launching stream; the ensemble
+(2 x 50 000 x 573 float64 = 458 MB) is larger than L2, so no flush is needed
+between steps.  One JSON line is printed by rank 0.
+
+--impl reference times the reference's own CPU implementation of the same
+step (its C kernels compiled from source when present, else the oracle's C
+restatement) on the host cores, each step a bounded sample of the
+configurations scaled to the full ensemble.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Lanczos steps/s, M=576 N=50k: mixed vs FP64 GPU at ≤1e-4 rel spectral error"
+UNIT = "steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="m573_n50k")
+    ap.add_argument("--precision", default=None, choices=[None, "mixed", "fp64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(name):
+    from tdscha_gb300.synthetic import WORKLOADS, make_ensemble
+    if name not in WORKLOADS:
+        raise SystemExit("unknown workload %s (known: %s)" % (name, ", ".join(WORKLOADS)))
+    spec = WORKLOADS[name]
+    ens = make_ensemble(spec["M"], spec["N"], seed=2024, n_syms=spec["n_syms"],
+                        rho_sigma=spec["rho_sigma"])
+    return spec, ens
+
+
+def identity_tables(M):
+    return ([np.ones((1, 1, 1))] * M, [np.array([i], dtype=np.intc) for i in range(M)],
+            np.arange(M, dtype=np.intc))
+
+
+def sym_tables(ens):
+    if ens.get("symmetries") is None:
+        return identity_tables(ens["X"].shape[1])
+    return ens["symmetries"], ens["degenerate_space"], ens["sym_block_id"]
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_sample_time(ens, n_cfg, n_threads, use_ref):
+    """Seconds of one perturbation-average call over the first n_cfg configurations."""
+    import oracle
+    from tdscha_gb300.synthetic import random_R1, random_sym
+    M = ens["X"].shape[1]
+    syms, spaces, bid = sym_tables(ens)
+    R1, Y1 = random_R1(M, 5), random_sym(M, 6, scale=1e-3)
+    X, Y, rho = ens["X"][:n_cfg], ens["Y"][:n_cfg], ens["rho"][:n_cfg]
+    t0 = time.perf_counter()
+    if use_ref:
+        import contextlib
+        import io
+        import sscha_HP_odd  # the reference's own C module, built from source
+        f, d2v = np.zeros(M), np.zeros((M, M))
+        with contextlib.redirect_stdout(io.StringIO()):
+            sscha_HP_odd.GetPerturbAverageSym(X, Y, ens["w"], rho, R1, Y1, ens["T"], 1,
+                                              syms[0].shape[0], syms,
+                                              np.array([len(s) for s in spaces], np.intc),
+                                              spaces, bid, f, d2v)
+    else:
+        oracle.perturb_averages(X, Y, ens["w"], rho, R1, Y1, ens["T"], 1, syms, spaces, bid,
+                                n_threads=n_threads)
+    return time.perf_counter() - t0
+
+
+def cpu_impl():
+    """('reference', 1 thread) when the reference's C module is importable here, else the port."""
+    refdir = os.path.join(ROOT, "oracle", "_ref")
+    if os.path.isdir(refdir):
+        sys.path.insert(0, refdir)
+        try:
+            import sscha_HP_odd  # noqa: F401
+            return "reference"
+        except ImportError:
+            pass
+    return "port"
+
+
+def cpu_baseline(ens, target_s, apps_per_step, force_port=False):
+    import oracle
+    oracle.build()
+    N = ens["X"].shape[0]
+    kind = "port" if force_port else cpu_impl()
+    cores = 1 if kind == "reference" else (os.cpu_count() or 1)
+    n0 = min(N, max(cores, 16))
+    t0 = cpu_sample_time(ens, n0, cores, kind == "reference")
+    n = int(min(N, max(n0, n0 * target_s / max(t0, 1e-6))))
+    t = cpu_sample_time(ens, n, cores, kind == "reference") if n > n0 else t0
+    per_app = t * N / n
+    return {"value": 1.0 / (apps_per_step * per_app), "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": "perturbation averages over %d of %d configurations (%.1f s), scaled to "
+                      "%d applications per step; recurrence not included" % (n, N, t, apps_per_step)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    spec, ens = workload(args.workload)
+    import oracle
+    oracle.build()
+    kind = cpu_impl()
+    cores = 1 if kind == "reference" else (os.cpu_count() or 1)
+    N = ens["X"].shape[0]
+    n0 = min(N, max(cores, 16))
+    t0 = cpu_sample_time(ens, n0, cores, kind == "reference")
+    # each step: a sample of about 2 s, scaled to the full step
+    n = int(min(N, max(n0, n0 * 2.0 / max(t0, 1e-6))))
+    for _ in range(args.warmup):
+        cpu_sample_time(ens, n, cores, kind == "reference")
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += cpu_sample_time(ens, n, cores, kind == "reference")
+    step_s = 2 * (tot / args.steps) * N / n
+    value = 1.0 / step_s
+    sample = ("bi-Lanczos step = 2 perturbation-average calls; each timed step runs one call over "
+              "%d of %d configurations, scaled by N/%d and x2" % (n, N, n))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "M": spec["M"], "N": spec["N"],
+                       "n_syms": spec["n_syms"], "lanczos": "bi-Lanczos (2 applications/step)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU side
+KERNEL_NAMES = {0: "stageA (V = D Y1 + quadratic forms)", 1: "row scalars", 2: "force average",
+                3: "stageB (G = U^T W)", 4: "finalise", 5: "operand preparation"}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from tdscha_gb300 import _native as nat
+    from tdscha_gb300.synthetic import random_R1
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = nat.load()
+    spec, ens = workload(args.workload)
+    M, N = spec["M"], spec["N"]
+    prec_name = args.precision or "fp64"
+    prec = nat.PREC_MIXED if prec_name == "mixed" else nat.PREC_FP64
+    syms, spaces, bid = sym_tables(ens)
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=(prec_name == "mixed"))
+    ctx.set_options(False, False, False, False, False, 0.0)     # bi-Lanczos (normal repr.)
+    P = ctx.P
+    W, K = args.warmup, args.steps
+    cap = W + 2 * K + 4
+    dev = torch.device("cuda", local)
+    Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+    Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+    psi = np.zeros(P)
+    psi[:M] = random_R1(M, 11)
+    first = torch.from_numpy(psi / np.sqrt(psi.dot(psi))).to(dev)
+    Qd[0].copy_(first)
+    Pd[0].copy_(first)
+    hist = np.zeros(4 * cap)
+    hist[3] = 1.0
+    done = ctypes.c_int(0)
+    conv = ctypes.c_int(0)
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+
+    def steps(start, n):
+        nat.check(lib.tdscha_lanczos_run(ctx.handle, Qd.data_ptr(), Pd.data_ptr(), cap, start, n,
+                                         0, prec, 0, nat.dp(hist), ctypes.byref(done),
+                                         ctypes.byref(conv), st))
+        if conv.value or done.value != n:
+            raise RuntimeError("Lanczos converged early (%d of %d steps)" % (done.value, n))
+
+    steps(0, W)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    steps(W, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = ws * K / (ms / 1e3)
+
+    # per-kernel device time: the same K steps again with CUDA events around
+    # each kernel of the perturbation averages (kept out of the headline pass)
+    nat.check(lib.tdscha_ctx_profile(ctx.handle, 1))
+    steps(W + K, K)
+    torch.cuda.synchronize()
+    nat.check(lib.tdscha_ctx_profile(ctx.handle, 0))
+    kern = {}
+    for kid in range(6):
+        tot, cnt = ctypes.c_double(0), ctypes.c_int(0)
+        nat.check(lib.tdscha_ctx_profile_read(ctx.handle, kid, ctypes.byref(tot), ctypes.byref(cnt)))
+        if cnt.value:
+            kern[kid] = (tot.value, cnt.value)
+    ctx.close()
+    apps = 2 * K
+    R = N * spec["n_syms"]
+    flops_app = 4.0 * R * M * M          # two GEMM stages of 2 R M^2 each
+    # dominant kernel
+    kid = max(kern, key=lambda k: kern[k][0]) if kern else None
+    roof = None
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    if kid is not None:
+        tot_ms, cnt = kern[kid]
+        per_launch_s = tot_ms / cnt / 1e3
+        if kid in (0, 3):
+            work = 2.0 * R * M * M           # flops per launch of one GEMM stage
+            achieved = work / per_launch_s / 1e12
+            if prec_name == "fp64":
+                peak, src = 1.25, "nominal GB300 FP64 1.25 TFLOP/s (not in MEASURED_PEAKS.json)"
+            else:
+                peak = peaks.get("bf16_tflops", 1900.0)
+                src = "of measured bf16_tflops" if "bf16_tflops" in peaks else "of fallback"
+            roof = {"bound": "tensor" if prec_name == "mixed" else "fp64", "kernel": KERNEL_NAMES[kid],
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": None, "peak_source": src,
+                    "avg_launch_ms": tot_ms / cnt}
+        else:
+            nbytes = 2.0 * R * M * 8
+            achieved = nbytes / per_launch_s / 1e9
+            peak = peaks.get("hbm_gbs", 6800.0)
+            roof = {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                    "avg_launch_ms": tot_ms / cnt}
+    kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1]}
+               for k, v in kern.items()}
+    # kernels launched per step: per application (precision dependent) + recurrence
+    per_app = (len(kern) + 3) if prec_name == "fp64" else (len(kern) + 3)
+    gpu_launches = K * (2 * per_app + 5)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(ens, spec, prec_name, K, W)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(ens, 15.0, 2)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
+                "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "bf16x3+f64",
+                "data": "synthetic (seeded ensemble with the workload's shapes)",
+                "precision": prec_name,
+                "config": {"workload": args.workload, "M": M, "N": N, "n_syms": spec["n_syms"],
+                           "lanczos": "bi-Lanczos (2 applications/step)",
+                           "parallelism": "replicas" if ws > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (ensemble %.0f MB)" % (2 * R * M * 8 / 1e6)},
+                "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks, "gpu_launches": gpu_launches,
+                "flops_per_application": flops_app}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def measure_e2e(ens, spec, prec_name, K, W):
+    """Public API end to end: host ensemble -> Lanczos.run_FT(K) -> host coefficients."""
+    import torch
+    from tdscha_gb300.DynamicalLanczos import Lanczos
+    from tdscha_gb300.synthetic import random_R1
+    M = spec["M"]
+
+    def one(nsteps):
+        lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
+                                   use_wigner=False, precision=prec_name)
+        lanc.init(use_symmetries=False)
+        lanc.prepare_perturbation(random_R1(M, 11), masses_exp=0)
+        lanc.run_FT(nsteps, verbose=False)
+        g = lanc.get_green_function_continued_fraction(np.linspace(0, 600, 2000) / 109691.40235,
+                                                       smearing=5 / 109691.40235)
+        lanc._invalidate()
+        return g
+
+    one(min(W, 2))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    one(K)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    P = M + M * (M + 1)
+    h2d = (2 * ens["X"].size * 8 + ens["w"].size * 8 + ens["rho"].size * 8 + P * 8) / K
+    d2h = 16 * 8 + 2 * 2000 * 8 / K
+    return {"value": K / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "what": "Lanczos.from_arrays + init + prepare_perturbation + run_FT(K) + "
+                    "continued fraction on 2000 frequencies, ensemble upload included"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * tdscha_gb300 -- C ABI of the GB300 (sm_103a) Lanczos linear-response engine.
+ *
+ * Plain pointers and sizes only.  Every entry point returns 0 on success or a
+ * negative TDSCHA_ERR_* code (never exits the process); the message of the
+ * last failure on the calling thread is available from tdscha_last_error().
+ *
+ * Layouts follow the reference:
+ *   X, Y      : double[N][M] row-major (configuration-major), the ensemble's
+ *               displacements / forces in the mass-scaled polarisation basis
+ *               (Modules/DynamicalLanczos.py:446-452)
+ *   Y1, d2v   : double[M][M] row-major
+ *   psi       : double[M + M*(M+1)], sectors R | upper triangle | upper
+ *               triangle, triangles stored row by row from the diagonal
+ *               (Modules/DynamicalLanczos.py:3326-3345)
+ *   symmetry  : n_blocks degenerate blocks; block b has n_deg[b] modes listed
+ *               at deg_space[sum_{b'<b} n_deg[b']...]; its N_syms matrices
+ *               (N_syms, n_deg[b], n_deg[b]) are stored back to back in `sym`
+ *               in block order (the flattened form of the lists passed to
+ *               GetPerturbAverageSym, CModules/odd_corr_module.c:491-634);
+ *               blocks_ids[M] maps each mode to its block.
+ */
+#ifndef TDSCHA_GB300_H
+#define TDSCHA_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDSCHA_OK 0
+#define TDSCHA_ERR_ARG (-1)      /* bad argument (size, flag, pointer)          */
+#define TDSCHA_ERR_CUDA (-2)     /* CUDA runtime / driver failure               */
+#define TDSCHA_ERR_NAN (-3)      /* NaN met in the recurrence or input          */
+#define TDSCHA_ERR_STATE (-4)    /* call not valid in the context's state       */
+#define TDSCHA_ERR_TIMEOUT (-5)  /* a bounded device wait gave up               */
+
+/* precision of the perturbation averages */
+#define TDSCHA_PREC_FP64 0       /* float64 on the CUDA cores                   */
+#define TDSCHA_PREC_MIXED 1      /* split-bf16 x3 tensor-core GEMMs, fp32 accumulate */
+
+typedef struct tdscha_ctx tdscha_ctx;
+
+/* Text of the last error on this thread ("" if none). */
+const char *tdscha_last_error(void);
+
+/* Library version string. */
+const char *tdscha_version(void);
+
+/*
+ * One-shot drop-in for sscha_HP_odd.GetPerturbAverageSym
+ * (CModules/odd_corr_module.c:491-634, called from
+ * Modules/DynamicalLanczos.py:3114-3116): host buffers in, host buffers out.
+ * f_out[M] is overwritten; d2v_out[M*M] is overwritten with the D3 term and
+ * the D4 term is added when apply_D4 == 1 (LanczosFunctions.c:2741-2745).
+ * Uploads the ensemble, runs in float64 on the GPU, copies back.
+ */
+int tdscha_get_perturb_average_sym(int M, int N, const double *X, const double *Y,
+                                   const double *w, const double *rho,
+                                   const double *R1, const double *Y1, double T,
+                                   int apply_D4, int N_syms, int n_blocks,
+                                   const int *n_deg, const int *deg_space,
+                                   const double *sym, const int *blocks_ids,
+                                   double *f_out, double *d2v_out);
+
+/*
+ * Context: the ensemble uploaded once and kept resident in HBM, with the
+ * symmetry images, the per-mode Bose factors and (with_mixed != 0) the
+ * split-bf16 copies used by TDSCHA_PREC_MIXED.  Replaces the state the
+ * reference keeps in `Lanczos` (Modules/DynamicalLanczos.py:183-505, :694-871)
+ * and re-sends to the C module on every call.  Host pointers.
+ */
+int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X, const double *Y,
+                      const double *w, const double *rho, double T, int N_syms,
+                      int n_blocks, const int *n_deg, const int *deg_space,
+                      const double *sym, const int *blocks_ids, int with_mixed);
+int tdscha_ctx_destroy(tdscha_ctx *ctx);
+
+/*
+ * Flags of the operator (Modules/DynamicalLanczos.py:242-245, :2227-2253):
+ * use_wigner, ignore_harmonic, ignore_v3, ignore_v4, reverse_L, shift_value.
+ */
+int tdscha_ctx_set_options(tdscha_ctx *ctx, int use_wigner, int ignore_harmonic,
+                           int ignore_v3, int ignore_v4, int reverse_L, double shift_value);
+
+/*
+ * Perturbation averages on the resident ensemble: the context form of
+ * GetPerturbAverageSym.  R1[M], Y1[M*M] in; f_out[M], d2v_out[M*M] out, with
+ * the same overwrite/add convention as above.  device_ptrs != 0: all four
+ * pointers are device memory and the call is asynchronous on `stream`
+ * (a cudaStream_t, 0 = legacy default); otherwise host memory, synchronous.
+ */
+int tdscha_perturb_averages(tdscha_ctx *ctx, const double *R1, const double *Y1,
+                            int apply_D4, int precision, double *f_out, double *d2v_out,
+                            int device_ptrs, void *stream);
+
+/*
+ * psi_out = L psi_in (or L^T psi_in with transpose != 0): the harmonic part
+ * (apply_L1_FT, Modules/DynamicalLanczos.py:2287-2445), the anharmonic part
+ * (apply_anharmonic_FT, :2951-3363) and the reverse/shift (:3639-3641), as
+ * apply_full_L (:3549-3651) computes them.  Device pointers of length
+ * M + M*(M+1); asynchronous on `stream`.
+ */
+int tdscha_apply_full_L(tdscha_ctx *ctx, const double *psi_in, double *psi_out,
+                        int transpose, int precision, void *stream);
+
+/*
+ * Lanczos iterations (run_FT, Modules/DynamicalLanczos.py:5958-6497) with the
+ * reference's default n_rep_orth = 0 (no Gram-Schmidt), bi-Lanczos when
+ * run_simm == 0 and the symmetric Wigner Lanczos with the double-counting mask
+ * (mask_dot_wigner, :5905-5954) when run_simm != 0.
+ *
+ * basis_Q, basis_P: device buffers of (capacity) x P doubles; rows
+ *   0 .. start_step hold the Krylov vectors already computed (row 0 is the
+ *   normalised start vector, which the caller writes before the first call).
+ * hist: host double[4 * capacity] holding a_k, b_k, c_k, s_norm_k in rows of 4
+ *   for k < start_step (a, b, c) and k <= start_step (s_norm); the call
+ *   appends the new rows.  n_iter steps are attempted; *steps_done receives
+ *   the number of a_k appended and *converged 1 when |b| or |c| < 1e-12
+ *   stopped the run (the last step then appends only a_k, like the reference).
+ * full_reorth != 0 adds a full re-biorthogonalisation of each new pair of
+ *   vectors against the stored basis (not in the reference's default path).
+ */
+int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                       int start_step, int n_iter, int run_simm, int precision,
+                       int full_reorth, double *hist, int *steps_done, int *converged,
+                       void *stream);
+
+/*
+ * Continued-fraction Green function on the GPU, one thread per frequency
+ * (get_green_function_continued_fraction, Modules/DynamicalLanczos.py:
+ * 5032-5162).  a[n], b[n_b], c[n_c] host arrays; c is used when n_c == n_b,
+ * otherwise c = b.  w[n_w] in Ry (host); g_out: host interleaved complex
+ * (re, im) of length 2*n_w.
+ */
+int tdscha_continued_fraction(const double *a, int n, const double *b, int n_b,
+                              const double *c, int n_c, const double *w, int n_w,
+                              int use_wigner, double modulus, int reverse_L,
+                              double shift_value, int use_terminator, int last_average,
+                              double smearing, int smooth_ramp, double *g_out);
+
+/*
+ * Diagnostics (no counterpart in the reference): per-kernel CUDA-event timing
+ * of the perturbation averages.  enable != 0 clears and starts recording,
+ * 0 stops.  tdscha_ctx_profile_read returns the total device milliseconds and
+ * the launch count recorded for kernel_id: 0 stage A (quadratic forms),
+ * 1 row scalars, 2 force average, 3 stage B (weighted outer products),
+ * 4 finalisation, 5 operand preparation; it synchronises the device.
+ */
+int tdscha_ctx_profile(tdscha_ctx *ctx, int enable);
+int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, int *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDSCHA_GB300_H */

@@ -1,0 +1,645 @@
+"""GB300 drop-in for `tdscha.DynamicalLanczos.Lanczos` (Modules/DynamicalLanczos.py).
+
+The public surface keeps the reference's names, argument meanings and error
+behaviour: ensemble/perturbation setup, `init`, `prepare_perturbation`,
+`prepare_mode`, `prepare_two_ph`, `apply_full_L`, `run_FT`,
+`get_green_function_continued_fraction`, `save_status` / `load_status`,
+`save_abc` / `load_abc`, and the attributes `a_coeffs`, `b_coeffs`,
+`c_coeffs`, `basis_Q`, `basis_P`, `s_norm`, `psi`, `use_wigner`,
+`ignore_v3`, `ignore_v4`, `ignore_harmonic`, `reverse_L`, `shift_value`,
+`perturbation_modulus`.
+
+Every operator application and Lanczos step runs on the GPU through the
+C ABI of libtdscha_gb300.so (no CPU path).  The Krylov basis lives in device
+memory (torch tensors) and is copied to the host only when `basis_Q` /
+`basis_P` are read or a status is saved.
+
+Extra knobs: `precision` ("fp64" or "mixed": split-bf16 tensor-core
+perturbation averages with fp32 accumulation; the Lanczos recurrence stays
+in float64) and `Lanczos.from_arrays` for ensembles already projected on the
+mode basis.
+"""
+import os
+import time
+
+import numpy as np
+
+from . import _native as nat
+
+__EPSILON__ = 1e-12
+__RyToK__ = 157887.32400374097
+TYPE_DP = np.double
+
+MODE_SLOW_SERIAL = 0
+MODE_FAST_SERIAL = 1
+MODE_FAST_MPI = 2
+MODE_FAST_JULIA = 3
+MODE_GB300 = 4
+
+
+def f_ups(w, T):
+    """2 w / (1 + 2 n) (Modules/DynamicalLanczos.py:141-153)."""
+    n_w = bose_occupation(w, T)
+    return 2 * w / (1 + 2 * n_w)
+
+
+def bose_occupation(w, T):
+    n_w = 0
+    if T > 0:
+        n_w = 1 / (np.exp(w * __RyToK__ / T) - 1)
+    return n_w
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("tdscha_gb300 needs a CUDA GPU (no CPU fallback)")
+    return torch
+
+
+class Lanczos(object):
+    def __init__(self, ensemble=None, mode=None, unwrap_symmetries=False, select_modes=None,
+                 use_wigner=True, lo_to_split="random", precision="fp64"):
+        self.mode = MODE_GB300 if mode is None else mode
+        self.verbose = True
+        self.T = 0
+        self.nat = 0
+        self.m = []
+        self.w = []
+        self.pols = []
+        self.n_modes = 0
+        self.ignore_harmonic = False
+        self.ignore_v3 = False
+        self.ignore_v4 = False
+        self.N = 0
+        self.rho = []
+        self.N_eff = 0
+        self.X = []
+        self.Y = []
+        self.psi = []
+        self.eigvals = None
+        self.eigvects = None
+        self.a_coeffs = []
+        self.b_coeffs = []
+        self.c_coeffs = []
+        self.krilov_basis = []
+        self.s_norm = []
+        self.arnoldi_matrix = []
+        self.reverse_L = False
+        self.shift_value = 0
+        self.symmetrize = False
+        self.symmetries = None
+        self.degenerate_space = None
+        self.N_degeneracy = None
+        self.initialized = False
+        self.perturbation_modulus = 1
+        self.sym_block_id = None
+        self.n_syms = 1
+        self.sym_julia = None
+        self.deg_julia = None
+        self.gamma_only = False
+        self.use_wigner = use_wigner
+        self.ignore_small_w = False
+        self.unwrapped = False
+        self.precision = precision
+        self.full_reorth = False
+        self._ctx = None
+        self._ctx_key = None
+        self._Qd = None
+        self._Pd = None
+        self._basis_host = None
+        if ensemble is not None:
+            self._init_from_ensemble(ensemble, unwrap_symmetries, select_modes, lo_to_split)
+
+    # ------------------------------------------------------------------ setup
+    @classmethod
+    def from_arrays(cls, X, Y, w, rho, T, pols=None, m=None, use_wigner=True, precision="fp64"):
+        """Ensemble already in the mass-scaled mode basis: X, Y (N, M), w (M) in Ry."""
+        self = cls(use_wigner=use_wigner, precision=precision)
+        self.set_ensemble(X, Y, w, rho, T, pols, m)
+        return self
+
+    def set_ensemble(self, X, Y, w, rho, T, pols=None, m=None):
+        X = np.ascontiguousarray(X, dtype=TYPE_DP)
+        Y = np.ascontiguousarray(Y, dtype=TYPE_DP)
+        if X.ndim != 2 or X.shape != Y.shape:
+            raise ValueError("X and Y must have the same (N, n_modes) shape")
+        self.X, self.Y = X, Y
+        self.N, self.n_modes = X.shape
+        self.w = np.asarray(w, dtype=TYPE_DP).copy()
+        self.rho = np.asarray(rho, dtype=TYPE_DP).copy()
+        self.N_eff = np.sum(self.rho)
+        self.T = float(T)
+        M = self.n_modes
+        self.pols = np.eye(M) if pols is None else np.asarray(pols, dtype=TYPE_DP)
+        self.m = np.ones(self.pols.shape[0]) if m is None else np.asarray(m, dtype=TYPE_DP)
+        self.nat = self.pols.shape[0] // 3
+        self.psi = np.zeros(M + M * (M + 1), dtype=TYPE_DP)
+        self._invalidate()
+
+    def _init_from_ensemble(self, ensemble, unwrap_symmetries, select_modes, lo_to_split):
+        """Project a python-sscha ensemble on the modes (DynamicalLanczos.py:300-452)."""
+        import cellconstructor as CC  # noqa: F401  (physics deps of the reference)
+        import cellconstructor.Methods
+        import sscha.Ensemble as Ensemble
+        dyn = ensemble.current_dyn.Copy()
+        super_structure = dyn.structure.generate_supercell(dyn.GetSupercell())
+        ws, pols = dyn.DiagonalizeSupercell(lo_to_split=lo_to_split)
+        nat_sc = super_structure.N_atoms
+        m = super_structure.get_masses_array()
+        mm = np.tile(m, (3, 1)).T.ravel()
+        trans_mask = CC.Methods.get_translations(pols, m)
+        good = ~trans_mask
+        if select_modes is not None:
+            good = good & np.asarray(select_modes, dtype=bool)
+        w = ws[good]
+        pols = pols[:, good]
+        N = ensemble.N
+        rho = ensemble.rho.copy()
+        u = ensemble.u_disps / Ensemble.Bohr
+        f = ensemble.forces.reshape(N, 3 * nat_sc).copy()
+        f -= ensemble.sscha_forces.reshape(N, 3 * nat_sc)
+        f_mean = ensemble.get_average_forces(get_error=False)
+        qe_sym = CC.symmetries.QE_Symmetry(dyn.structure)
+        qe_sym.SetupQPoint()
+        qe_sym.SymmetrizeVector(f_mean)
+        f_mean = np.tile(f_mean, (np.prod(ensemble.current_dyn.GetSupercell()), 1)).ravel()
+        f_mean *= Ensemble.Bohr
+        f *= Ensemble.Bohr
+        if unwrap_symmetries:
+            u, f, rho = ensemble.get_unwrapped_ensemble()
+            N = len(rho)
+            self.unwrapped = True
+            u /= Ensemble.Bohr
+            f *= Ensemble.Bohr
+        f[:, :] -= np.tile(f_mean, (N, 1))
+        u *= np.tile(np.sqrt(mm), (N, 1))
+        f /= np.tile(np.sqrt(mm), (N, 1))
+        self.dyn = dyn
+        self.set_ensemble(u.dot(pols), f.dot(pols), w, rho, ensemble.current_T, pols, mm)
+        self.nat = nat_sc
+
+    def _invalidate(self):
+        if self._ctx is not None:
+            self._ctx.close()
+        self._ctx = None
+        self._ctx_key = None
+
+    def reset(self):
+        """Reset the Lanczos state keeping ensemble and options (:527-557)."""
+        M = self.n_modes
+        self.psi = np.zeros(M + M * (M + 1), dtype=TYPE_DP)
+        self.eigvals = None
+        self.eigvects = None
+        self.a_coeffs = []
+        self.b_coeffs = []
+        self.c_coeffs = []
+        self.basis_P = []
+        self.basis_Q = []
+        self.s_norm = []
+        self.krilov_basis = []
+        self.arnoldi_matrix = []
+
+    def init(self, use_symmetries=True, symmetries=None):
+        """Allocate psi and prepare the symmetry tables (:564-582)."""
+        M = self.n_modes
+        self.psi = np.zeros(M + M * (M + 1), dtype=TYPE_DP)
+        self.prepare_symmetrization(no_sym=not use_symmetries, symmetries=symmetries)
+        self.initialized = True
+
+    def prepare_symmetrization(self, no_sym=False, verbose=True, symmetries=None):
+        """Mode-space symmetry blocks (:694-871).
+
+        `symmetries` may be a (symmetries, degenerate_space) pair of per-block
+        lists already in the mode basis (what CC.symmetries.GetSymmetriesOnModesDeg
+        returns).  Without it, and without no_sym, the reference asks spglib
+        for the supercell symmetries; that needs cellconstructor and spglib.
+        """
+        self.initialized = True
+        M = self.n_modes
+        if no_sym or self.unwrapped:
+            self.set_symmetries([np.ones((1, 1, 1), dtype=np.double)] * M,
+                                [np.array([i], dtype=np.intc) for i in range(M)])
+            return
+        if symmetries is None:
+            import spglib
+            import cellconstructor as CC
+            import cellconstructor.symmetries
+            super_structure = self.dyn.structure.generate_supercell(self.dyn.GetSupercell())
+            super_symmetries = CC.symmetries.GetSymmetriesFromSPGLIB(
+                spglib.get_symmetry(super_structure.get_spglib_cell()), False)
+            pol_syms, basis = CC.symmetries.GetSymmetriesOnModesDeg(super_symmetries,
+                                                                    super_structure, self.pols,
+                                                                    self.w)
+            self.set_symmetries(pol_syms, basis)
+            return
+        syms, basis = symmetries
+        self.set_symmetries(syms, basis)
+
+    def set_symmetries(self, symmetries, degenerate_space, sym_block_id=None):
+        M = self.n_modes
+        self.symmetries = [np.ascontiguousarray(s, dtype=np.double) for s in symmetries]
+        self.degenerate_space = [np.array(x, dtype=np.intc) for x in degenerate_space]
+        self.N_degeneracy = np.array([len(x) for x in self.degenerate_space], dtype=np.intc)
+        if sym_block_id is None:
+            sym_block_id = -np.ones(M, dtype=np.intc)
+            for j, block in enumerate(self.degenerate_space):
+                sym_block_id[block] = j
+            if np.any(sym_block_id < 0):
+                raise ValueError("Error, something went wrong during the symmetrization")
+        self.sym_block_id = np.asarray(sym_block_id, dtype=np.intc)
+        self.n_syms = self.symmetries[0].shape[0]
+        self.initialized = True
+        self._invalidate()
+
+    # -------------------------------------------------------- perturbations
+    def prepare_perturbation(self, vector, masses_exp=1, add=False):
+        """psi[:M] (+)= sum_a v_a e_mu^a sqrt(m_a)^masses_exp (:2023-2075)."""
+        if not add:
+            self.reset()
+            self.psi = np.zeros(self.psi.shape, dtype=TYPE_DP)
+        m_on = np.sqrt(self.m) ** masses_exp
+        new_v = np.einsum("a, a, ab->b", m_on, vector, self.pols)
+        self.psi[: self.n_modes] += new_v
+        self.perturbation_modulus = new_v.dot(new_v)
+
+    def prepare_mode(self, index):
+        """Unit perturbation on one mode (:2077-2091)."""
+        self.reset()
+        self.psi[:] = 0
+        self.psi[index] = 1
+        self.perturbation_modulus = 1
+
+    def prepare_two_ph(self, a, b):
+        """Two-phonon perturbation, Wigner only (:2095-2145)."""
+        if not self.use_wigner:
+            raise NotImplementedError("The two phonon response is available only in Wigner")
+        if a > self.n_modes or b > self.n_modes:
+            raise ValueError("The a-b indices must be smaller than {}".format(self.n_modes))
+        self.reset()
+        self.psi[:] = 0
+        chi_plus = self.get_chi_plus()
+        chi_minus = self.get_chi_minus()
+        mat = np.zeros((self.n_modes, self.n_modes))
+        mat[a, b] = 0.5
+        mat[b, a] += 0.5
+        pert_a = -np.sqrt(-0.5 * chi_minus) * mat
+        pert_b = +np.sqrt(+0.5 * chi_plus) * mat
+        iu = np.triu_indices(self.n_modes)
+        h = len(iu[0])
+        M = self.n_modes
+        self.psi[M:M + h] = pert_a[iu]
+        self.psi[M + h:] = pert_b[iu]
+        self.perturbation_modulus = self.psi.dot(self.psi * self.mask_dot_wigner())
+
+    def set_max_frequency(self, freq):
+        """Reverse-and-shift setup (:2227-2253)."""
+        self.shift_value = 4 * freq * freq
+        self.reverse_L = True
+
+    # ------------------------------------------------------ host helpers
+    def _bose_matrix(self):
+        M = self.n_modes
+        w = np.tile(self.w, (M, 1))
+        n = np.zeros((M, M), dtype=np.double)
+        if self.T > __EPSILON__:
+            n = 1.0 / (np.exp(w * 157887.32400374097 / self.T) - 1.0)
+        return w, n
+
+    def get_chi_minus(self):
+        w, n = self._bose_matrix()
+        return (w - w.T) * (n - n.T) / (2. * w * w.T)
+
+    def get_chi_plus(self):
+        w, n = self._bose_matrix()
+        return (w + w.T) * (1 + n + n.T) / (2. * w * w.T)
+
+    def mask_dot_wigner(self, debug=False):
+        M = self.n_modes
+        mask = np.ones(M + M * (M + 1))
+        r, c = np.triu_indices(M)
+        h = len(r)
+        mask[M:M + h][r < c] = 2
+        mask[M + h:][r < c] = 2
+        return mask
+
+    def _sym_from_sector(self, start, half_off_diagonal):
+        M = self.n_modes
+        h = M * (M + 1) // 2
+        A = np.zeros((M, M))
+        iu = np.triu_indices(M)
+        A[iu] = self.psi[start:start + h]
+        A.T[iu] = self.psi[start:start + h]
+        if half_off_diagonal:
+            nm = np.ones((M, M)) / 2
+            np.fill_diagonal(nm, 1)
+            A *= nm
+        return A
+
+    def get_Y1(self, half_off_diagonal=False):
+        return self._sym_from_sector(self.n_modes, half_off_diagonal)
+
+    def get_ReA1(self, half_off_diagonal=False):
+        return self._sym_from_sector(self.n_modes + self.n_modes * (self.n_modes + 1) // 2,
+                                     half_off_diagonal)
+
+    # ------------------------------------------------------------ device side
+    def _context(self):
+        if not self.initialized:
+            raise ValueError("Error, this class must be initialized before lunching the "
+                             "computation:\n Use the .init()")
+        want_mixed = self.precision == "mixed"
+        key = (id(self.X), id(self.Y), id(self.rho), self.T, id(self.symmetries))
+        if self._ctx is not None and (self._ctx_key != key or (want_mixed and not self._ctx.with_mixed)):
+            self._invalidate()
+        if self._ctx is None:
+            _torch()
+            self._ctx = nat.Context(self.X, self.Y, self.w, self.rho, self.T, self.symmetries,
+                                    self.degenerate_space, self.sym_block_id,
+                                    with_mixed=want_mixed)
+            self._ctx_key = key
+        self._ctx.set_options(self.use_wigner, self.ignore_harmonic, self.ignore_v3,
+                              self.ignore_v4, self.reverse_L, self.shift_value)
+        return self._ctx
+
+    def _prec(self):
+        if self.precision == "fp64":
+            return nat.PREC_FP64
+        if self.precision == "mixed":
+            return nat.PREC_MIXED
+        raise ValueError("precision must be 'fp64' or 'mixed', got %r" % (self.precision,))
+
+    def _apply_dev(self, psi, transpose, ignore_harmonic=None, ignore_v3=None, plain=False):
+        torch = _torch()
+        ctx = self._context()
+        if ignore_harmonic is not None or ignore_v3 is not None or plain:
+            ctx.set_options(self.use_wigner,
+                            self.ignore_harmonic if ignore_harmonic is None else ignore_harmonic,
+                            self.ignore_v3 if ignore_v3 is None else ignore_v3, self.ignore_v4,
+                            False if plain else self.reverse_L, 0 if plain else self.shift_value)
+        x = torch.as_tensor(np.ascontiguousarray(psi, dtype=np.float64)).cuda()
+        y = torch.empty_like(x)
+        st = torch.cuda.current_stream().cuda_stream
+        nat.check(nat.load().tdscha_apply_full_L(ctx.handle, x.data_ptr(), y.data_ptr(),
+                                                 1 if transpose else 0, self._prec(), st))
+        out = y.cpu().numpy()
+        return out
+
+    def apply_L1_FT(self, transpose=False):
+        """Harmonic part only, on self.psi (:2287-2445)."""
+        return self._apply_dev(self.psi, transpose, ignore_v3=True, plain=True)
+
+    def apply_anharmonic_FT(self, transpose=False, test_weights=False, use_old_version=False):
+        """Anharmonic part only, on self.psi (:2951-3363)."""
+        return self._apply_dev(self.psi, transpose, ignore_harmonic=True, ignore_v3=False,
+                               plain=True)
+
+    def apply_full_L(self, target=None, force_t_0=False, force_FT=True, transpose=False,
+                     fast_lanczos=True):
+        """psi <- L psi on the GPU (:3549-3651); overwrites and returns self.psi."""
+        if force_t_0 and force_FT:
+            raise ValueError("Error, only one between force_t_0 and force_FT can be True")
+        if target is not None:
+            self.psi = target
+        out = self._apply_dev(self.psi, transpose)
+        self.psi = out
+        return self.psi
+
+    def get_perturb_averages(self, R1, Y1, apply_d4=True):
+        """(f_pert_av, d2v_pert_av) of the resident ensemble (GetPerturbAverageSym)."""
+        ctx = self._context()
+        R1 = nat.f64(R1)
+        Y1 = nat.f64(Y1)
+        f = np.zeros(self.n_modes)
+        d2v = np.zeros((self.n_modes, self.n_modes))
+        nat.check(nat.load().tdscha_perturb_averages(ctx.handle, R1.ctypes.data, Y1.ctypes.data,
+                                                     1 if apply_d4 else 0, self._prec(),
+                                                     f.ctypes.data, d2v.ctypes.data, 0, None))
+        return f, d2v
+
+    # ------------------------------------------------------------- Krylov
+    @property
+    def basis_Q(self):
+        self._sync_basis()
+        return self._basis_host[0]
+
+    @basis_Q.setter
+    def basis_Q(self, v):
+        self._sync_basis(drop_device=True)
+        self._basis_host = (list(v), self._basis_host[1] if self._basis_host else [])
+
+    @property
+    def basis_P(self):
+        self._sync_basis()
+        return self._basis_host[1]
+
+    @basis_P.setter
+    def basis_P(self, v):
+        self._sync_basis(drop_device=True)
+        self._basis_host = (self._basis_host[0] if self._basis_host else [], list(v))
+
+    def _sync_basis(self, drop_device=False):
+        if getattr(self, "_Qd", None) is not None:
+            n = self._nbasis
+            Q = self._Qd[:n].cpu().numpy()
+            Pm = self._Pd[:n].cpu().numpy()
+            self._basis_host = ([q for q in Q], [p for p in Pm])
+            if drop_device:
+                self._Qd = self._Pd = None
+        elif getattr(self, "_basis_host", None) is None:
+            self._basis_host = ([], [])
+
+    def run_FT(self, n_iter, save_dir=None, save_each=5, verbose=True, n_rep_orth=0, n_ortho=10,
+               flush_output=True, debug=False, prefix="LANCZOS", run_simm=None, optimized=False):
+        """Lanczos iterations on the GPU (:5958-6497).
+
+        n_rep_orth > 0 enables one pass of full re-biorthogonalisation of each
+        new pair against the whole stored basis (the reference's own
+        Gram-Schmidt loop is not reproduced); the default 0 matches the
+        reference's default run.
+        """
+        self.verbose = verbose
+        if not self.initialized:
+            self.prepare_symmetrization()
+        if self.psi is None:
+            raise ValueError("Error, you must initialize a perturbation to start the Lanczos.")
+        psi_norm = np.sum(np.asarray(self.psi) ** 2)
+        if np.isnan(psi_norm) or psi_norm == 0:
+            raise ValueError("Error, you must initialize a perturbation to start the Lanczos.\n"
+                             "Use prepare_raman/ir or prepare_perturbation before calling the run method.")
+        if save_dir is not None and not os.path.exists(save_dir):
+            os.makedirs(save_dir)
+        if run_simm is None:
+            run_simm = self.use_wigner
+        if run_simm and not self.use_wigner:
+            raise NotImplementedError("The symmetric Lanczos works only with Wigner. Set "
+                                      "use_wigner to True")
+        torch = _torch()
+        ctx = self._context()
+        P = ctx.P
+        i_step = len(self.a_coeffs)
+        mask = self.mask_dot_wigner() if run_simm else None
+        dev = torch.device("cuda")
+        if i_step == 0:
+            psi = np.asarray(self.psi, dtype=np.float64)
+            if not run_simm:
+                first = psi / np.sqrt(psi.dot(psi))
+            else:
+                first = psi / np.sqrt(psi.dot(psi * mask))
+            self.s_norm = [1]
+            rows_Q = [first]
+            rows_P = [first]
+        else:
+            if len(self.b_coeffs) != len(self.c_coeffs):
+                raise AssertionError("Something wrong when restoring the Lanczos. len b = {} len c = {}"
+                                     .format(len(self.b_coeffs), len(self.c_coeffs)))
+            rows_Q = rows_P = None
+        cap = i_step + n_iter + 2
+        if i_step == 0 or self._Qd is None or self._Qd.shape[0] < cap:
+            Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+            Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+            if i_step == 0:
+                Qd[0].copy_(torch.from_numpy(rows_Q[0]))
+                Pd[0].copy_(torch.from_numpy(rows_P[0]))
+            elif self._Qd is not None:
+                Qd[: self._nbasis].copy_(self._Qd[: self._nbasis])
+                Pd[: self._nbasis].copy_(self._Pd[: self._nbasis])
+            else:
+                Qh = np.asarray(self._basis_host[0], dtype=np.float64)
+                Ph = np.asarray(self._basis_host[1], dtype=np.float64)
+                Qd[: len(Qh)].copy_(torch.from_numpy(Qh))
+                Pd[: len(Ph)].copy_(torch.from_numpy(Ph))
+            self._Qd, self._Pd = Qd, Pd
+        self._nbasis = i_step + 1
+        self._basis_host = None
+        hist = np.zeros(4 * cap, dtype=np.float64)
+        for k, a in enumerate(self.a_coeffs):
+            hist[4 * k] = a
+        for k, b in enumerate(self.b_coeffs):
+            hist[4 * k + 1] = b
+        for k, c in enumerate(self.c_coeffs):
+            hist[4 * k + 2] = c
+        for k, s in enumerate(list(self.s_norm)[: i_step + 1]):
+            hist[4 * k + 3] = s
+        steps_done = nat.ctypes.c_int(0)
+        conv = nat.ctypes.c_int(0)
+        st = torch.cuda.current_stream().cuda_stream
+        reorth = 1 if (n_rep_orth > 0 or self.full_reorth) else 0
+        chunk = save_each if save_dir is not None else n_iter
+        done = 0
+        converged = False
+        while done < n_iter and not converged:
+            todo = min(chunk, n_iter - done)
+            start = i_step + done
+            t0 = time.time()
+            nat.check(nat.load().tdscha_lanczos_run(
+                ctx.handle, self._Qd.data_ptr(), self._Pd.data_ptr(), cap, start, todo,
+                1 if run_simm else 0, self._prec(), reorth, nat.dp(hist),
+                nat.ctypes.byref(steps_done), nat.ctypes.byref(conv), st))
+            n = steps_done.value
+            for k in range(start, start + n):
+                self.a_coeffs.append(float(hist[4 * k]))
+                if conv.value and k == start + n - 1:
+                    break
+                self.b_coeffs.append(float(hist[4 * k + 1]))
+                self.c_coeffs.append(float(hist[4 * k + 2]))
+                self.s_norm.append(float(hist[4 * (k + 1) + 3]))
+                self._nbasis = k + 2
+            converged = bool(conv.value)
+            done += n
+            if verbose:
+                print("Lanczos steps %d-%d in %.3f s" % (start + 1, start + n, time.time() - t0))
+            if save_dir is not None and not converged and (start + n) % save_each == 0:
+                self.save_status("%s/%s_STEP%d" % (save_dir, prefix, start + n))
+        if converged and verbose:
+            print("   last a coeff = {}".format(self.a_coeffs[-1]))
+
+    def get_green_function_continued_fraction(self, w_array, use_terminator=True, last_average=1,
+                                              smearing=0, smooth_ramp=0):
+        """G(w) by the continued fraction, evaluated on the GPU (:5032-5162)."""
+        w_array = np.ascontiguousarray(w_array, dtype=np.float64)
+        a = np.ascontiguousarray(self.a_coeffs, dtype=np.float64)
+        b = np.ascontiguousarray(self.b_coeffs, dtype=np.float64)
+        c = np.ascontiguousarray(self.c_coeffs, dtype=np.float64)
+        if len(a) == 0:
+            raise ValueError("no Lanczos coefficients")
+        out = np.zeros(2 * w_array.size, dtype=np.float64)
+        nat.check(nat.load().tdscha_continued_fraction(
+            nat.dp(a), len(a), nat.dp(b), len(b), nat.dp(c), len(c),
+            nat.dp(w_array.ravel()), w_array.size, 1 if self.use_wigner else 0,
+            float(self.perturbation_modulus), 1 if self.reverse_L else 0,
+            float(self.shift_value), 1 if use_terminator else 0, int(last_average),
+            float(smearing), int(smooth_ramp), nat.dp(out)))
+        return (out[0::2] + 1j * out[1::2]).reshape(w_array.shape)
+
+    # ------------------------------------------------------------ I/O
+    def save_abc(self, file):
+        total = len(self.a_coeffs)
+        abc = np.zeros((total, 3), dtype=np.double)
+        abc[:, 0] = self.a_coeffs
+        abc[: len(self.b_coeffs), 1] = self.b_coeffs
+        abc[: len(self.c_coeffs), 2] = self.c_coeffs
+        np.savetxt(file, abc, header="a; b; c")
+
+    def load_abc(self, file):
+        abc = np.loadtxt(file)
+        self.a_coeffs = abc[:, 0]
+        self.b_coeffs = abc[:, 1]
+        self.c_coeffs = abc[:, 2]
+
+    def save_status(self, file):
+        """npz with the reference's key set (:3678-3727)."""
+        if ".npz" not in file.lower():
+            file += ".npz"
+        np.savez_compressed(file, T=self.T, nat=self.nat, m=self.m, w=self.w, pols=self.pols,
+                            n_modes=self.n_modes, ignore_v3=self.ignore_v3,
+                            ignore_v4=self.ignore_v4, N=self.N, rho=self.rho, X=self.X, Y=self.Y,
+                            psi=self.psi, a_coeffs=self.a_coeffs, b_coeffs=self.b_coeffs,
+                            c_coeffs=self.c_coeffs, basis_Q=np.asarray(self.basis_Q),
+                            basis_P=np.asarray(self.basis_P), s_norm=self.s_norm,
+                            krilov_basis=self.krilov_basis, arnoldi_matrix=self.arnoldi_matrix,
+                            reverse=self.reverse_L, shift=self.shift_value,
+                            perturbation_modulus=self.perturbation_modulus,
+                            use_wigner=self.use_wigner, ignore_small_w=self.ignore_small_w,
+                            sym_julia=self.sym_julia, deg_julia=self.deg_julia,
+                            n_syms=self.n_syms)
+
+    def load_status(self, file, is_file_instance=False):
+        """Restore a status written by save_status (this class's or the reference's)."""
+        if not is_file_instance:
+            if ".npz" not in file.lower():
+                file += ".npz"
+            if not os.path.exists(file):
+                raise IOError("Error while loading %s" % file)
+        data = dict(np.load(file, allow_pickle=True))
+        self.T = np.double(data["T"])
+        self.nat = int(data["nat"])
+        self.m = data["m"]
+        self.w = data["w"]
+        self.pols = data["pols"]
+        self.n_modes = int(data["n_modes"])
+        self.ignore_v3 = bool(data["ignore_v3"])
+        self.ignore_v4 = bool(data["ignore_v4"])
+        self.N = int(data["N"])
+        self.rho = data["rho"]
+        self.N_eff = np.sum(self.rho)
+        self.X = np.ascontiguousarray(data["X"])
+        self.Y = np.ascontiguousarray(data["Y"])
+        self.psi = data["psi"]
+        self.a_coeffs = list(data["a_coeffs"])
+        self.b_coeffs = list(data["b_coeffs"])
+        self.c_coeffs = list(data["c_coeffs"]) if "c_coeffs" in data else []
+        self.krilov_basis = data["krilov_basis"]
+        self.arnoldi_matrix = data["arnoldi_matrix"]
+        self.n_syms = int(data["n_syms"]) if "n_syms" in data else 1
+        self._Qd = self._Pd = None
+        self._basis_host = (list(data["basis_Q"]), list(data["basis_P"]))
+        self.s_norm = list(data["s_norm"])
+        self.use_wigner = bool(data["use_wigner"])
+        self.ignore_small_w = bool(data.get("ignore_small_w", False))
+        if "reverse" in data:
+            self.reverse_L = bool(data["reverse"])
+            self.shift_value = float(data["shift"])
+        if "perturbation_modulus" in data:
+            self.perturbation_modulus = float(data["perturbation_modulus"])
+        self._invalidate()

@@ -1,0 +1,154 @@
+// Internal declarations shared by the translation units of libtdscha_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/tdscha_gb300.h"
+
+namespace tdscha {
+
+constexpr double kRyToK = 157887.32400374097;   // LanczosFunctions.h:9
+constexpr double kEps = 1e-12;                   // DynamicalLanczos.py:121
+
+void set_error(const char *fmt, ...);
+
+#define TDS_CUDA(call)                                                               \
+    do {                                                                             \
+        cudaError_t _e = (call);                                                     \
+        if (_e != cudaSuccess) {                                                     \
+            ::tdscha::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,           \
+                                cudaGetErrorString(_e));                             \
+            return TDSCHA_ERR_CUDA;                                                  \
+        }                                                                            \
+    } while (0)
+
+#define TDS_CHECK_LAUNCH()                                                           \
+    do {                                                                             \
+        cudaError_t _e = cudaGetLastError();                                         \
+        if (_e != cudaSuccess) {                                                     \
+            ::tdscha::set_error("%s:%d launch: %s", __FILE__, __LINE__,              \
+                                cudaGetErrorString(_e));                             \
+            return TDSCHA_ERR_CUDA;                                                  \
+        }                                                                            \
+    } while (0)
+
+#define TDS_TRY(expr)                                                                \
+    do {                                                                             \
+        int _rc = (expr);                                                            \
+        if (_rc != TDSCHA_OK) return _rc;                                            \
+    } while (0)
+
+// Split-bf16 copies of the ensemble used by the tensor-core path.  Rows are
+// image rows r = i*S + j (configuration-major, like the reference's bigindex,
+// tdscha_core.jl:212-238).  Mp is M padded to the tile width; Rp is R padded
+// to the K block of the second GEMM.
+struct MixedStore {
+    int Mp = 0;
+    long Rp = 0;
+    // row layout (R x Mp): A operand of V = D Y1, and the epilogue's rows
+    __nv_bfloat16 *d_hi = nullptr, *d_lo = nullptr;
+    float *d32 = nullptr;    // d rows (fp32 value hi+lo)      R x Mp
+    float *g32 = nullptr;    // g = f_psi * f rows (fp32)      R x Mp
+    // transposed layout (Mp x Rp): operands of G = U^T W
+    __nv_bfloat16 *ut_hi = nullptr, *ut_lo = nullptr;   // U^T, U = f_Y * D
+    float *ft32 = nullptr;                               // F^T (fp32)
+    float *ut32 = nullptr;                               // U^T (fp32 value hi+lo)
+    __nv_bfloat16 *wt_hi = nullptr, *wt_lo = nullptr;   // W^T, rebuilt per call
+    __nv_bfloat16 *y1_hi = nullptr, *y1_lo = nullptr;   // Y1 (Mp x Mp), per call
+    float *qp = nullptr;          // per-column-tile partial q, p  (ntile x 2 x R)
+    float *gpart = nullptr;       // split-K partial G            (nsplit x Mp x Mp)
+    int nsplit = 0;
+    int nctile = 0;
+    void *tmaps = nullptr;        // device copy of the TMA descriptors
+    std::vector<uint8_t> tmaps_host;
+    int *err_flag = nullptr;      // bounded-wait failure flag (device)
+};
+
+}  // namespace tdscha
+
+struct tdscha_ctx {
+    int device = 0;
+    int M = 0, N = 0, S = 0;
+    long R = 0;                 // image rows N*S
+    long P = 0;                 // psi length M + M(M+1)
+    long H = 0;                 // M(M+1)/2
+    double T = 0, sum_rho = 0;  // sum_rho accumulated in config order
+    int with_mixed = 0;
+    // operator options
+    int use_wigner = 1, ignore_harmonic = 0, ignore_v3 = 0, ignore_v4 = 0, reverse_L = 0;
+    double shift = 0;
+    // per-mode (device)
+    double *w = nullptr, *fY = nullptr, *fpsi = nullptr, *rho = nullptr;
+    double *Yw = nullptr, *ReAw = nullptr;     // equilibrium Upsilon / ReA eigenvalues
+    // image rows (device), R x M
+    double *D = nullptr, *F = nullptr;
+    // per-pair coefficients (device), length H, rebuilt by set_options
+    double *pc = nullptr;       // 10 arrays of H: see lanczos.cu
+    // per-application scratch (device)
+    double *R1 = nullptr, *Y1 = nullptr, *f = nullptr, *d2v = nullptr;
+    double *qp_part = nullptr;  // fp64 path: nct x 2 x R
+    double *alpha = nullptr, *beta = nullptr, *c1 = nullptr, *c2 = nullptr;   // R each
+    double *gpart = nullptr;    // fp64 path: nsplit x M x M
+    double *fpart = nullptr;    // nfchunk x M
+    int nct64 = 0, nsplit64 = 0, nfchunk = 0;
+    // Lanczos work vectors (device), P each
+    double *Lq = nullptr, *pL = nullptr, *rk = nullptr, *sk = nullptr;
+    double *mask = nullptr;     // Wigner double-counting mask (P)
+    double *dots = nullptr;     // block partials of the fused dot kernels
+    double *scal = nullptr;     // device scalars of the recurrence
+    double *hist_dev = nullptr; // device copy of the coefficient history
+    int hist_cap = 0;
+    double *host_pinned = nullptr;
+    int nblk_dot = 0;
+    tdscha::MixedStore mx;
+    // diagnostics: CUDA-event pairs per kernel id while profiling is on
+    int prof = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[8];
+};
+
+namespace tdscha {
+
+// perturb_fp64.cu
+int perturb_fp64(tdscha_ctx *c, int apply_d4, cudaStream_t st);
+int alloc_fp64_scratch(tdscha_ctx *c);
+// perturb_mixed.cu
+int mixed_prepare(tdscha_ctx *c);
+int mixed_release(tdscha_ctx *c);
+int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st);
+// lanczos.cu
+int build_pair_coeffs(tdscha_ctx *c);
+int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,
+                     int precision, cudaStream_t st);
+// shared: f / d2v finalisation from the row scalars and G partials
+int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t st);
+
+inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Bracket a launch with CUDA events when profiling is on.
+struct ProfScope {
+    tdscha_ctx *c;
+    int id;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    ProfScope(tdscha_ctx *c_, int id_, cudaStream_t st_) : c(c_), id(id_), st(st_) {
+        if (c->prof) {
+            cudaEventCreate(&a);
+            cudaEventRecord(a, st);
+        }
+    }
+    ~ProfScope() {
+        if (c->prof && a) {
+            cudaEvent_t b;
+            cudaEventCreate(&b);
+            cudaEventRecord(b, st);
+            c->prof_ev[id].push_back({a, b});
+        }
+    }
+};
+
+}  // namespace tdscha

@@ -1,0 +1,580 @@
+// The operator around the perturbation averages and the Krylov driver, all in
+// float64 on the GPU:
+//   * psi -> (R1, Y1) unpack: get_Y1 / get_ReA1 / get_alpha1_beta1_wigner
+//     and the transpose rescaling (Modules/DynamicalLanczos.py:2773-2948,
+//     :3009-3053);
+//   * psi' = L1 psi + anharmonic repack + reverse/shift: apply_L1_FT
+//     (:2287-2445), the repack of apply_anharmonic_FT (:3281-3363) and
+//     apply_full_L (:3549-3651), fused in one elementwise kernel;
+//   * the bi-/symmetric Lanczos recurrence of run_FT (:5958-6497) with
+//     deterministic block-partial dot products;
+//   * the continued fraction (:5032-5162), one thread per frequency.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tdscha {
+
+// per-pair coefficient arrays inside ctx->pc (each of length H)
+enum { PC_X = 0, PC_Y, PC_X1, PC_Y1, PC_UA, PC_UB, PC_RA, PC_RB, PC_TY, PC_TRA, PC_I, PC_J };
+
+int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st);
+
+int build_pair_coeffs(tdscha_ctx *c) {
+    const int M = c->M;
+    const long H = c->H;
+    std::vector<double> w(M);
+    TDS_CUDA(cudaMemcpy(w.data(), c->w, sizeof(double) * M, cudaMemcpyDeviceToHost));
+    std::vector<double> pc(12 * H);
+    const double T = c->T;
+    // Bose factors as apply_L1_FT writes them (division form, :2363-2366)
+    auto nb_div = [&](double x) { return T > 0 ? 1 / (exp(x / (T / kRyToK)) - 1) : 0.0; };
+    // and as get_chi_minus/plus write them (multiplication form, :2650-2652)
+    auto nb_mul = [&](double x) { return T > kEps ? 1.0 / (exp(x * 157887.32400374097 / T) - 1.0) : 0.0; };
+    std::vector<double> yw(M), reaw(M);
+    for (int m = 0; m < M; ++m) {
+        double n_mu = T > kEps ? 1.0 / (exp(w[m] * 157887.32400374097 / T) - 1.0) : 0.0;
+        yw[m] = 2 * w[m] / (2 * n_mu + 1);
+        reaw[m] = 2 * w[m] * n_mu * (n_mu + 1) / (2 * n_mu + 1);
+    }
+    long k = 0;
+    for (int i = 0; i < M; ++i) {
+        for (int j = i; j < M; ++j, ++k) {
+            double wa = w[j], wb = w[i];          // i_a = column, i_b = row (:2338-2346)
+            double na = nb_div(wa), nbb = nb_div(wb);
+            double den = (2 * na + 1) * (2 * nbb + 1);
+            if (!c->use_wigner) {
+                double X_ab = -wa * wa - wb * wb - (2 * wa * wb) / den;
+                double Y_ab = -(8 * wa * wb) / den;
+                double X1_ab = -(2 * na * nbb + na + nbb) * (2 * na * nbb + na + nbb + 1) * (2 * wa * wb) / den;
+                double Y1_ab = -wa * wa - wb * wb + (2 * wa * wb) / den;
+                pc[PC_X * H + k] = -X_ab;
+                pc[PC_Y * H + k] = -Y_ab;
+                pc[PC_X1 * H + k] = -X1_ab;
+                pc[PC_Y1 * H + k] = -Y1_ab;
+            } else {
+                pc[PC_X * H + k] = -(wa * wa + wb * wb - 2. * wa * wb);
+                pc[PC_Y1 * H + k] = -(wa * wa + wb * wb + 2. * wa * wb);
+            }
+            // Wigner change of variables a', b' -> alpha (:2818-2839)
+            double Xf = ((1 + 2 * na) * (1 + 2 * nbb) / 8);
+            double w2_on_X = (wa * wb) / Xf;
+            double chi_m = ((wa - wb) * (na - nbb)) / (2 * wa * wb);
+            double chi_p = ((wa + wb) * (1 + na + nbb)) / (2 * wa * wb);
+            pc[PC_UA * H + k] = w2_on_X * sqrt(-0.5 * chi_m);
+            pc[PC_UB * H + k] = w2_on_X * sqrt(+0.5 * chi_p);
+            // repack factors from get_chi_minus / get_chi_plus (row i, column j)
+            double ni = nb_mul(w[i]), nj = nb_mul(w[j]);
+            double cm = ((w[j] - w[i]) * (nj - ni)) / ((2. * w[j]) * w[i]);
+            double cp = ((w[j] + w[i]) * (1 + nj + ni)) / ((2. * w[j]) * w[i]);
+            pc[PC_RA * H + k] = sqrt(-0.5 * cm);
+            pc[PC_RB * H + k] = -sqrt(+0.5 * cp);
+            // transpose rescaling coefficients (:3036-3050), [a=i][b=j]
+            double cY = yw[i] * yw[j] * yw[j] + yw[i] * yw[i] * yw[j];
+            double cRA = yw[i] * reaw[j] * yw[j] + yw[i] * reaw[i] * yw[j];
+            pc[PC_TY * H + k] = cY * 2;
+            pc[PC_TRA * H + k] = cRA * 2;
+            pc[PC_I * H + k] = i;
+            pc[PC_J * H + k] = j;
+        }
+    }
+    TDS_CUDA(cudaMemcpy(c->pc, pc.data(), sizeof(double) * 12 * H, cudaMemcpyHostToDevice));
+    // Wigner double-counting mask (mask_dot_wigner, :5905-5954)
+    std::vector<double> mask(c->P, 1.0);
+    k = 0;
+    for (int i = 0; i < M; ++i)
+        for (int j = i; j < M; ++j, ++k)
+            if (i < j) { mask[M + k] = 2; mask[M + H + k] = 2; }
+    TDS_CUDA(cudaMemcpy(c->mask, mask.data(), sizeof(double) * c->P, cudaMemcpyHostToDevice));
+    return TDSCHA_OK;
+}
+
+__device__ __forceinline__ long tri_index(int i, int j, int M) {
+    return (long)i * M - (long)i * (i - 1) / 2 + (j - i);
+}
+
+__global__ void k_unpack(const double *__restrict__ psi, const double *__restrict__ pc, int M,
+                         long H, int wigner, int transpose, int ignore_v3,
+                         double *__restrict__ R1, double *__restrict__ Y1) {
+    long n = (long)M * M;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        int a = (int)(e / M), b = (int)(e % M);
+        int i = min(a, b), j = max(a, b);
+        long k = tri_index(i, j, M);
+        double y = psi[M + k], ra = psi[M + H + k], v;
+        if (wigner) {
+            v = pc[PC_UA * H + k] * y - pc[PC_UB * H + k] * ra;
+        } else if (!transpose) {
+            v = y;
+        } else {
+            double h = (i != j) ? 0.5 : 1.0;
+            v = (y * h) * pc[PC_TY * H + k] + (ra * h) * pc[PC_TRA * H + k];
+        }
+        Y1[e] = v;
+        if (e < M) R1[e] = ignore_v3 ? 0.0 : psi[e];
+    }
+}
+
+// out = L1 psi (+ anharmonic repack of f, d2v) then reverse / shift.
+__global__ void k_assemble(const double *__restrict__ psi, const double *__restrict__ f,
+                           const double *__restrict__ d2v, const double *__restrict__ pc,
+                           const double *__restrict__ w, const double *__restrict__ Yw,
+                           const double *__restrict__ ReAw, int M, long H, int wigner,
+                           int transpose, int ignore_harmonic, int with_anh, int reverse,
+                           double shift, double *__restrict__ out) {
+    long P = M + 2 * H;
+    double sg = wigner ? 1.0 : -1.0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < P; e += (long)gridDim.x * blockDim.x) {
+        double l1 = 0.0, an = 0.0;
+        if (e < M) {
+            if (!ignore_harmonic) {
+                double t = (psi[e] * w[e]) * w[e];
+                l1 = wigner ? -t : t;
+            }
+            if (with_anh) an = sg * f[e];
+        } else {
+            bool ysec = e < M + H;
+            long k = ysec ? e - M : e - M - H;
+            double pY = psi[M + k], pA = psi[M + H + k];
+            if (!ignore_harmonic) {
+                if (wigner) {
+                    l1 = ysec ? pc[PC_X * H + k] * pY : pc[PC_Y1 * H + k] * pA;
+                } else if (!transpose) {
+                    l1 = ysec ? pc[PC_X * H + k] * pY + pc[PC_Y * H + k] * pA
+                              : pc[PC_X1 * H + k] * pY + pc[PC_Y1 * H + k] * pA;
+                } else {
+                    l1 = ysec ? pc[PC_X * H + k] * pY + pc[PC_X1 * H + k] * pA
+                              : pc[PC_Y * H + k] * pY + pc[PC_Y1 * H + k] * pA;
+                }
+            }
+            if (with_anh) {
+                int i = (int)pc[PC_I * H + k], j = (int)pc[PC_J * H + k];
+                double dv = d2v[(long)i * M + j];
+                double v;
+                if (wigner) {
+                    v = (ysec ? pc[PC_RA * H + k] : pc[PC_RB * H + k]) * dv;
+                } else if (!transpose) {
+                    const double *ew = ysec ? Yw : ReAw;
+                    v = dv * ew[i] + dv * ew[j];
+                } else if (ysec) {
+                    v = 0.5 * ((1.0 / Yw[i]) * dv * (1.0 / Yw[j]));
+                    if (i != j) v *= 2;
+                } else {
+                    v = 0.0;
+                }
+                an = sg * v;
+            }
+        }
+        double o = l1 + an;
+        if (reverse) o *= -1;
+        o += shift * psi[e];
+        out[e] = o;
+    }
+}
+
+int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,
+                     int precision, cudaStream_t st) {
+    int M = c->M;
+    long H = c->H;
+    int with_anh = !c->ignore_v3;
+    if (with_anh) {
+        int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 4096));
+        k_unpack<<<nb, 256, 0, st>>>(psi_in, c->pc, M, H, c->use_wigner, transpose, c->ignore_v3,
+                                     c->R1, c->Y1);
+        TDS_CHECK_LAUNCH();
+        TDS_TRY(run_perturb(c, c->ignore_v4 ? 0 : 1, precision, st));
+    }
+    int nb = std::max(1, std::min(ceil_div(c->P, 256), 4096));
+    k_assemble<<<nb, 256, 0, st>>>(psi_in, c->f, c->d2v, c->pc, c->w, c->Yw, c->ReAw, M, H,
+                                   c->use_wigner, transpose, c->ignore_harmonic, with_anh,
+                                   c->reverse_L, c->shift, psi_out);
+    TDS_CHECK_LAUNCH();
+    return TDSCHA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos recurrence.  Device scalars (ctx->scal):
+enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN };
+// hist_dev rows of 4: a_k, b_k, c_k, s_norm_k.
+
+constexpr int kDotThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
+    return s;   // valid in thread 0
+}
+
+// partial of sum x*y*mask (mask may be null) per block
+__global__ void k_dot1(const double *__restrict__ x, const double *__restrict__ y,
+                       const double *__restrict__ mask, long n, double *__restrict__ part) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        acc += x[e] * (mask ? y[e] * mask[e] : y[e]);
+    double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232)
+__global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
+                         int k, double *__restrict__ scal) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double d = 0;
+    for (int b = 0; b < nblk; ++b) d += part[b];
+    double c_old = k >= 1 ? hist[4 * (k - 1) + 2] : 1.0;
+    double p_norm = hist[4 * k + 3] / c_old;
+    double a = d * p_norm;
+    scal[SC_A] = a;
+    scal[SC_PNORM] = p_norm;
+    scal[SC_NAN] = isnan(a) ? 1.0 : 0.0;
+    double cq = 0, cp = 0;
+    if (k >= 1) {
+        cq = hist[4 * (k - 1) + 2];
+        double old_p_norm = (k < 2) ? hist[4 * (k - 1) + 3] : hist[4 * (k - 1) + 3] / hist[4 * (k - 2) + 2];
+        cp = hist[4 * (k - 1) + 1] * (old_p_norm / p_norm);
+    }
+    scal[SC_CQ] = cq;
+    scal[SC_CP] = cp;
+}
+
+// rk = Lq - a q - cq q_prev ; sk = pL - a p - cp p_prev ; partial dots ss, rr, sr
+__global__ void k_resid(const double *__restrict__ Lq, const double *__restrict__ pL,
+                        const double *__restrict__ q, const double *__restrict__ p,
+                        const double *__restrict__ qprev, const double *__restrict__ pprev,
+                        const double *__restrict__ mask, const double *__restrict__ scal, long n,
+                        double *__restrict__ rk, double *__restrict__ sk, double *__restrict__ part,
+                        int nblk) {
+    __shared__ double sh[32];
+    double a = scal[SC_A], cq = scal[SC_CQ], cp = scal[SC_CP];
+    double ss = 0, rr = 0, sr = 0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        double r = Lq[e] - a * q[e];
+        double s = pL[e] - a * p[e];
+        if (qprev) r -= cq * qprev[e];
+        if (pprev) s -= cp * pprev[e];
+        rk[e] = r;
+        sk[e] = s;
+        double m = mask ? mask[e] : 1.0;
+        ss += s * (s * m);
+        rr += r * (r * m);
+        sr += s * (r * m);
+    }
+    double t;
+    t = block_sum(ss, sh); if (threadIdx.x == 0) part[blockIdx.x] = t;
+    t = block_sum(rr, sh); if (threadIdx.x == 0) part[nblk + blockIdx.x] = t;
+    t = block_sum(sr, sh); if (threadIdx.x == 0) part[2 * nblk + blockIdx.x] = t;
+}
+
+__global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
+                          int k, double *__restrict__ scal) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double ss = 0, rr = 0, sr = 0;
+    for (int b = 0; b < nblk; ++b) { ss += part[b]; rr += part[nblk + b]; sr += part[2 * nblk + b]; }
+    double s_raw = sqrt(ss);
+    double s_norm = s_raw * scal[SC_PNORM];
+    double b = sqrt(rr);
+    double c = (sr / (s_raw * b)) * s_norm;
+    scal[SC_B] = b;
+    scal[SC_C] = c;
+    scal[SC_SNORM] = s_norm;
+    scal[SC_SRAW] = s_raw;
+    bool conv = fabs(b) < kEps || fabs(c) < kEps;
+    scal[SC_CONV] = conv ? 1.0 : 0.0;
+    hist[4 * k + 0] = scal[SC_A];
+    if (!conv) {
+        hist[4 * k + 1] = b;
+        hist[4 * k + 2] = c;
+        hist[4 * (k + 1) + 3] = s_norm;
+    }
+}
+
+__global__ void k_normalize(const double *__restrict__ rk, const double *__restrict__ sk,
+                            const double *__restrict__ scal, long n, double *__restrict__ qn,
+                            double *__restrict__ pn) {
+    if (scal[SC_CONV] != 0.0) return;
+    double b = scal[SC_B], s = scal[SC_SRAW];
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        qn[e] = rk[e] / b;
+        pn[e] = sk[e] / s;
+    }
+}
+
+// Full re-biorthogonalisation of the new pair (q_{k+1}, p_{k+1}) against the
+// stored basis: q -= sum_j (p_j.q) q_j ; p -= sum_j (q_j.p) p_j with the
+// biorthogonality weights p_j.q_j measured on the stored vectors (one
+// classical Gram-Schmidt pass; the recurrence scalars are not changed).
+__global__ void k_proj_coeffs(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                              const double *__restrict__ qn, const double *__restrict__ pn,
+                              const double *__restrict__ mask, long n, int nvec, long ld,
+                              double *__restrict__ part) {
+    // one block per basis vector j: part[2j] = p_j.q_new, part[2j+1] = q_j.p_new
+    __shared__ double sh[32];
+    int j = blockIdx.x;
+    const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
+    double a = 0, b = 0;
+    for (long e = threadIdx.x; e < n; e += blockDim.x) {
+        double m = mask ? mask[e] : 1.0;
+        a += pj[e] * (qn[e] * m);
+        b += qj[e] * (pn[e] * m);
+    }
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) part[2 * j] = t;
+    t = block_sum(b, sh);
+    if (threadIdx.x == 0) part[2 * j + 1] = t;
+}
+
+__global__ void k_proj_apply(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                             const double *__restrict__ coef, const double *__restrict__ pqn,
+                             long n, int nvec, long ld, double *__restrict__ qn,
+                             double *__restrict__ pn) {
+    // coef[2j], coef[2j+1] as written by k_proj_coeffs; pqn[j] = p_j.q_j
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        double q = qn[e], p = pn[e];
+        for (int j = 0; j < nvec; ++j) {
+            double inv = 1.0 / pqn[j];
+            q -= coef[2 * j] * inv * Qb[(long)j * ld + e];
+            p -= coef[2 * j + 1] * inv * Pb[(long)j * ld + e];
+        }
+        qn[e] = q;
+        pn[e] = p;
+    }
+}
+
+__global__ void k_pq_diag(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                          const double *__restrict__ mask, long n, long ld,
+                          double *__restrict__ out) {
+    __shared__ double sh[32];
+    int j = blockIdx.x;
+    double a = 0;
+    for (long e = threadIdx.x; e < n; e += blockDim.x) {
+        double m = mask ? mask[e] : 1.0;
+        a += Pb[(long)j * ld + e] * (Qb[(long)j * ld + e] * m);
+    }
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) out[j] = t;
+}
+
+}  // namespace tdscha
+
+using namespace tdscha;
+
+extern "C" int tdscha_apply_full_L(tdscha_ctx *ctx, const double *psi_in, double *psi_out,
+                                   int transpose, int precision, void *stream) {
+    set_error("");
+    if (!ctx || !psi_in || !psi_out) { set_error("apply_full_L: null pointer"); return TDSCHA_ERR_ARG; }
+    if (psi_in == psi_out) { set_error("apply_full_L: in-place application is not supported"); return TDSCHA_ERR_ARG; }
+    return apply_full_L_dev(ctx, psi_in, psi_out, transpose, precision, (cudaStream_t)stream);
+}
+
+extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                                  int start_step, int n_iter, int run_simm, int precision,
+                                  int full_reorth, double *hist, int *steps_done, int *converged,
+                                  void *stream) {
+    set_error("");
+    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
+        set_error("lanczos_run: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
+        set_error("lanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
+        return TDSCHA_ERR_ARG;
+    }
+    if (run_simm && !ctx->use_wigner) {
+        set_error("lanczos_run: the symmetric Lanczos works only with Wigner");
+        return TDSCHA_ERR_ARG;
+    }
+    *steps_done = 0;
+    *converged = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const long P = ctx->P;
+    const int nblk = ctx->nblk_dot;
+    const double *mask = run_simm ? ctx->mask : nullptr;
+    // device copy of the history (capacity rows)
+    if (ctx->hist_cap < capacity + 1) {
+        if (ctx->hist_dev) cudaFree(ctx->hist_dev);
+        ctx->hist_dev = nullptr;
+        TDS_CUDA(cudaMalloc(&ctx->hist_dev, sizeof(double) * 4 * (capacity + 1)));
+        ctx->hist_cap = capacity + 1;
+    }
+    TDS_CUDA(cudaMemcpyAsync(ctx->hist_dev, hist, sizeof(double) * 4 * (start_step + 1),
+                             cudaMemcpyHostToDevice, st));
+    double *pqn = nullptr, *coef = nullptr;
+    if (full_reorth) {
+        TDS_CUDA(cudaMalloc(&pqn, sizeof(double) * (capacity + 1)));
+        TDS_CUDA(cudaMalloc(&coef, sizeof(double) * 2 * (capacity + 1)));
+    }
+    int rc = TDSCHA_OK;
+    int nb = std::max(1, std::min(ceil_div(P, kDotThreads), nblk));
+    for (int it = 0; it < n_iter; ++it) {
+        int k = start_step + it;
+        if (k + 1 >= capacity) {
+            set_error("lanczos_run: basis capacity %d exhausted at step %d", capacity, k);
+            rc = TDSCHA_ERR_ARG;
+            break;
+        }
+        double *q = basis_Q + (long)k * P, *p = basis_P + (long)k * P;
+        if ((rc = apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st)) != TDSCHA_OK) break;
+        const double *pL = ctx->Lq;
+        if (!run_simm) {
+            if ((rc = apply_full_L_dev(ctx, p, ctx->pL, 1, precision, st)) != TDSCHA_OK) break;
+            pL = ctx->pL;
+        }
+        k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
+        k_scal_a<<<1, 32, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
+        const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
+        k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
+                                             ctx->rk, ctx->sk, ctx->dots, nb);
+        k_scal_bc<<<1, 32, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
+        k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
+        {
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
+        }
+        if (cudaMemcpyAsync(ctx->host_pinned, ctx->scal, sizeof(double) * 16,
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+            rc = TDSCHA_ERR_CUDA;
+            break;
+        }
+        const double *sc = ctx->host_pinned;
+        if (sc[SC_NAN] != 0.0) {
+            set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", k);
+            rc = TDSCHA_ERR_NAN;
+            break;
+        }
+        hist[4 * k + 0] = sc[SC_A];
+        *steps_done = it + 1;
+        if (sc[SC_CONV] != 0.0) { *converged = 1; break; }
+        hist[4 * k + 1] = sc[SC_B];
+        hist[4 * k + 2] = sc[SC_C];
+        hist[4 * (k + 1) + 3] = sc[SC_SNORM];
+        if (full_reorth) {
+            int nvec = k + 1;
+            k_pq_diag<<<nvec, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, pqn);
+            k_proj_coeffs<<<nvec, 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, nvec, P, coef);
+            k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_P, coef, pqn, P, nvec, P, qn, pn);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) { set_error("reorth launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
+        }
+    }
+    if (pqn) cudaFree(pqn);
+    if (coef) cudaFree(coef);
+    return rc;
+}
+
+namespace tdscha {
+
+struct cplx { double x, y; };
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ cplx cdiv(cplx a, cplx b) {
+    // Smith's algorithm
+    if (fabs(b.x) >= fabs(b.y)) {
+        double r = b.y / b.x, d = b.x + b.y * r;
+        return {(a.x + a.y * r) / d, (a.y - a.x * r) / d};
+    }
+    double r = b.x / b.y, d = b.y + b.x * r;
+    return {(a.x * r + a.y) / d, (a.y * r - a.x) / d};
+}
+
+__global__ void k_cfrac(const double *__restrict__ a, int n, const double *__restrict__ b,
+                        const double *__restrict__ c, int nonsym, const double *__restrict__ w,
+                        int n_w, int wigner, double modulus, double sign, double shift,
+                        int use_term, int last_average, double smearing, int smooth_ramp,
+                        int n_b, double *__restrict__ g) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_w) return;
+    double wv = w[t];
+    double w2 = wv * wv;
+    cplx gf;
+    double a_m = 0, b_m = 0, c_m = 0;
+    if (use_term) {
+        int la = min(last_average, n), lb = min(last_average, n_b);
+        double sa = 0, sb = 0, scc = 0;
+        for (int i = n - la; i < n; ++i) sa += a[i];
+        for (int i = n_b - lb; i < n_b; ++i) { sb += b[i]; scc += c[i]; }
+        double a_av = sa / la, b_av = sb / lb, c_av = nonsym ? scc / lb : b_av;
+        a_m = a_av * sign - sign * shift;
+        b_m = b_av * sign;
+        c_m = c_av * sign;
+        double d = wigner ? a_m + w2 : a_m - w2;
+        double disc = d * d - 4 * b_m * c_m;
+        cplx sq = disc >= 0 ? cplx{sqrt(disc), 0.0} : cplx{0.0, sqrt(-disc)};
+        double den = 2 * b_m * c_m;
+        cplx gp = {(d + sq.x) / den, sq.y / den};
+        cplx gm = {(d - sq.x) / den, -sq.y / den};
+        gf = (hypot(gp.x, gp.y) < hypot(gm.x, gm.y)) ? gp : gm;
+    } else {
+        double av = a[n - 1] * sign - sign * shift;
+        cplx den = {wigner ? av + w2 : av - w2, 2 * wv * smearing};
+        gf = cdiv({1.0, 0.0}, den);
+    }
+    for (int i = n - 2; i >= 0; --i) {
+        double av = a[i] * sign - sign * shift;
+        double bv = b[i] * sign;
+        double cv = nonsym ? c[i] * sign : bv;
+        if (use_term && smooth_ramp > 0 && i >= n - smooth_ramp) {
+            double al = (double)(i - n + smooth_ramp + 1) / smooth_ramp;
+            av = (1 - al) * av + al * a_m;
+            bv = (1 - al) * bv + al * b_m;
+            cv = (1 - al) * cv + al * c_m;
+        }
+        cplx bcg = cmul({bv * cv, 0.0}, gf);
+        cplx den = {(wigner ? av + w2 : av - w2) - bcg.x, 2 * wv * smearing - bcg.y};
+        gf = cdiv({1.0, 0.0}, den);
+    }
+    if (wigner) gf = {-gf.x, gf.y};
+    g[2 * t] = gf.x * modulus;
+    g[2 * t + 1] = gf.y * modulus;
+}
+
+}  // namespace tdscha
+
+extern "C" int tdscha_continued_fraction(const double *a, int n, const double *b, int n_b,
+                                         const double *c, int n_c, const double *w, int n_w,
+                                         int use_wigner, double modulus, int reverse_L,
+                                         double shift_value, int use_terminator,
+                                         int last_average, double smearing, int smooth_ramp,
+                                         double *g_out) {
+    set_error("");
+    if (n < 1 || n_w < 0 || !a || !w || !g_out || n_b < 0 || (n > 1 && n_b < n - 1) || (n_b > 0 && !b)) {
+        set_error("continued_fraction: bad arguments");
+        return TDSCHA_ERR_ARG;
+    }
+    if (use_terminator && (n_b < 1 || last_average < 1)) {
+        set_error("continued_fraction: the terminator needs b coefficients and last_average >= 1");
+        return TDSCHA_ERR_ARG;
+    }
+    if (n_w == 0) return TDSCHA_OK;
+    int nonsym = (n_c == n_b && c != nullptr) ? 1 : 0;
+    double *d_a = nullptr, *d_b = nullptr, *d_c = nullptr, *d_w = nullptr, *d_g = nullptr;
+    size_t nbb = std::max(n_b, 1);
+    TDS_CUDA(cudaMalloc(&d_a, sizeof(double) * n));
+    TDS_CUDA(cudaMalloc(&d_b, sizeof(double) * nbb));
+    TDS_CUDA(cudaMalloc(&d_c, sizeof(double) * nbb));
+    TDS_CUDA(cudaMalloc(&d_w, sizeof(double) * n_w));
+    TDS_CUDA(cudaMalloc(&d_g, sizeof(double) * 2 * n_w));
+    cudaMemcpy(d_a, a, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (n_b) cudaMemcpy(d_b, b, sizeof(double) * n_b, cudaMemcpyHostToDevice);
+    if (nonsym && n_b) cudaMemcpy(d_c, c, sizeof(double) * n_b, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_w, w, sizeof(double) * n_w, cudaMemcpyHostToDevice);
+    k_cfrac<<<ceil_div(n_w, 128), 128>>>(d_a, n, d_b, d_c, nonsym, d_w, n_w, use_wigner, modulus,
+                                         reverse_L ? -1.0 : 1.0, shift_value, use_terminator,
+                                         last_average, smearing, smooth_ramp, n_b, d_g);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(g_out, d_g, sizeof(double) * 2 * n_w, cudaMemcpyDeviceToHost);
+    cudaFree(d_a); cudaFree(d_b); cudaFree(d_c); cudaFree(d_w); cudaFree(d_g);
+    if (e != cudaSuccess) { set_error("continued_fraction: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
+    return TDSCHA_OK;
+}

@@ -1,0 +1,128 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Run in a checkout that has the reference tree (default /root/reference, or
+$TDSCHA_REFERENCE_ROOT) after `oracle/build_ref.sh`:
+
+    python tests/golden/make_golden.py
+
+Every output below comes from the reference's own code: its C module
+`sscha_HP_odd` compiled from CModules/*.c, and its Python driver
+Modules/DynamicalLanczos.py (imported with stubbed physics deps by
+ref_harness.py).  Inputs are seeded synthetic ensembles
+(tdscha_gb300/synthetic.py) stored verbatim in the fixtures, so the tests
+do not depend on the generator staying unchanged.
+"""
+import contextlib
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from ref_harness import load_reference, make_reference_lanczos  # noqa: E402
+from tdscha_gb300.synthetic import (make_ensemble, random_R1, random_sym,  # noqa: E402
+                                    RY_TO_CM)
+
+
+def _ident(M):
+    return ([np.ones((1, 1, 1))] * M, [np.array([i], dtype=np.intc) for i in range(M)],
+            np.arange(M, dtype=np.intc))
+
+
+def _pack_syms(syms, deg):
+    n_deg = np.array([len(b) for b in deg], dtype=np.intc)
+    return (n_deg, np.concatenate([np.asarray(b, dtype=np.intc) for b in deg]),
+            np.concatenate([np.asarray(s).ravel() for s in syms]))
+
+
+def perturb_cases():
+    load_reference()
+    import sscha_HP_odd
+    out = {}
+    cases = [("m21_n200_s1", 21, 200, 1, 0.0, 11), ("m12_n30_s48", 12, 30, 48, 0.1, 12),
+             ("m9_n7_s8", 9, 7, 8, 0.1, 13), ("m1_n5_s1", 1, 5, 1, 0.0, 14)]
+    for name, M, N, S, sig, seed in cases:
+        if S > 1:
+            ens = make_ensemble(M, N, seed=seed, n_syms=S, rho_sigma=sig)
+            syms, deg, bid = ens["symmetries"], ens["degenerate_space"], ens["sym_block_id"]
+        else:
+            ens = make_ensemble(M, N, seed=seed, n_syms=1, rho_sigma=sig)
+            syms, deg, bid = _ident(M)
+        R1 = random_R1(M, seed + 100)
+        Y1 = random_sym(M, seed + 200, scale=1e-3)
+        n_deg, deg_flat, sym_flat = _pack_syms(syms, deg)
+        for d4 in (0, 1):
+            f = np.zeros(M)
+            d2v = np.zeros((M, M))
+            with contextlib.redirect_stdout(io.StringIO()):
+                sscha_HP_odd.GetPerturbAverageSym(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                                  ens["T"], d4, syms[0].shape[0], syms, n_deg, deg,
+                                                  bid, f, d2v)
+            key = "%s_d4%d" % (name, d4)
+            out[key + "/f"] = f
+            out[key + "/d2v"] = d2v
+        for k, v in dict(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"], R1=R1,
+                         Y1=Y1, n_deg=n_deg, deg_space=deg_flat, sym=sym_flat, blocks_ids=bid,
+                         S=S).items():
+            out["%s/%s" % (name, k)] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, "perturb_averages.npz"), **out)
+
+
+def run_case(fname, M, N, S, sig, seed, n_steps, variants):
+    if S > 1:
+        ens = make_ensemble(M, N, seed=seed, n_syms=S, rho_sigma=sig)
+    else:
+        ens = make_ensemble(M, N, seed=seed, n_syms=1, rho_sigma=sig)
+    R1 = random_R1(M, seed + 1)
+    wgrid = np.linspace(0.0, 600.0, 200) / RY_TO_CM
+    smear = 5.0 / RY_TO_CM
+    out = dict(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"], R1=R1,
+               wgrid=wgrid, smearing=smear, n_steps=n_steps)
+    if S > 1:
+        n_deg, deg_flat, sym_flat = _pack_syms(ens["symmetries"], ens["degenerate_space"])
+        out.update(n_deg=n_deg, deg_space=deg_flat, sym=sym_flat, blocks_ids=ens["sym_block_id"],
+                   S=S)
+    for tag, wig, d4 in variants:
+        lanc = make_reference_lanczos(ens, use_wigner=wig)
+        lanc.ignore_v4 = not d4
+        lanc.psi[:] = 0
+        lanc.psi[:M] = R1
+        lanc.perturbation_modulus = R1.dot(R1)
+        with contextlib.redirect_stdout(io.StringIO()):
+            lanc.run_FT(n_steps, verbose=False)
+            g = lanc.get_green_function_continued_fraction(wgrid, smearing=smear)
+            g_nt = lanc.get_green_function_continued_fraction(wgrid, use_terminator=False,
+                                                              smearing=smear)
+        out[tag + "/a"] = np.array(lanc.a_coeffs)
+        out[tag + "/b"] = np.array(lanc.b_coeffs)
+        out[tag + "/c"] = np.array(lanc.c_coeffs)
+        out[tag + "/G"] = g
+        out[tag + "/G_noterm"] = g_nt
+        # one operator application on the start vector, both directions
+        psi0 = np.zeros(M + M * (M + 1))
+        psi0[:M] = R1
+        rng = np.random.default_rng(seed + 7)
+        psi_r = rng.standard_normal(len(psi0)) * 1e-2
+        psi_r[:M] += R1
+        with contextlib.redirect_stdout(io.StringIO()):
+            out[tag + "/Lpsi"] = lanc.apply_full_L(psi_r.copy()).copy()
+            out[tag + "/LTpsi"] = lanc.apply_full_L(psi_r.copy(), transpose=True).copy()
+        out[tag + "/psi_r"] = psi_r
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
+def main():
+    perturb_cases()
+    run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
+             [("bilanczos", False, True), ("wigner", True, True), ("wigner_nod4", True, False)])
+    run_case("runft_m12_n120_s48.npz", 12, 120, 48, 0.1, 31, 20,
+             [("bilanczos", False, True), ("wigner", True, True)])
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
