@@ -52,7 +52,6 @@ struct MixedStore {
     long Rp = 0;
     // row layout (R x Mp): A operand of V = D Y1, and the epilogue's rows
     __nv_bfloat16 *d_hi = nullptr, *d_lo = nullptr;
-    float *d32 = nullptr;    // d rows (fp32 value hi+lo)      R x Mp
     float *g32 = nullptr;    // g = f_psi * f rows (fp32)      R x Mp
     // transposed layout (Mp x Rp): operands of G = U^T W
     __nv_bfloat16 *ut_hi = nullptr, *ut_lo = nullptr;   // U^T, U = f_Y * D
@@ -120,6 +119,7 @@ int alloc_fp64_scratch(tdscha_ctx *c);
 int mixed_prepare(tdscha_ctx *c);
 int mixed_release(tdscha_ctx *c);
 int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st);
+int mixed_check_error(tdscha_ctx *c);
 // lanczos.cu
 int build_pair_coeffs(tdscha_ctx *c);
 int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,

@@ -314,7 +314,10 @@ extern "C" int tdscha_perturb_averages(tdscha_ctx *ctx, const double *R1, const 
     TDS_TRY(run_perturb(ctx, apply_D4, precision, st));
     TDS_CUDA(cudaMemcpyAsync(f_out, ctx->f, sizeof(double) * M, outk, st));
     TDS_CUDA(cudaMemcpyAsync(d2v_out, ctx->d2v, sizeof(double) * M * M, outk, st));
-    if (!device_ptrs) TDS_CUDA(cudaStreamSynchronize(st));
+    if (!device_ptrs) {
+        TDS_CUDA(cudaStreamSynchronize(st));
+        TDS_TRY(mixed_check_error(ctx));
+    }
     return TDSCHA_OK;
 }
 

@@ -449,6 +449,7 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             break;
         }
         const double *sc = ctx->host_pinned;
+        if ((rc = mixed_check_error(ctx)) != TDSCHA_OK) break;
         if (sc[SC_NAN] != 0.0) {
             set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", k);
             rc = TDSCHA_ERR_NAN;

@@ -1,15 +1,800 @@
-// Mixed-precision perturbation averages (tensor cores).  Placeholder until
-// the tcgen05 GEMM pipeline lands: reports that the mode is unavailable.
+// Mixed-precision perturbation averages on the 5th-generation tensor cores.
+//
+// Same GEMM form as the float64 path (perturb_fp64.cu):
+//   stage A   V = D Y1           (R x M x M)   -> per-row q, p, s, t in the epilogue
+//   stage B   G = U^T W          (M x M x R)   -> split-K fp32 partial tiles
+// with every operand held as a pair of bf16 values (x = hi + lo, 16
+// significant bits) and each product taken as hi*hi + hi*lo + lo*hi
+// (three tcgen05.mma per K step into one fp32 TMEM accumulator).  The
+// recurrence around it stays in float64.
+//
+// Kernel anatomy (k_gemm_tc): one CTA = one 128 x BN output tile, 128 threads.
+//   warp 0 lane 0  TMA producer: cp.async.bulk.tensor 2D loads of the four
+//                  operand tiles (A hi/lo 128x64, B hi/lo BNx64, 128B swizzle)
+//                  into a STAGES-deep ring, completion on mbarrier full[s]
+//   warp 1 lane 0  MMA issuer: 4 K-slices x 3 products per stage, then
+//                  tcgen05.commit -> empty[s]; a final commit -> done
+//   all 4 warps    epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
+//                  32w..32w+31), fused row dots (stage A) or tile store (B)
+// Every mbarrier wait is bounded (clock64 budget); on expiry the kernel sets
+// the context's error flag, drains its own copies and MMAs (bounded again),
+// frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+
 #include "common.cuh"
 
 namespace tdscha {
 
-int mixed_prepare(tdscha_ctx *c) { (void)c; return TDSCHA_OK; }
-int mixed_release(tdscha_ctx *c) { (void)c; return TDSCHA_OK; }
+constexpr int kBM = 128;          // tile rows (TMEM lanes)
+constexpr int kBK = 64;           // K block: 64 bf16 = one 128-byte swizzle row
+constexpr uint32_t kABytes = kBM * kBK * 2;
+constexpr int kBNB = 128;         // stage B tile width
+constexpr int kStagesA = 2;
+constexpr int kStagesB = 3;
+constexpr long long kDefaultBudget = 4000000000LL;   // ~2 s at 2 GHz
+
+struct TmaQuad {
+    CUtensorMap a_hi, a_lo, b_hi, b_lo;
+};
+
+struct GemmArgs {
+    // geometry
+    int nkb;            // k-blocks per CTA (stage A); k-blocks per split (stage B)
+    int nkb_total;      // stage B: total k-blocks
+    long R;             // image rows
+    int Mp;             // padded mode count
+    int ldG;            // stage B: leading dimension of the partial tiles
+    int ntile;          // stage B: tiles per dimension
+    // stage A epilogue
+    const __nv_bfloat16 *d_hi, *d_lo;
+    const float *g32;
+    const float *vec_s, *vec_t;   // f_Y*R1 and R1/f_psi (Mp)
+    float *qpst;                  // [nct][4][R]
+    // stage B epilogue
+    float *gpart;
+    // bounded waits
+    int *err;
+    long long budget;
+};
+
+// ------------------------------------------------------------------ PTX
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase of the given parity; false when the budget runs out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long budget) {
+    long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (clock64() - t0 > budget) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar,
+                                            int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
+// layout written by TMA (8-row groups 1024 bytes apart).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+    d |= (uint64_t)(16 >> 4) << 16;                 // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                         // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                         // layout: 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: A = B = bf16, D = f32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4)                      // D format f32
+           | (1u << 7)                    // A format bf16
+           | (1u << 10)                   // B format bf16
+           | ((uint32_t)(N >> 3) << 17)   // N / 8
+           | ((uint32_t)(M >> 4) << 24);  // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+          "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+          "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_alloc(uint32_t slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                 "n"(NCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "n"(NCOLS)
+                 : "memory");
+}
+
+template <int N>
+struct TmemCols {
+    static constexpr int value = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : N <= 256 ? 256 : 512;
+};
+
+// ------------------------------------------------------------ the GEMM
+// MODE 0: stage A (row dots epilogue).  MODE 1: stage B (split-K tile store).
+template <int BN, int STAGES, int MODE>
+__global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQuad tm,
+                                                     const GemmArgs args) {
+    constexpr uint32_t kBBytes = BN * kBK * 2;
+    constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
+    constexpr int kCols = TmemCols<BN>::value;
+    constexpr uint32_t kIdesc = idesc_bf16(kBM, BN);
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * kStageBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES),
+                   done = smem_u32(bars + 2 * STAGES);
+
+    // tile coordinates and K range
+    int arow, brow, kb0, nkb;
+    if (MODE == 0) {
+        arow = blockIdx.y * kBM;
+        brow = blockIdx.x * BN;
+        kb0 = 0;
+        nkb = args.nkb;
+    } else {
+        int ta = blockIdx.x / args.ntile, tb = blockIdx.x % args.ntile;
+        arow = ta * kBM;
+        brow = tb * BN;
+        kb0 = blockIdx.y * args.nkb;
+        nkb = min(args.nkb, args.nkb_total - kb0);
+    }
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc<kCols>(smem_u32(tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const long long budget = args.budget;
+    bool failed = false;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        int issued = 0;
+        for (int i = 0; i < nkb; ++i) {
+            int s = i % STAGES;
+            if (i >= STAGES && !mbar_wait(empty0 + 8 * s, ((i / STAGES) & 1) ^ 1, budget)) {
+                failed = true;
+                break;
+            }
+            uint32_t base = smem_u32(smem + s * kStageBytes);
+            uint32_t bar = full0 + 8 * s;
+            int kx = (kb0 + i) * kBK;
+            mbar_expect_tx(bar, kStageBytes);
+            tma_load_2d(base, &tm.a_hi, bar, kx, arow);
+            tma_load_2d(base + kABytes, &tm.a_lo, bar, kx, arow);
+            tma_load_2d(base + 2 * kABytes, &tm.b_hi, bar, kx, brow);
+            tma_load_2d(base + 2 * kABytes + kBBytes, &tm.b_lo, bar, kx, brow);
+            issued = i + 1;
+        }
+        if (failed) {
+            // drain: every issued stage must land before the CTA exits
+            for (int i = max(0, issued - STAGES); i < issued; ++i)
+                mbar_wait(full0 + 8 * (i % STAGES), (i / STAGES) & 1, kDefaultBudget);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        for (int i = 0; i < nkb; ++i) {
+            int s = i % STAGES;
+            if (!mbar_wait(full0 + 8 * s, (i / STAGES) & 1, budget)) {
+                failed = true;
+                break;
+            }
+            tc_fence_after();
+            uint32_t base = smem_u32(smem + s * kStageBytes);
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+                uint64_t ah = sdesc_sw128(base + kk * 32);
+                uint64_t al = sdesc_sw128(base + kABytes + kk * 32);
+                uint64_t bh = sdesc_sw128(base + 2 * kABytes + kk * 32);
+                uint64_t bl = sdesc_sw128(base + 2 * kABytes + kBBytes + kk * 32);
+                mma_bf16(tmem, ah, bh, kIdesc, (i | kk) != 0);
+                mma_bf16(tmem, ah, bl, kIdesc, 1);
+                mma_bf16(tmem, al, bh, kIdesc, 1);
+            }
+            mma_commit(empty0 + 8 * s);
+        }
+        mma_commit(done);   // also after a failure: tracks the MMAs already issued
+    }
+    if (failed) *(volatile int *)args.err = 1;
+    __syncwarp();
+
+    // ---- epilogue
+    bool ready = mbar_wait(done, 0, budget);
+    if (!ready) {
+        if (lane == 0) *(volatile int *)args.err = 2;
+        ready = mbar_wait(done, 0, kDefaultBudget);   // MMAs must finish before dealloc
+    }
+    tc_fence_after();
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool have_acc = nkb > 0 && ready;
+    if (MODE == 0) {
+        long row = (long)arow + warp * 32 + lane;
+        float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
+#pragma unroll 1
+        for (int ch = 0; ch < BN / 32; ++ch) {
+            uint32_t v[32];
+            tmem_ld32(lane_base + ch * 32, v);
+            int col0 = brow + ch * 32;
+            if (row < args.R && have_acc) {
+                const uint4 *ph = reinterpret_cast<const uint4 *>(args.d_hi + row * args.Mp + col0);
+                const uint4 *pl = reinterpret_cast<const uint4 *>(args.d_lo + row * args.Mp + col0);
+                const float4 *pg = reinterpret_cast<const float4 *>(args.g32 + row * args.Mp + col0);
+#pragma unroll
+                for (int j8 = 0; j8 < 4; ++j8) {
+                    uint4 h = ph[j8], l = pl[j8];
+                    const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&h);
+                    const __nv_bfloat162 *l2 = reinterpret_cast<const __nv_bfloat162 *>(&l);
+                    float4 g0 = pg[2 * j8], g1 = pg[2 * j8 + 1];
+                    float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        float2 hf = __bfloat1622float2(h2[e]), lf = __bfloat1622float2(l2[e]);
+                        float d0 = hf.x + lf.x, d1 = hf.y + lf.y;
+                        int j = j8 * 8 + 2 * e;
+                        float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
+                        q = fmaf(d0, v0, q);
+                        q = fmaf(d1, v1, q);
+                        p = fmaf(gg[2 * e], v0, p);
+                        p = fmaf(gg[2 * e + 1], v1, p);
+                        sacc = fmaf(args.vec_s[col0 + j], d0, sacc);
+                        sacc = fmaf(args.vec_s[col0 + j + 1], d1, sacc);
+                        tacc = fmaf(args.vec_t[col0 + j], gg[2 * e], tacc);
+                        tacc = fmaf(args.vec_t[col0 + j + 1], gg[2 * e + 1], tacc);
+                    }
+                }
+            }
+        }
+        if (row < args.R) {
+            long R = args.R;
+            float *o = args.qpst + (long)blockIdx.x * 4 * R;
+            o[row] = q;
+            o[R + row] = p;
+            o[2 * R + row] = sacc;
+            o[3 * R + row] = tacc;
+        }
+    } else {
+        long a = arow + warp * 32 + lane;
+        float *dst = args.gpart + (long)blockIdx.y * args.ldG * args.ldG + a * args.ldG + brow;
+#pragma unroll 1
+        for (int ch = 0; ch < BN / 32; ++ch) {
+            uint32_t v[32];
+            tmem_ld32(lane_base + ch * 32, v);
+            float4 *d4 = reinterpret_cast<float4 *>(dst + ch * 32);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float4 o;
+                if (have_acc) {
+                    o.x = __uint_as_float(v[4 * j]);
+                    o.y = __uint_as_float(v[4 * j + 1]);
+                    o.z = __uint_as_float(v[4 * j + 2]);
+                    o.w = __uint_as_float(v[4 * j + 3]);
+                } else {
+                    o = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                d4[j] = o;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc<kCols>(tmem);
+}
+
+// --------------------------------------------------------- data movers
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+    hi = __float2bfloat16_rn(x);
+    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// Resident operands from the float64 image rows D, F (R x M):
+//   d_hi/d_lo, g32       (R x Mp)  row layout, stage A operand and epilogue
+//   ut_hi/ut_lo, ft32    (Mp x Rp) transposed layout, stage B operands
+__global__ void k_prep_rows(const double *__restrict__ D, const double *__restrict__ F,
+                            const double *__restrict__ fpsi, long R, int M, int Mp,
+                            __nv_bfloat16 *__restrict__ d_hi, __nv_bfloat16 *__restrict__ d_lo,
+                            float *__restrict__ g32) {
+    long n = R * Mp;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        long r = e / Mp;
+        int m = (int)(e % Mp);
+        float x = 0.f, g = 0.f;
+        if (m < M) {
+            x = (float)D[r * M + m];
+            g = (float)(fpsi[m] * F[r * M + m]);
+        }
+        __nv_bfloat16 h, l;
+        split_bf16(x, h, l);
+        d_hi[e] = h;
+        d_lo[e] = l;
+        g32[e] = g;
+    }
+}
+
+// transpose through shared memory: 32 x 32 tiles of (r, m)
+__global__ void k_prep_cols(const double *__restrict__ D, const double *__restrict__ F,
+                            const double *__restrict__ fY, long R, int M, long Rp,
+                            __nv_bfloat16 *__restrict__ ut_hi, __nv_bfloat16 *__restrict__ ut_lo,
+                            float *__restrict__ ut32, float *__restrict__ ft32) {
+    __shared__ float tu[32][33], tf[32][33];
+    long r0 = (long)blockIdx.x * 32;
+    int m0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        long r = r0 + k;
+        int m = m0 + threadIdx.x;
+        float u = 0.f, f = 0.f;
+        if (r < R && m < M) {
+            u = (float)(fY[m] * D[r * M + m]);
+            f = (float)F[r * M + m];
+        }
+        tu[k][threadIdx.x] = u;
+        tf[k][threadIdx.x] = f;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int m = m0 + k;
+        long r = r0 + threadIdx.x;
+        if (r < Rp) {
+            float u = tu[threadIdx.x][k];
+            __nv_bfloat16 h, l;
+            split_bf16(u, h, l);
+            long o = (long)m * Rp + r;
+            ut_hi[o] = h;
+            ut_lo[o] = l;
+            ut32[o] = __bfloat162float(h) + __bfloat162float(l);
+            ft32[o] = tf[threadIdx.x][k];
+        }
+    }
+}
+
+// Y1 (symmetric, float64 M x M) -> split bf16 (Mp x Mp, zero padded) and the
+// two epilogue vectors f_Y*R1 and R1/f_psi.
+__global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restrict__ R1,
+                          const double *__restrict__ fY, const double *__restrict__ fpsi, int M,
+                          int Mp, __nv_bfloat16 *__restrict__ y_hi,
+                          __nv_bfloat16 *__restrict__ y_lo, float *__restrict__ vs,
+                          float *__restrict__ vt) {
+    long n = (long)Mp * Mp;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        int a = (int)(e / Mp), b = (int)(e % Mp);
+        float x = (a < M && b < M) ? (float)Y1[(long)a * M + b] : 0.f;
+        __nv_bfloat16 h, l;
+        split_bf16(x, h, l);
+        y_hi[e] = h;
+        y_lo[e] = l;
+        if (e < Mp) {
+            int m = (int)e;
+            vs[m] = m < M ? (float)(fY[m] * R1[m]) : 0.f;
+            vt[m] = m < M ? (float)(R1[m] / fpsi[m]) : 0.f;
+        }
+    }
+}
+
+// Row scalars from the stage A partials (sums in float64).
+__global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, int S,
+                             const double *__restrict__ rho, int apply_d4,
+                             float4 *__restrict__ abcc) {
+    long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double q = 0, p = 0, s = 0, t = 0;
+    for (int ct = 0; ct < nct; ++ct) {
+        const float *o = qpst + (long)ct * 4 * R;
+        q += o[r];
+        p += o[R + r];
+        s += o[2 * R + r];
+        t += o[3 * R + r];
+    }
+    double rw = rho[r / S];
+    double d4 = apply_d4 ? 1.0 : 0.0;
+    abcc[r] = make_float4((float)(rw * (s / 3 - d4 * q / 8)), (float)(rw * (t / 3 - d4 * p / 4)),
+                          (float)(-rw * q / 6), (float)(-rw * p / 3));
+}
+
+// W^T[b][r] = alpha_r F^T[b][r] + beta_r/2 U^T[b][r] as split bf16, and the
+// force-average partials fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
+constexpr int kWRows = 8;      // b rows per block
+constexpr int kWChunk = 2048;  // r per block
+__global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
+                                                const float *__restrict__ ut32,
+                                                const float4 *__restrict__ abcc, long R, long Rp,
+                                                int M, __nv_bfloat16 *__restrict__ wt_hi,
+                                                __nv_bfloat16 *__restrict__ wt_lo,
+                                                float *__restrict__ fpart) {
+    __shared__ float red[kWRows][8];
+    int b0 = blockIdx.x * kWRows;
+    long r0 = (long)blockIdx.y * kWChunk;
+    float facc[kWRows];
+#pragma unroll
+    for (int k = 0; k < kWRows; ++k) facc[k] = 0.f;
+    for (int it = 0; it < kWChunk / 256; ++it) {
+        long r = r0 + it * 256 + threadIdx.x;
+        if (r >= R) break;
+        float4 w = abcc[r];
+#pragma unroll
+        for (int k = 0; k < kWRows; ++k) {
+            int b = b0 + k;
+            if (b >= M) break;
+            long o = (long)b * Rp + r;
+            float f = ft32[o], u = ut32[o];
+            float x = w.x * f + 0.5f * w.y * u;
+            __nv_bfloat16 h, l;
+            split_bf16(x, h, l);
+            wt_hi[o] = h;
+            wt_lo[o] = l;
+            facc[k] = fmaf(w.z, f, fmaf(w.w, u, facc[k]));
+        }
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kWRows; ++k) {
+        float v = facc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kWRows) {
+        int b = b0 + threadIdx.x;
+        float s = 0.f;
+        for (int w8 = 0; w8 < 8; ++w8) s += red[threadIdx.x][w8];
+        if (b < M) fpart[(long)blockIdx.y * M + b] = s;
+    }
+}
+
+__global__ void k_finalize_mixed(const float *__restrict__ gpart, int nsplit, int ldG,
+                                 const float *__restrict__ fpart, int nfchunk, int M, double norm,
+                                 double *__restrict__ f, double *__restrict__ d2v) {
+    long n = (long)M * M;
+    long stride = (long)ldG * ldG;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        int a = (int)(e / M), b = (int)(e % M);
+        double gab = 0, gba = 0;
+        for (int s = 0; s < nsplit; ++s) {
+            gab += (double)gpart[s * stride + (long)a * ldG + b];
+            gba += (double)gpart[s * stride + (long)b * ldG + a];
+        }
+        d2v[e] = -(gab + gba) / norm;
+        if (e < M) {
+            double acc = 0;
+            for (int ch = 0; ch < nfchunk; ++ch) acc += (double)fpart[(long)ch * M + e];
+            f[e] = acc / norm;
+        }
+    }
+}
+
+// ------------------------------------------------------------- host side
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2D bf16 tensor (inner x outer, row pitch inner*2 bytes), box 64 x box_rows,
+// 128-byte swizzle, zero fill out of bounds.
+static int make_map(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer,
+                    uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return TDSCHA_ERR_CUDA; }
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((inner * 2) & 15) || inner % kBK) {
+        set_error("tensor map: misaligned base or pitch");
+        return TDSCHA_ERR_ARG;
+    }
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return TDSCHA_ERR_CUDA; }
+    return TDSCHA_OK;
+}
+
+template <int BN, int STAGES>
+static constexpr size_t gemm_smem() {
+    return 1024 + STAGES * (2 * (size_t)kABytes + 2 * (size_t)BN * kBK * 2) + 8 * (2 * STAGES + 1) + 16;
+}
+
+// Stage A column tile: the widest multiple of 64 (<= 192) dividing Mp.
+static int choose_bn(int Mp) {
+    int k = Mp / 64;
+    for (int c = 3; c >= 1; --c)
+        if (k % c == 0) return 64 * c;
+    return 64;
+}
+
+struct MixedExtra {
+    TmaQuad tmA, tmB;
+    int bnA = 0;
+    float *vs = nullptr, *vt = nullptr;
+    float4 *abcc = nullptr;
+    float *fpart = nullptr;
+    int nfchunk = 0;
+    int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
+    long long budget = kDefaultBudget;
+};
+
+static MixedExtra *extra(tdscha_ctx *c) { return reinterpret_cast<MixedExtra *>(c->mx.tmaps); }
+
+int mixed_prepare(tdscha_ctx *c) {
+    MixedStore &mx = c->mx;
+    const int M = c->M;
+    const long R = c->R;
+    mx.Mp = ((M + 63) / 64) * 64;
+    mx.Rp = ((R + 63) / 64) * 64;
+    const int Mp = mx.Mp;
+    const long Rp = mx.Rp;
+    MixedExtra *x = new MixedExtra();
+    mx.tmaps = x;
+    if (const char *b = getenv("TDSCHA_WAIT_BUDGET_CYCLES")) x->budget = atoll(b);
+    x->bnA = choose_bn(Mp);
+    mx.nctile = Mp / x->bnA;
+    x->ldG = ((Mp + kBM - 1) / kBM) * kBM;
+    x->ntB = x->ldG / kBM;
+    x->nkbB = (int)(Rp / kBK);
+    int want = std::max(1, ceil_div(2 * 152, x->ntB * x->ntB));
+    want = std::min(want, x->nkbB);
+    x->kbps = ceil_div(x->nkbB, want);
+    mx.nsplit = ceil_div(x->nkbB, x->kbps);
+    x->nfchunk = ceil_div(R, kWChunk);
+    size_t rowN = (size_t)R * Mp, colN = (size_t)Mp * Rp;
+    TDS_CUDA(cudaMalloc(&mx.d_hi, 2 * rowN));
+    TDS_CUDA(cudaMalloc(&mx.d_lo, 2 * rowN));
+    TDS_CUDA(cudaMalloc(&mx.g32, 4 * rowN));
+    TDS_CUDA(cudaMalloc(&mx.ut_hi, 2 * colN));
+    TDS_CUDA(cudaMalloc(&mx.ut_lo, 2 * colN));
+    TDS_CUDA(cudaMalloc(&mx.ut32, 4 * colN));
+    TDS_CUDA(cudaMalloc(&mx.ft32, 4 * colN));
+    TDS_CUDA(cudaMalloc(&mx.wt_hi, 2 * colN));
+    TDS_CUDA(cudaMalloc(&mx.wt_lo, 2 * colN));
+    TDS_CUDA(cudaMalloc(&mx.y1_hi, 2 * (size_t)Mp * Mp));
+    TDS_CUDA(cudaMalloc(&mx.y1_lo, 2 * (size_t)Mp * Mp));
+    TDS_CUDA(cudaMalloc(&mx.qp, sizeof(float) * 4 * mx.nctile * R));
+    TDS_CUDA(cudaMalloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldG));
+    TDS_CUDA(cudaMalloc(&x->vs, sizeof(float) * Mp));
+    TDS_CUDA(cudaMalloc(&x->vt, sizeof(float) * Mp));
+    TDS_CUDA(cudaMalloc(&x->abcc, sizeof(float4) * R));
+    TDS_CUDA(cudaMalloc(&x->fpart, sizeof(float) * (size_t)x->nfchunk * M));
+    TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
+    *mx.err_flag = 0;
+    TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * colN));
+    TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * colN));
+    {
+        int nb = (int)std::min<long>((rowN + 255) / 256, 152L * 32);
+        k_prep_rows<<<nb, 256>>>(c->D, c->F, c->fpsi, R, M, Mp, mx.d_hi, mx.d_lo, mx.g32);
+        TDS_CHECK_LAUNCH();
+        dim3 g(ceil_div(Rp, 32), Mp / 32);
+        k_prep_cols<<<g, dim3(32, 8)>>>(c->D, c->F, c->fY, R, M, Rp, mx.ut_hi, mx.ut_lo, mx.ut32,
+                                        mx.ft32);
+        TDS_CHECK_LAUNCH();
+    }
+    TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
+    TDS_TRY(make_map(&x->tmA.a_lo, mx.d_lo, Mp, R, kBM));
+    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, Mp, x->bnA));
+    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, Mp, x->bnA));
+    TDS_TRY(make_map(&x->tmB.a_hi, mx.ut_hi, Rp, Mp, kBM));
+    TDS_TRY(make_map(&x->tmB.a_lo, mx.ut_lo, Rp, Mp, kBM));
+    TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, Mp, kBNB));
+    TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, Mp, kBNB));
+    static bool attr_done = false;
+    if (!attr_done) {
+        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<192, kStagesA, 0>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)gemm_smem<192, kStagesA>()));
+        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<128, kStagesA, 0>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)gemm_smem<128, kStagesA>()));
+        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<64, kStagesA, 0>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)gemm_smem<64, kStagesA>()));
+        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<kBNB, kStagesB, 1>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)gemm_smem<kBNB, kStagesB>()));
+        attr_done = true;
+    }
+    TDS_CUDA(cudaDeviceSynchronize());
+    return TDSCHA_OK;
+}
+
+int mixed_release(tdscha_ctx *c) {
+    MixedStore &mx = c->mx;
+    void *bufs[] = {mx.d_hi, mx.d_lo, mx.g32, mx.ut_hi, mx.ut_lo, mx.ut32, mx.ft32, mx.wt_hi,
+                    mx.wt_lo, mx.y1_hi, mx.y1_lo, mx.qp, mx.gpart};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+    if (MixedExtra *x = extra(c)) {
+        if (x->vs) cudaFree(x->vs);
+        if (x->vt) cudaFree(x->vt);
+        if (x->abcc) cudaFree(x->abcc);
+        if (x->fpart) cudaFree(x->fpart);
+        delete x;
+    }
+    if (mx.err_flag) cudaFreeHost(mx.err_flag);
+    mx = MixedStore();
+    return TDSCHA_OK;
+}
+
+int mixed_check_error(tdscha_ctx *c) {
+    if (c->mx.err_flag && *(volatile int *)c->mx.err_flag) {
+        int v = *(volatile int *)c->mx.err_flag;
+        *(volatile int *)c->mx.err_flag = 0;
+        set_error("tensor-core pipeline: a bounded wait expired (code %d)", v);
+        return TDSCHA_ERR_TIMEOUT;
+    }
+    return TDSCHA_OK;
+}
+
 int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
-    (void)c; (void)apply_d4; (void)st;
-    set_error("mixed precision is not available in this build");
-    return TDSCHA_ERR_STATE;
+    MixedStore &mx = c->mx;
+    MixedExtra *x = extra(c);
+    if (!x) { set_error("mixed store not prepared"); return TDSCHA_ERR_STATE; }
+    const int M = c->M, Mp = mx.Mp;
+    const long R = c->R, Rp = mx.Rp;
+    int *err_dev = nullptr;
+    TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
+    {
+        ProfScope ps(c, 5, st);
+        int nb = std::max(1, std::min(ceil_div((long)Mp * Mp, 256), 1024));
+        k_prep_y1<<<nb, 256, 0, st>>>(c->Y1, c->R1, c->fY, c->fpsi, M, Mp, mx.y1_hi, mx.y1_lo,
+                                      x->vs, x->vt);
+        TDS_CHECK_LAUNCH();
+    }
+    GemmArgs ga{};
+    ga.nkb = Mp / kBK;
+    ga.R = R;
+    ga.Mp = Mp;
+    ga.d_hi = mx.d_hi;
+    ga.d_lo = mx.d_lo;
+    ga.g32 = mx.g32;
+    ga.vec_s = x->vs;
+    ga.vec_t = x->vt;
+    ga.qpst = mx.qp;
+    ga.err = err_dev;
+    ga.budget = x->budget;
+    {
+        ProfScope ps(c, 0, st);
+        dim3 grid(mx.nctile, ceil_div(R, kBM));
+        switch (x->bnA) {
+            case 192:
+                k_gemm_tc<192, kStagesA, 0><<<grid, 128, gemm_smem<192, kStagesA>(), st>>>(x->tmA, ga);
+                break;
+            case 128:
+                k_gemm_tc<128, kStagesA, 0><<<grid, 128, gemm_smem<128, kStagesA>(), st>>>(x->tmA, ga);
+                break;
+            default:
+                k_gemm_tc<64, kStagesA, 0><<<grid, 128, gemm_smem<64, kStagesA>(), st>>>(x->tmA, ga);
+                break;
+        }
+        TDS_CHECK_LAUNCH();
+    }
+    {
+        ProfScope ps(c, 1, st);
+        k_rows_mixed<<<ceil_div(R, 256), 256, 0, st>>>(mx.qp, mx.nctile, R, c->S, c->rho, apply_d4,
+                                                        x->abcc);
+        TDS_CHECK_LAUNCH();
+    }
+    {
+        ProfScope ps(c, 2, st);
+        dim3 g(ceil_div(M, kWRows), x->nfchunk);
+        k_wbuild<<<g, 256, 0, st>>>(mx.ft32, mx.ut32, x->abcc, R, Rp, M, mx.wt_hi, mx.wt_lo,
+                                    x->fpart);
+        TDS_CHECK_LAUNCH();
+    }
+    GemmArgs gb{};
+    gb.nkb = x->kbps;
+    gb.nkb_total = x->nkbB;
+    gb.R = R;
+    gb.Mp = Mp;
+    gb.ldG = x->ldG;
+    gb.ntile = x->ntB;
+    gb.gpart = mx.gpart;
+    gb.err = err_dev;
+    gb.budget = x->budget;
+    {
+        ProfScope ps(c, 3, st);
+        dim3 grid(x->ntB * x->ntB, mx.nsplit);
+        k_gemm_tc<kBNB, kStagesB, 1><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, gb);
+        TDS_CHECK_LAUNCH();
+    }
+    {
+        ProfScope ps(c, 4, st);
+        int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 2048));
+        k_finalize_mixed<<<nb, 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, x->fpart, x->nfchunk, M,
+                                             c->sum_rho * c->S, c->f, c->d2v);
+        TDS_CHECK_LAUNCH();
+    }
+    return TDSCHA_OK;
 }
 
 }  // namespace tdscha

@@ -119,7 +119,10 @@ def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
              [("bilanczos", False, True), ("wigner", True, True), ("wigner_nod4", True, False)])
-    run_case("runft_m12_n120_s48.npz", 12, 120, 48, 0.1, 31, 20,
+    # 12 steps: this symmetric case nearly breaks down at step 14 (b_13 ~ 1e-8),
+    # after which a rounding-order change alone (in the reference itself)
+    # moves the coefficients by O(1).
+    run_case("runft_m12_n120_s48.npz", 12, 120, 48, 0.1, 31, 12,
              [("bilanczos", False, True), ("wigner", True, True)])
     print("fixtures written to", HERE)
 

@@ -1,0 +1,105 @@
+"""Tensor-core (split-bf16 x3, fp32 accumulate) perturbation averages and the
+mixed-precision Lanczos run, against the float64 oracle / float64 GPU path.
+
+Tolerances: one perturbation-average call within 1e-3 of the largest entry
+(split-bf16 operands carry 16 significant bits); the spectral function of a
+mixed-precision run within 1e-4 relative (max |dA| / max |A| over the
+frequency grid) of the float64 run -- the accuracy bar of the mixed path."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tdscha_gb300 import _native as nat
+from tdscha_gb300.DynamicalLanczos import Lanczos
+from tdscha_gb300.synthetic import RY_TO_CM, make_ensemble, random_R1, random_sym
+
+pytestmark = pytest.mark.gpu
+
+TOL_CALL = 1e-3
+TOL_SPECTRAL = 1e-4
+
+
+def rel(got, ref):
+    return np.abs(np.asarray(got) - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+def _mixed_call(ctx, R1, Y1, d4=1):
+    M = R1.size
+    f = np.zeros(M)
+    d2v = np.zeros((M, M))
+    nat.check(nat.load().tdscha_perturb_averages(ctx.handle, R1.ctypes.data, Y1.ctypes.data, d4,
+                                                 nat.PREC_MIXED, f.ctypes.data, d2v.ctypes.data,
+                                                 0, None))
+    return f, d2v
+
+
+@pytest.mark.parametrize("M,N,S", [(64, 3000, 1), (21, 1000, 1), (131, 2000, 1), (24, 300, 48),
+                                   (573, 1500, 1)])
+def test_mixed_perturb_matches_oracle(gpu_lib, M, N, S):
+    ens = make_ensemble(M, N, seed=100 + M, n_syms=S, rho_sigma=0.1)
+    if S == 1:
+        syms, spaces, bid = oracle.identity_symmetries(M)
+    else:
+        syms, spaces, bid = ens["symmetries"], ens["degenerate_space"], ens["sym_block_id"]
+    R1 = random_R1(M, 8)
+    Y1 = random_sym(M, 9, scale=1e-3)
+    f_ref, d_ref = oracle.perturb_averages(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                           ens["T"], 1, syms, spaces, bid, n_threads=8)
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    f, d2v = _mixed_call(ctx, R1, Y1)
+    ef, ed = rel(f, f_ref), rel(d2v, d_ref)
+    print("M=%d N=%d S=%d: f err %.2e  d2v err %.2e" % (M, N, S, ef, ed))
+    assert ef <= TOL_CALL and ed <= TOL_CALL
+    f2, d2 = _mixed_call(ctx, R1, Y1)
+    assert np.array_equal(f, f2) and np.array_equal(d2v, d2)      # deterministic
+    ctx.close()
+
+
+def _spectral_run(ens, precision, steps, R1):
+    lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
+                               use_wigner=False, precision=precision)
+    lanc.init(use_symmetries=False)
+    lanc.prepare_perturbation(R1, masses_exp=0)
+    lanc.run_FT(steps, verbose=False)
+    w = np.linspace(0, 600, 2000) / RY_TO_CM
+    G = lanc.get_green_function_continued_fraction(w, smearing=5 / RY_TO_CM)
+    return lanc, -G.imag
+
+
+@pytest.mark.parametrize("M,N,steps", [(48, 4000, 60), (96, 8000, 80)])
+def test_mixed_lanczos_spectral_error(gpu_lib, M, N, steps):
+    ens = make_ensemble(M, N, seed=7 + M, rho_sigma=0.1)
+    R1 = random_R1(M, 3)
+    l64, A64 = _spectral_run(ens, "fp64", steps, R1)
+    lmx, Amx = _spectral_run(ens, "mixed", steps, R1)
+    err = rel(Amx, A64)
+    a64, amx = np.array(l64.a_coeffs), np.array(lmx.a_coeffs)
+    print("M=%d N=%d: spectral err %.2e, a_0..9 max rel %.2e" % (
+        M, N, err, np.max(np.abs(amx[:10] - a64[:10]) / np.abs(a64[:10]))))
+    assert err <= TOL_SPECTRAL
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(gpu_lib, monkeypatch):
+    M, N = 64, 512
+    ens = make_ensemble(M, N, seed=5)
+    syms, spaces, bid = oracle.identity_symmetries(M)
+    R1, Y1 = random_R1(M, 1), random_sym(M, 2, scale=1e-3)
+    monkeypatch.setenv("TDSCHA_WAIT_BUDGET_CYCLES", "0")
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    monkeypatch.delenv("TDSCHA_WAIT_BUDGET_CYCLES")
+    with pytest.raises(nat.TdschaError) as e:
+        _mixed_call(ctx, R1, Y1)
+    assert e.value.code == nat.ERR_TIMEOUT
+    ctx.close()
+    # the CUDA context is still usable: a fresh context computes correctly
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    f, d2v = _mixed_call(ctx, R1, Y1)
+    f_ref, d_ref = oracle.perturb_averages(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                           ens["T"], 1, syms, spaces, bid)
+    assert rel(d2v, d_ref) <= TOL_CALL
+    ctx.close()
