@@ -44,6 +44,14 @@ def parse():
     ap.add_argument("--precision", default=None, choices=[None, "mixed", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--check-steps", type=int, default=None,
+                    help="steps of the mixed-vs-float64 spectral check (default: the workload's)")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="timed steps of the float64 comparison arm")
+    ap.add_argument("--no-reorth", action="store_true",
+                    help="plain recurrence (the reference default); without full "
+                         "re-biorthogonalisation the spectral check is not reproducible "
+                         "even between two float64 runs")
     return ap.parse_args()
 
 
@@ -219,7 +227,7 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU side
-KERNEL_NAMES = {0: "stageA (V = D Y1 + quadratic forms)", 1: "row scalars", 2: "force average",
+KERNEL_NAMES = {0: "stageA (V = D Y1 + quadratic forms)", 1: "row scalars", 2: "force average (+ W build, mixed)",
                 3: "stageB (G = U^T W)", 4: "finalise", 5: "operand preparation"}
 
 
@@ -236,7 +244,7 @@ def run_ours(args):
     lib = nat.load()
     spec, ens = workload(args.workload)
     M, N = spec["M"], spec["N"]
-    prec_name = args.precision or "fp64"
+    prec_name = args.precision or "mixed"
     prec = nat.PREC_MIXED if prec_name == "mixed" else nat.PREC_FP64
     syms, spaces, bid = sym_tables(ens)
     ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
@@ -260,9 +268,11 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     st = stream.cuda_stream
 
+    reorth = 0 if args.no_reorth else 1
+
     def steps(start, n):
         nat.check(lib.tdscha_lanczos_run(ctx.handle, Qd.data_ptr(), Pd.data_ptr(), cap, start, n,
-                                         0, prec, 0, nat.dp(hist), ctypes.byref(done),
+                                         0, prec, reorth, nat.dp(hist), ctypes.byref(done),
                                          ctypes.byref(conv), st))
         if conv.value or done.value != n:
             raise RuntimeError("Lanczos converged early (%d of %d steps)" % (done.value, n))
@@ -340,9 +350,14 @@ def run_ours(args):
     per_app = (len(kern) + 3) if prec_name == "fp64" else (len(kern) + 3)
     gpu_launches = K * (2 * per_app + 5)
 
+    # float64 arm of the metric (same GPU) and the spectral-error check
+    fp64 = None
+    check = None
+    if prec_name == "mixed":
+        fp64, check = fp64_arm_and_check(args, ens, spec, syms, spaces, bid, dev, local)
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(ens, spec, prec_name, K, W)
+        e2e = measure_e2e(ens, spec, prec_name, K, W, not args.no_reorth)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(ens, 15.0, 2)
@@ -354,9 +369,12 @@ def run_ours(args):
                 "precision": prec_name,
                 "config": {"workload": args.workload, "M": M, "N": N, "n_syms": spec["n_syms"],
                            "lanczos": "bi-Lanczos (2 applications/step)",
+                           "reorth": "none" if args.no_reorth else
+                                     "full re-biorthogonalisation against the stored basis (float64)",
                            "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (ensemble %.0f MB)" % (2 * R * M * 8 / 1e6)},
                 "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+                "fp64_gpu": fp64, "accuracy_vs_fp64": check,
                 "clocks": clocks, "gpu_launches": gpu_launches,
                 "flops_per_application": flops_app}
         print(json.dumps(line), flush=True)
@@ -364,7 +382,98 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def measure_e2e(ens, spec, prec_name, K, W):
+def lanczos_coeffs(lib, nat, ctx, prec, n, dev, M, P, reorth=1, eps=0.0):
+    """n bi-Lanczos steps from the bench's start vector; returns (a, b, c, seconds)."""
+    import torch
+    from tdscha_gb300.synthetic import random_R1
+    cap = n + 2
+    Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+    Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+    psi = np.zeros(P)
+    psi[:M] = random_R1(M, 11)
+    if eps:
+        psi[:M] *= 1 + eps * np.random.default_rng(1).standard_normal(M)
+    first = torch.from_numpy(psi / np.sqrt(psi.dot(psi))).to(dev)
+    Qd[0].copy_(first)
+    Pd[0].copy_(first)
+    hist = np.zeros(4 * cap)
+    hist[3] = 1.0
+    done, conv = ctypes.c_int(0), ctypes.c_int(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nat.check(lib.tdscha_lanczos_run(ctx.handle, Qd.data_ptr(), Pd.data_ptr(), cap, 0, n, 0, prec,
+                                     reorth, nat.dp(hist), ctypes.byref(done), ctypes.byref(conv),
+                                     torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    k = done.value
+    h = hist[: 4 * (k + 1)].reshape(-1, 4)
+    nb = k - 1 if conv.value else k
+    return h[:k, 0].copy(), h[:nb, 1].copy(), h[:nb, 2].copy(), dt
+
+
+def spectral(a, b, c, wgrid, smear):
+    """-Im G(w) of a bi-Lanczos run (continued fraction with terminator, in numpy)."""
+    n = len(a)
+    a_m, b_m, c_m = a[-1], b[-1], c[-1]
+    dd = a_m - wgrid ** 2
+    disc = dd ** 2 - 4 * b_m * c_m
+    sq = np.sqrt(disc + 0j)
+    gp, gm = (dd + sq) / (2 * b_m * c_m), (dd - sq) / (2 * b_m * c_m)
+    g = np.where(np.abs(gp) < np.abs(gm), gp, gm)
+    for i in range(n - 2, -1, -1):
+        g = 1.0 / (a[i] - wgrid ** 2 + 2j * wgrid * smear - b[i] * c[i] * g)
+    return -g.imag
+
+
+def fp64_arm_and_check(args, ens, spec, syms, spaces, bid, dev, local):
+    """Steps/s of the float64 path on the same GPU, and the mixed path's error
+    against it: each Lanczos coefficient and the spectral function on a
+    2000-point grid (0-700 cm^-1, 5 cm^-1 smearing) after the workload's
+    full step count."""
+    from tdscha_gb300 import _native as nat
+    lib = nat.load()
+    M = spec["M"]
+    n_check = args.check_steps if args.check_steps is not None else spec["steps"]
+    ctx64 = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                        with_mixed=True)
+    ctx64.set_options(False, False, False, False, False, 0.0)
+    P = ctx64.P
+    out = {}
+    reorth = 0 if args.no_reorth else 1
+    # float64 timing (K_fp64 steps after one warm-up step)
+    lanczos_coeffs(lib, nat, ctx64, nat.PREC_FP64, 1, dev, M, P, reorth)
+    _, _, _, dt = lanczos_coeffs(lib, nat, ctx64, nat.PREC_FP64, args.fp64_steps, dev, M, P,
+                                 reorth)
+    out["fp64"] = {"value": args.fp64_steps / dt, "unit": UNIT, "steps": args.fp64_steps,
+                   "timer": "host wall clock around synchronised tdscha_lanczos_run"}
+    check = None
+    if n_check > 0:
+        a64, b64, c64, t64 = lanczos_coeffs(lib, nat, ctx64, nat.PREC_FP64, n_check, dev, M, P,
+                                            reorth)
+        amx, bmx, cmx, tmx = lanczos_coeffs(lib, nat, ctx64, nat.PREC_MIXED, n_check, dev, M, P,
+                                            reorth)
+        w = np.linspace(0.0, 700.0, 2000) / 109691.40235
+        sm = 5.0 / 109691.40235
+        A64 = spectral(a64, b64, c64, w, sm)
+        Amx = spectral(amx, bmx, cmx, w, sm)
+        n = min(len(a64), len(amx))
+        ra = np.abs(amx[:n] - a64[:n]) / np.abs(a64[:n])
+        nb = min(len(b64), len(bmx))
+        rb = np.abs(bmx[:nb] - b64[:nb]) / np.abs(b64[:nb])
+        check = {"steps": n_check,
+                 "spectral_rel_err": float(np.abs(Amx - A64).max() / np.abs(A64).max()),
+                 "a_rel_err_max": float(ra.max()), "a_rel_err_first20": float(ra[:20].max()),
+                 "b_rel_err_max": float(rb.max()), "b_rel_err_first20": float(rb[:20].max()),
+                 "fp64_run_s": t64, "mixed_run_s": tmx,
+                 "grid": "2000 points 0-700 cm^-1, smearing 5 cm^-1, terminator on",
+                 "reorth": bool(reorth)}
+        out["full_run_steps_per_s"] = {"fp64": n_check / t64, "mixed": n_check / tmx}
+    ctx64.close()
+    return out, check
+
+
+def measure_e2e(ens, spec, prec_name, K, W, reorth):
     """Public API end to end: host ensemble -> Lanczos.run_FT(K) -> host coefficients."""
     import torch
     from tdscha_gb300.DynamicalLanczos import Lanczos
@@ -375,6 +484,7 @@ def measure_e2e(ens, spec, prec_name, K, W):
         lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
                                    use_wigner=False, precision=prec_name)
         lanc.init(use_symmetries=False)
+        lanc.full_reorth = reorth
         lanc.prepare_perturbation(random_R1(M, 11), masses_exp=0)
         lanc.run_FT(nsteps, verbose=False)
         g = lanc.get_green_function_continued_fraction(np.linspace(0, 600, 2000) / 109691.40235,

@@ -2,7 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -43,7 +43,7 @@ void set_error(const char *fmt, ...);
         if (_rc != TDSCHA_OK) return _rc;                                            \
     } while (0)
 
-// Split-bf16 copies of the ensemble used by the tensor-core path.  Rows are
+// Two-limb fp16 copies of the ensemble used by the tensor-core path.  Rows are
 // image rows r = i*S + j (configuration-major, like the reference's bigindex,
 // tdscha_core.jl:212-238).  Mp is M padded to the tile width; Rp is R padded
 // to the K block of the second GEMM.
@@ -51,14 +51,14 @@ struct MixedStore {
     int Mp = 0;
     long Rp = 0;
     // row layout (R x Mp): A operand of V = D Y1, and the epilogue's rows
-    __nv_bfloat16 *d_hi = nullptr, *d_lo = nullptr;
+    __half *d_hi = nullptr, *d_lo = nullptr;
     float *g32 = nullptr;    // g = f_psi * f rows (fp32)      R x Mp
     // transposed layout (Mp x Rp): operands of G = U^T W
-    __nv_bfloat16 *ut_hi = nullptr, *ut_lo = nullptr;   // U^T, U = f_Y * D
+    __half *ut_hi = nullptr, *ut_lo = nullptr;          // U^T, U = f_Y * D
     float *ft32 = nullptr;                               // F^T (fp32)
-    float *ut32 = nullptr;                               // U^T (fp32 value hi+lo)
-    __nv_bfloat16 *wt_hi = nullptr, *wt_lo = nullptr;   // W^T, rebuilt per call
-    __nv_bfloat16 *y1_hi = nullptr, *y1_lo = nullptr;   // Y1 (Mp x Mp), per call
+    float *ut32 = nullptr;                               // U^T (fp32)
+    __half *wt_hi = nullptr, *wt_lo = nullptr;          // W^T, rebuilt per call
+    __half *y1_hi = nullptr, *y1_lo = nullptr;          // Y1 (Mp x Mp), per call
     float *qp = nullptr;          // per-column-tile partial q, p  (ntile x 2 x R)
     float *gpart = nullptr;       // split-K partial G            (nsplit x Mp x Mp)
     int nsplit = 0;
@@ -102,6 +102,9 @@ struct tdscha_ctx {
     double *scal = nullptr;     // device scalars of the recurrence
     double *hist_dev = nullptr; // device copy of the coefficient history
     int hist_cap = 0;
+    double *pqn = nullptr;      // p_j . q_j of the stored basis (full reorthogonalisation)
+    double *rcoef = nullptr;    // projection coefficients (2 per basis vector)
+    int pqn_cap = 0;
     double *host_pinned = nullptr;
     int nblk_dot = 0;
     tdscha::MixedStore mx;

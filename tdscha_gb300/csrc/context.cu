@@ -84,7 +84,7 @@ static void ctx_free(tdscha_ctx *c) {
     double *bufs[] = {c->w, c->fY, c->fpsi, c->rho, c->Yw, c->ReAw, c->D, c->F, c->pc,
                       c->R1, c->Y1, c->f, c->d2v, c->qp_part, c->alpha, c->beta, c->c1,
                       c->c2, c->gpart, c->fpart, c->Lq, c->pL, c->rk, c->sk, c->mask,
-                      c->dots, c->scal, c->hist_dev};
+                      c->dots, c->scal, c->hist_dev, c->pqn, c->rcoef};
     for (double *p : bufs)
         if (p) cudaFree(p);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);

@@ -309,14 +309,13 @@ __global__ void k_normalize(const double *__restrict__ rk, const double *__restr
 }
 
 // Full re-biorthogonalisation of the new pair (q_{k+1}, p_{k+1}) against the
-// stored basis: q -= sum_j (p_j.q) q_j ; p -= sum_j (q_j.p) p_j with the
-// biorthogonality weights p_j.q_j measured on the stored vectors (one
-// classical Gram-Schmidt pass; the recurrence scalars are not changed).
-__global__ void k_proj_coeffs(const double *__restrict__ Qb, const double *__restrict__ Pb,
-                              const double *__restrict__ qn, const double *__restrict__ pn,
-                              const double *__restrict__ mask, long n, int nvec, long ld,
-                              double *__restrict__ part) {
-    // one block per basis vector j: part[2j] = p_j.q_new, part[2j+1] = q_j.p_new
+// stored basis: q -= sum_j (p_j.q / p_j.q_j) q_j and p -= sum_j (q_j.p / p_j.q_j) p_j
+// (one classical Gram-Schmidt pass; the recurrence scalars are not changed).
+// One block per basis vector for the dot products.
+__global__ void k_proj_dots(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                            const double *__restrict__ qn, const double *__restrict__ pn,
+                            const double *__restrict__ mask, long n, long ld,
+                            double *__restrict__ part) {
     __shared__ double sh[32];
     int j = blockIdx.x;
     const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
@@ -332,28 +331,39 @@ __global__ void k_proj_coeffs(const double *__restrict__ Qb, const double *__res
     if (threadIdx.x == 0) part[2 * j + 1] = t;
 }
 
+__global__ void k_proj_scale(double *__restrict__ coef, const double *__restrict__ pqn, int nvec) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nvec) {
+        double inv = 1.0 / pqn[j];
+        coef[2 * j] *= inv;
+        coef[2 * j + 1] *= inv;
+    }
+}
+
+constexpr int kProjMax = 2048;   // coefficients cached in shared memory per pass
 __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__restrict__ Pb,
-                             const double *__restrict__ coef, const double *__restrict__ pqn,
-                             long n, int nvec, long ld, double *__restrict__ qn,
-                             double *__restrict__ pn) {
-    // coef[2j], coef[2j+1] as written by k_proj_coeffs; pqn[j] = p_j.q_j
+                             const double *__restrict__ coef, long n, int j0, int nvec, long ld,
+                             double *__restrict__ qn, double *__restrict__ pn) {
+    __shared__ double cs[2 * kProjMax];
+    for (int t = threadIdx.x; t < 2 * nvec; t += blockDim.x) cs[t] = coef[2 * j0 + t];
+    __syncthreads();
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         double q = qn[e], p = pn[e];
         for (int j = 0; j < nvec; ++j) {
-            double inv = 1.0 / pqn[j];
-            q -= coef[2 * j] * inv * Qb[(long)j * ld + e];
-            p -= coef[2 * j + 1] * inv * Pb[(long)j * ld + e];
+            q = fma(-cs[2 * j], Qb[(long)(j0 + j) * ld + e], q);
+            p = fma(-cs[2 * j + 1], Pb[(long)(j0 + j) * ld + e], p);
         }
         qn[e] = q;
         pn[e] = p;
     }
 }
 
+// p_j . q_j for j in [j0, j1)
 __global__ void k_pq_diag(const double *__restrict__ Qb, const double *__restrict__ Pb,
-                          const double *__restrict__ mask, long n, long ld,
+                          const double *__restrict__ mask, long n, long ld, int j0,
                           double *__restrict__ out) {
     __shared__ double sh[32];
-    int j = blockIdx.x;
+    int j = j0 + blockIdx.x;
     double a = 0;
     for (long e = threadIdx.x; e < n; e += blockDim.x) {
         double m = mask ? mask[e] : 1.0;
@@ -407,10 +417,18 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
     }
     TDS_CUDA(cudaMemcpyAsync(ctx->hist_dev, hist, sizeof(double) * 4 * (start_step + 1),
                              cudaMemcpyHostToDevice, st));
-    double *pqn = nullptr, *coef = nullptr;
     if (full_reorth) {
-        TDS_CUDA(cudaMalloc(&pqn, sizeof(double) * (capacity + 1)));
-        TDS_CUDA(cudaMalloc(&coef, sizeof(double) * 2 * (capacity + 1)));
+        if (ctx->pqn_cap < capacity + 1) {
+            if (ctx->pqn) cudaFree(ctx->pqn);
+            if (ctx->rcoef) cudaFree(ctx->rcoef);
+            ctx->pqn = ctx->rcoef = nullptr;
+            TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
+            TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1)));
+            ctx->pqn_cap = capacity + 1;
+        }
+        // weights of the vectors already stored
+        k_pq_diag<<<start_step + 1, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0, ctx->pqn);
+        TDS_CHECK_LAUNCH();
     }
     int rc = TDSCHA_OK;
     int nb = std::max(1, std::min(ceil_div(P, kDotThreads), nblk));
@@ -463,15 +481,16 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         hist[4 * (k + 1) + 3] = sc[SC_SNORM];
         if (full_reorth) {
             int nvec = k + 1;
-            k_pq_diag<<<nvec, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, pqn);
-            k_proj_coeffs<<<nvec, 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, nvec, P, coef);
-            k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_P, coef, pqn, P, nvec, P, qn, pn);
+            k_proj_dots<<<nvec, 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P, ctx->rcoef);
+            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(ctx->rcoef, ctx->pqn, nvec);
+            for (int j0 = 0; j0 < nvec; j0 += kProjMax)
+                k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
+                                                 std::min(kProjMax, nvec - j0), P, qn, pn);
+            k_pq_diag<<<1, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, k + 1, ctx->pqn);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) { set_error("reorth launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
         }
     }
-    if (pqn) cudaFree(pqn);
-    if (coef) cudaFree(coef);
     return rc;
 }
 

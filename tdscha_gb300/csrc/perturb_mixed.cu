@@ -3,10 +3,20 @@
 // Same GEMM form as the float64 path (perturb_fp64.cu):
 //   stage A   V = D Y1           (R x M x M)   -> per-row q, p, s, t in the epilogue
 //   stage B   G = U^T W          (M x M x R)   -> split-K fp32 partial tiles
-// with every operand held as a pair of bf16 values (x = hi + lo, 16
-// significant bits) and each product taken as hi*hi + hi*lo + lo*hi
-// (three tcgen05.mma per K step into one fp32 TMEM accumulator).  The
-// recurrence around it stays in float64.
+// Every operand row of the K-major layout is scaled into [-1, 1] by a per-mode
+// (or per-row) factor and held as two fp16 limbs,
+//   x = hi + lo * 2^-11,   hi = fp16(x),   lo = fp16((x - hi) * 2^11),
+// about 22 significant bits; the low limb is kept at the magnitude of the high
+// one so it never falls into the fp16 subnormal range.  Each product is
+// hi*hi into TMEM accumulator D0 and hi*lo + lo*hi into accumulator D1 (three
+// tcgen05.mma per K step); the epilogue forms D0 + 2^-11 D1 and undoes the
+// scales.  The Lanczos recurrence around it stays in float64.
+//
+// Scales: stage A multiplies the K (mode) axis by 1/sd_m on D and by sd_m on
+// Y1 (sd_m = max_r |D[r][m]|, fixed per ensemble), and each Y1 row n by 1/t_n
+// (its max, per call); stage B scales U^T row a by 1/su_a (su_a = f_Y,a sd_a)
+// and W^T row b by 1/sw_b, an upper bound of max_r |W[r][b]| from the maxima
+// of alpha, beta, F and U.
 //
 // Kernel anatomy (k_gemm_tc): one CTA = one 128 x BN output tile, 128 threads.
 //   warp 0 lane 0  TMA producer: cp.async.bulk.tensor 2D loads of the four
@@ -21,6 +31,7 @@
 // frees its TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
 #include <cmath>
 
@@ -29,11 +40,14 @@
 namespace tdscha {
 
 constexpr int kBM = 128;          // tile rows (TMEM lanes)
-constexpr int kBK = 64;           // K block: 64 bf16 = one 128-byte swizzle row
+constexpr int kBK = 64;           // K block: 64 fp16 = one 128-byte swizzle row
 constexpr uint32_t kABytes = kBM * kBK * 2;
 constexpr int kBNB = 128;         // stage B tile width
 constexpr int kStagesA = 2;
 constexpr int kStagesB = 3;
+constexpr int kSplitRows = 2048;  // stage B rows per split (fp32 accumulation length)
+constexpr float kLoScale = 2048.f;
+constexpr float kLoInv = 1.f / 2048.f;
 constexpr long long kDefaultBudget = 4000000000LL;   // ~2 s at 2 GHz
 
 struct TmaQuad {
@@ -49,11 +63,12 @@ struct GemmArgs {
     int ldG;            // stage B: leading dimension of the partial tiles
     int ntile;          // stage B: tiles per dimension
     // stage A epilogue
-    const __nv_bfloat16 *d_hi, *d_lo;
-    const float *g32;
+    const float *d32, *g32;       // d and g = f_psi * f rows (R x Mp)
     const float *vec_s, *vec_t;   // f_Y*R1 and R1/f_psi (Mp)
+    const float *tcol;            // Y1 row scales t_n (Mp)
     float *qpst;                  // [nct][4][R]
     // stage B epilogue
+    const float *su, *sw;         // row scales of U^T and W^T (Mp)
     float *gpart;
     // bounded waits
     int *err;
@@ -116,17 +131,15 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor, kind::f16: A = B = bf16, D = f32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4)                      // D format f32
-           | (1u << 7)                    // A format bf16
-           | (1u << 10)                   // B format bf16
+// Instruction descriptor, kind::f16: A = B = fp16, D = f32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4)                      // D format f32 (A, B format fields 0 = fp16)
            | ((uint32_t)(N >> 3) << 17)   // N / 8
            | ((uint32_t)(M >> 4) << 24);  // M / 16
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
@@ -160,6 +173,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
           "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
           "=r"(v[31])
         : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
@@ -182,6 +198,16 @@ struct TmemCols {
     static constexpr int value = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : N <= 256 ? 256 : 512;
 };
 
+// D0 + 2^-11 D1 for 32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_combined(uint32_t lane_base, int col, int bn, float (&o)[32]) {
+    uint32_t v0[32], v1[32];
+    tmem_ld32(lane_base + col, v0);
+    tmem_ld32(lane_base + bn + col, v1);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 32; ++j) o[j] = fmaf(__uint_as_float(v1[j]), kLoInv, __uint_as_float(v0[j]));
+}
+
 // ------------------------------------------------------------ the GEMM
 // MODE 0: stage A (row dots epilogue).  MODE 1: stage B (split-K tile store).
 template <int BN, int STAGES, int MODE>
@@ -189,8 +215,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
                                                      const GemmArgs args) {
     constexpr uint32_t kBBytes = BN * kBK * 2;
     constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
-    constexpr int kCols = TmemCols<BN>::value;
-    constexpr uint32_t kIdesc = idesc_bf16(kBM, BN);
+    constexpr int kCols = TmemCols<2 * BN>::value;
+    constexpr uint32_t kIdesc = idesc_f16(kBM, BN);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -257,7 +283,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
                 mbar_wait(full0 + 8 * (i % STAGES), (i / STAGES) & 1, kDefaultBudget);
         }
     } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer
+        // ---- MMA issuer: D0 += hi*hi, D1 += hi*lo + lo*hi
+        const uint32_t d0 = tmem, d1 = tmem + BN;
         for (int i = 0; i < nkb; ++i) {
             int s = i % STAGES;
             if (!mbar_wait(full0 + 8 * s, (i / STAGES) & 1, budget)) {
@@ -272,9 +299,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
                 uint64_t al = sdesc_sw128(base + kABytes + kk * 32);
                 uint64_t bh = sdesc_sw128(base + 2 * kABytes + kk * 32);
                 uint64_t bl = sdesc_sw128(base + 2 * kABytes + kBBytes + kk * 32);
-                mma_bf16(tmem, ah, bh, kIdesc, (i | kk) != 0);
-                mma_bf16(tmem, ah, bl, kIdesc, 1);
-                mma_bf16(tmem, al, bh, kIdesc, 1);
+                uint32_t acc = (i | kk) != 0;
+                mma_f16(d0, ah, bh, kIdesc, acc);
+                mma_f16(d1, ah, bl, kIdesc, acc);
+                mma_f16(d1, al, bh, kIdesc, 1);
             }
             mma_commit(empty0 + 8 * s);
         }
@@ -297,34 +325,24 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
         float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
 #pragma unroll 1
         for (int ch = 0; ch < BN / 32; ++ch) {
-            uint32_t v[32];
-            tmem_ld32(lane_base + ch * 32, v);
+            float v[32];
+            tmem_combined(lane_base, ch * 32, BN, v);
             int col0 = brow + ch * 32;
             if (row < args.R && have_acc) {
-                const uint4 *ph = reinterpret_cast<const uint4 *>(args.d_hi + row * args.Mp + col0);
-                const uint4 *pl = reinterpret_cast<const uint4 *>(args.d_lo + row * args.Mp + col0);
+                const float4 *pd = reinterpret_cast<const float4 *>(args.d32 + row * args.Mp + col0);
                 const float4 *pg = reinterpret_cast<const float4 *>(args.g32 + row * args.Mp + col0);
 #pragma unroll
-                for (int j8 = 0; j8 < 4; ++j8) {
-                    uint4 h = ph[j8], l = pl[j8];
-                    const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&h);
-                    const __nv_bfloat162 *l2 = reinterpret_cast<const __nv_bfloat162 *>(&l);
-                    float4 g0 = pg[2 * j8], g1 = pg[2 * j8 + 1];
-                    float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+                for (int j4 = 0; j4 < 8; ++j4) {
+                    float4 d4 = pd[j4], g4 = pg[j4];
+                    float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
-                        float2 hf = __bfloat1622float2(h2[e]), lf = __bfloat1622float2(l2[e]);
-                        float d0 = hf.x + lf.x, d1 = hf.y + lf.y;
-                        int j = j8 * 8 + 2 * e;
-                        float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
-                        q = fmaf(d0, v0, q);
-                        q = fmaf(d1, v1, q);
-                        p = fmaf(gg[2 * e], v0, p);
-                        p = fmaf(gg[2 * e + 1], v1, p);
-                        sacc = fmaf(args.vec_s[col0 + j], d0, sacc);
-                        sacc = fmaf(args.vec_s[col0 + j + 1], d1, sacc);
-                        tacc = fmaf(args.vec_t[col0 + j], gg[2 * e], tacc);
-                        tacc = fmaf(args.vec_t[col0 + j + 1], gg[2 * e + 1], tacc);
+                        int j = 4 * j4 + e, c = col0 + j;
+                        float vv = v[j] * args.tcol[c];
+                        q = fmaf(dd[e], vv, q);
+                        p = fmaf(gg[e], vv, p);
+                        sacc = fmaf(args.vec_s[c], dd[e], sacc);
+                        tacc = fmaf(args.vec_t[c], gg[e], tacc);
                     }
                 }
             }
@@ -339,22 +357,27 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
         }
     } else {
         long a = arow + warp * 32 + lane;
+        float sa = a < args.Mp ? args.su[a] : 0.f;
         float *dst = args.gpart + (long)blockIdx.y * args.ldG * args.ldG + a * args.ldG + brow;
 #pragma unroll 1
         for (int ch = 0; ch < BN / 32; ++ch) {
-            uint32_t v[32];
-            tmem_ld32(lane_base + ch * 32, v);
+            float v[32];
+            tmem_combined(lane_base, ch * 32, BN, v);
             float4 *d4 = reinterpret_cast<float4 *>(dst + ch * 32);
+            int c0 = brow + ch * 32;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                float4 o;
+                float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (have_acc) {
-                    o.x = __uint_as_float(v[4 * j]);
-                    o.y = __uint_as_float(v[4 * j + 1]);
-                    o.z = __uint_as_float(v[4 * j + 2]);
-                    o.w = __uint_as_float(v[4 * j + 3]);
-                } else {
-                    o = make_float4(0.f, 0.f, 0.f, 0.f);
+                    int c = c0 + 4 * j;
+                    float s0 = c < args.Mp ? args.sw[c] : 0.f;
+                    float s1 = c + 1 < args.Mp ? args.sw[c + 1] : 0.f;
+                    float s2 = c + 2 < args.Mp ? args.sw[c + 2] : 0.f;
+                    float s3 = c + 3 < args.Mp ? args.sw[c + 3] : 0.f;
+                    o.x = v[4 * j] * sa * s0;
+                    o.y = v[4 * j + 1] * sa * s1;
+                    o.z = v[4 * j + 2] * sa * s2;
+                    o.w = v[4 * j + 3] * sa * s3;
                 }
                 d4[j] = o;
             }
@@ -366,49 +389,97 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
 }
 
 // --------------------------------------------------------- data movers
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
-    hi = __float2bfloat16_rn(x);
-    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+__device__ __forceinline__ void split_f16(float x, __half &hi, __half &lo) {
+    hi = __float2half_rn(x);
+    lo = __float2half_rn((x - __half2float(hi)) * kLoScale);
+}
+
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
+    // non-negative floats order like their bit patterns
+    atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+}
+
+// Column maxima of |D| and |F| (R x M float64) for the per-mode scales.
+__global__ void k_colmax(const double *__restrict__ D, const double *__restrict__ F, long R,
+                         int M, long rows_per_block, float *__restrict__ dmax,
+                         float *__restrict__ fmax) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    long rb = blockIdx.y * rows_per_block, re = min(R, rb + rows_per_block);
+    float a = 0.f, b = 0.f;
+    for (long r = rb; r < re; ++r) {
+        a = fmaxf(a, (float)fabs(D[r * M + m]));
+        b = fmaxf(b, (float)fabs(F[r * M + m]));
+    }
+    atomic_max_pos(dmax + m, a);
+    atomic_max_pos(fmax + m, b);
+}
+
+// Scales of the operands: sd (mode axis of stage A), su = f_Y sd (rows of
+// U^T), fmax (column maxima of F); zero columns get 1, padding gets 1 / 0.
+__global__ void k_scales(const float *__restrict__ dmax, const double *__restrict__ fY, int M,
+                         int Mp, float *__restrict__ sd, float *__restrict__ su,
+                         float *__restrict__ fmx) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= Mp) return;
+    if (m < M) {
+        float s = dmax[m] > 0.f ? dmax[m] : 1.f;
+        sd[m] = s;
+        float u = (float)(fY[m] * (double)s);
+        su[m] = u > 0.f ? u : 1.f;
+        if (!(fmx[m] > 0.f)) fmx[m] = 1.f;
+    } else {
+        sd[m] = 1.f;
+        su[m] = 1.f;
+        fmx[m] = 0.f;
+    }
 }
 
 // Resident operands from the float64 image rows D, F (R x M):
-//   d_hi/d_lo, g32       (R x Mp)  row layout, stage A operand and epilogue
-//   ut_hi/ut_lo, ft32    (Mp x Rp) transposed layout, stage B operands
+//   d_hi/d_lo  (R x Mp)  limbs of D[r][m] / sd_m   (stage A operand)
+//   d32, g32   (R x Mp)  D and f_psi * F in fp32    (stage A epilogue)
 __global__ void k_prep_rows(const double *__restrict__ D, const double *__restrict__ F,
-                            const double *__restrict__ fpsi, long R, int M, int Mp,
-                            __nv_bfloat16 *__restrict__ d_hi, __nv_bfloat16 *__restrict__ d_lo,
-                            float *__restrict__ g32) {
+                            const double *__restrict__ fpsi, const float *__restrict__ sd, long R,
+                            int M, int Mp, __half *__restrict__ d_hi, __half *__restrict__ d_lo,
+                            float *__restrict__ d32, float *__restrict__ g32) {
     long n = R * Mp;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         long r = e / Mp;
         int m = (int)(e % Mp);
-        float x = 0.f, g = 0.f;
+        float x = 0.f, g = 0.f, xs = 0.f;
         if (m < M) {
-            x = (float)D[r * M + m];
+            double dv = D[r * M + m];
+            x = (float)dv;
+            xs = (float)(dv / (double)sd[m]);
             g = (float)(fpsi[m] * F[r * M + m]);
         }
-        __nv_bfloat16 h, l;
-        split_bf16(x, h, l);
+        __half h, l;
+        split_f16(xs, h, l);
         d_hi[e] = h;
         d_lo[e] = l;
+        d32[e] = x;
         g32[e] = g;
     }
 }
 
-// transpose through shared memory: 32 x 32 tiles of (r, m)
+// Transposed operands (Mp x Rp) through 32 x 32 shared tiles:
+//   ut_hi/ut_lo  limbs of U[r][a] / su_a   (stage B A operand)
+//   ut32, ft32   U and F in fp32            (W build, force average)
 __global__ void k_prep_cols(const double *__restrict__ D, const double *__restrict__ F,
-                            const double *__restrict__ fY, long R, int M, long Rp,
-                            __nv_bfloat16 *__restrict__ ut_hi, __nv_bfloat16 *__restrict__ ut_lo,
+                            const double *__restrict__ fY, const float *__restrict__ su, long R,
+                            int M, long Rp, __half *__restrict__ ut_hi, __half *__restrict__ ut_lo,
                             float *__restrict__ ut32, float *__restrict__ ft32) {
-    __shared__ float tu[32][33], tf[32][33];
+    __shared__ double tu[32][33];
+    __shared__ float tf[32][33];
     long r0 = (long)blockIdx.x * 32;
     int m0 = blockIdx.y * 32;
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
         long r = r0 + k;
         int m = m0 + threadIdx.x;
-        float u = 0.f, f = 0.f;
+        double u = 0.0;
+        float f = 0.f;
         if (r < R && m < M) {
-            u = (float)(fY[m] * D[r * M + m]);
+            u = fY[m] * D[r * M + m];
             f = (float)F[r * M + m];
         }
         tu[k][threadIdx.x] = u;
@@ -419,77 +490,125 @@ __global__ void k_prep_cols(const double *__restrict__ D, const double *__restri
         int m = m0 + k;
         long r = r0 + threadIdx.x;
         if (r < Rp) {
-            float u = tu[threadIdx.x][k];
-            __nv_bfloat16 h, l;
-            split_bf16(u, h, l);
+            double u = tu[threadIdx.x][k];
+            float s = (m < M) ? su[m] : 1.f;
+            __half h, l;
+            split_f16((float)(u / (double)s), h, l);
             long o = (long)m * Rp + r;
             ut_hi[o] = h;
             ut_lo[o] = l;
-            ut32[o] = __bfloat162float(h) + __bfloat162float(l);
+            ut32[o] = (float)u;
             ft32[o] = tf[threadIdx.x][k];
         }
     }
 }
 
-// Y1 (symmetric, float64 M x M) -> split bf16 (Mp x Mp, zero padded) and the
-// two epilogue vectors f_Y*R1 and R1/f_psi.
+// Per call: Y1 row n scaled by sd (mode axis) and by 1/t_n, t_n its max; one
+// block per row.  Also the epilogue vectors f_Y*R1, R1/f_psi, and the reset
+// of the alpha / beta maxima.
 __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restrict__ R1,
-                          const double *__restrict__ fY, const double *__restrict__ fpsi, int M,
-                          int Mp, __nv_bfloat16 *__restrict__ y_hi,
-                          __nv_bfloat16 *__restrict__ y_lo, float *__restrict__ vs,
-                          float *__restrict__ vt) {
-    long n = (long)Mp * Mp;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        int a = (int)(e / Mp), b = (int)(e % Mp);
-        float x = (a < M && b < M) ? (float)Y1[(long)a * M + b] : 0.f;
-        __nv_bfloat16 h, l;
-        split_bf16(x, h, l);
-        y_hi[e] = h;
-        y_lo[e] = l;
-        if (e < Mp) {
-            int m = (int)e;
-            vs[m] = m < M ? (float)(fY[m] * R1[m]) : 0.f;
-            vt[m] = m < M ? (float)(R1[m] / fpsi[m]) : 0.f;
-        }
+                          const double *__restrict__ fY, const double *__restrict__ fpsi,
+                          const float *__restrict__ sd, int M, int Mp, __half *__restrict__ y_hi,
+                          __half *__restrict__ y_lo, float *__restrict__ tcol,
+                          float *__restrict__ vs, float *__restrict__ vt,
+                          float *__restrict__ absmax) {
+    __shared__ float red[32];
+    int n = blockIdx.x;
+    float mx = 0.f;
+    for (int m = threadIdx.x; m < Mp; m += blockDim.x)
+        if (n < M && m < M) mx = fmaxf(mx, fabsf((float)(Y1[(long)n * M + m] * (double)sd[m])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) red[0] = v;
+    }
+    __syncthreads();
+    float t = red[0] > 0.f ? red[0] : 1.f;
+    double inv = 1.0 / (double)t;
+    for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
+        float x = (n < M && m < M) ? (float)(Y1[(long)n * M + m] * (double)sd[m] * inv) : 0.f;
+        __half h, l;
+        split_f16(x, h, l);
+        y_hi[(long)n * Mp + m] = h;
+        y_lo[(long)n * Mp + m] = l;
+    }
+    if (threadIdx.x == 0) {
+        tcol[n] = n < M ? t : 0.f;
+        vs[n] = n < M ? (float)(fY[n] * R1[n]) : 0.f;
+        vt[n] = n < M ? (float)(R1[n] / fpsi[n]) : 0.f;
+        if (n == 0) { absmax[0] = 0.f; absmax[1] = 0.f; }
     }
 }
 
-// Row scalars from the stage A partials (sums in float64).
+// Row scalars from the stage A partials (sums in float64), and max |alpha|,
+// max |beta| for the W scales.
 __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, int S,
                              const double *__restrict__ rho, int apply_d4,
-                             float4 *__restrict__ abcc) {
+                             float4 *__restrict__ abcc, float *__restrict__ absmax) {
     long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (r >= R) return;
-    double q = 0, p = 0, s = 0, t = 0;
-    for (int ct = 0; ct < nct; ++ct) {
-        const float *o = qpst + (long)ct * 4 * R;
-        q += o[r];
-        p += o[R + r];
-        s += o[2 * R + r];
-        t += o[3 * R + r];
+    float ma = 0.f, mb = 0.f;
+    if (r < R) {
+        double q = 0, p = 0, s = 0, t = 0;
+        for (int ct = 0; ct < nct; ++ct) {
+            const float *o = qpst + (long)ct * 4 * R;
+            q += o[r];
+            p += o[R + r];
+            s += o[2 * R + r];
+            t += o[3 * R + r];
+        }
+        double rw = rho[r / S];
+        double d4 = apply_d4 ? 1.0 : 0.0;
+        float4 v = make_float4((float)(rw * (s / 3 - d4 * q / 8)), (float)(rw * (t / 3 - d4 * p / 4)),
+                               (float)(-rw * q / 6), (float)(-rw * p / 3));
+        abcc[r] = v;
+        ma = fabsf(v.x);
+        mb = fabsf(v.y);
     }
-    double rw = rho[r / S];
-    double d4 = apply_d4 ? 1.0 : 0.0;
-    abcc[r] = make_float4((float)(rw * (s / 3 - d4 * q / 8)), (float)(rw * (t / 3 - d4 * p / 4)),
-                          (float)(-rw * q / 6), (float)(-rw * p / 3));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_pos(absmax, ma);
+        atomic_max_pos(absmax + 1, mb);
+    }
 }
 
-// W^T[b][r] = alpha_r F^T[b][r] + beta_r/2 U^T[b][r] as split bf16, and the
-// force-average partials fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
+// W^T[b][r] = (alpha_r F^T[b][r] + beta_r/2 U^T[b][r]) / sw_b as fp16 limbs,
+// sw_b = max|alpha| fmax_b + max|beta|/2 su_b; and the force-average partials
+// fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
 constexpr int kWRows = 8;      // b rows per block
 constexpr int kWChunk = 2048;  // r per block
 __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
                                                 const float *__restrict__ ut32,
-                                                const float4 *__restrict__ abcc, long R, long Rp,
-                                                int M, __nv_bfloat16 *__restrict__ wt_hi,
-                                                __nv_bfloat16 *__restrict__ wt_lo,
+                                                const float4 *__restrict__ abcc,
+                                                const float *__restrict__ absmax,
+                                                const float *__restrict__ fmax,
+                                                const float *__restrict__ su, long R, long Rp,
+                                                int M, __half *__restrict__ wt_hi,
+                                                __half *__restrict__ wt_lo,
+                                                float *__restrict__ sw_out,
                                                 float *__restrict__ fpart) {
     __shared__ float red[kWRows][8];
     int b0 = blockIdx.x * kWRows;
     long r0 = (long)blockIdx.y * kWChunk;
-    float facc[kWRows];
+    const float amax = absmax[0], bmax = absmax[1];
+    float inv[kWRows], facc[kWRows];
 #pragma unroll
-    for (int k = 0; k < kWRows; ++k) facc[k] = 0.f;
+    for (int k = 0; k < kWRows; ++k) {
+        int b = b0 + k;
+        float sw = b < M ? amax * fmax[b] + 0.5f * bmax * su[b] : 1.f;
+        if (!(sw > 0.f)) sw = 1.f;
+        inv[k] = 1.f / sw;
+        facc[k] = 0.f;
+        if (blockIdx.y == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
+    }
     for (int it = 0; it < kWChunk / 256; ++it) {
         long r = r0 + it * 256 + threadIdx.x;
         if (r >= R) break;
@@ -500,9 +619,9 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
             if (b >= M) break;
             long o = (long)b * Rp + r;
             float f = ft32[o], u = ut32[o];
-            float x = w.x * f + 0.5f * w.y * u;
-            __nv_bfloat16 h, l;
-            split_bf16(x, h, l);
+            float x = (w.x * f + 0.5f * w.y * u) * inv[k];
+            __half h, l;
+            split_f16(x, h, l);
             wt_hi[o] = h;
             wt_lo[o] = l;
             facc[k] = fmaf(w.z, f, fmaf(w.w, u, facc[k]));
@@ -560,21 +679,22 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 2D bf16 tensor (inner x outer, row pitch inner*2 bytes), box 64 x box_rows,
+// 2D fp16 tensor (inner x outer, row pitch inner*2 bytes), box 64 x box_rows,
 // 128-byte swizzle, zero fill out of bounds.
 static int make_map(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer,
                     uint32_t box_rows) {
     auto fn = encode_fn();
     if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return TDSCHA_ERR_CUDA; }
-    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((inner * 2) & 15) || inner % kBK) {
-        set_error("tensor map: misaligned base or pitch");
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((inner * 2) & 15) || inner % kBK ||
+        box_rows == 0 || box_rows > 256) {
+        set_error("tensor map: misaligned base or pitch, or bad box");
         return TDSCHA_ERR_ARG;
     }
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * 2};
     cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides,
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides,
                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return TDSCHA_ERR_CUDA; }
@@ -597,7 +717,9 @@ static int choose_bn(int Mp) {
 struct MixedExtra {
     TmaQuad tmA, tmB;
     int bnA = 0;
-    float *vs = nullptr, *vt = nullptr;
+    float *sd = nullptr, *fmx = nullptr, *su = nullptr, *sw = nullptr, *tcol = nullptr;
+    float *vs = nullptr, *vt = nullptr, *absmax = nullptr;
+    float *d32 = nullptr;
     float4 *abcc = nullptr;
     float *fpart = nullptr;
     int nfchunk = 0;
@@ -623,7 +745,7 @@ int mixed_prepare(tdscha_ctx *c) {
     x->ldG = ((Mp + kBM - 1) / kBM) * kBM;
     x->ntB = x->ldG / kBM;
     x->nkbB = (int)(Rp / kBK);
-    int want = std::max(1, ceil_div(2 * 152, x->ntB * x->ntB));
+    int want = std::max(1, ceil_div(R, kSplitRows));
     want = std::min(want, x->nkbB);
     x->kbps = ceil_div(x->nkbB, want);
     mx.nsplit = ceil_div(x->nkbB, x->kbps);
@@ -631,6 +753,7 @@ int mixed_prepare(tdscha_ctx *c) {
     size_t rowN = (size_t)R * Mp, colN = (size_t)Mp * Rp;
     TDS_CUDA(cudaMalloc(&mx.d_hi, 2 * rowN));
     TDS_CUDA(cudaMalloc(&mx.d_lo, 2 * rowN));
+    TDS_CUDA(cudaMalloc(&x->d32, 4 * rowN));
     TDS_CUDA(cudaMalloc(&mx.g32, 4 * rowN));
     TDS_CUDA(cudaMalloc(&mx.ut_hi, 2 * colN));
     TDS_CUDA(cudaMalloc(&mx.ut_lo, 2 * colN));
@@ -642,21 +765,36 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cudaMalloc(&mx.y1_lo, 2 * (size_t)Mp * Mp));
     TDS_CUDA(cudaMalloc(&mx.qp, sizeof(float) * 4 * mx.nctile * R));
     TDS_CUDA(cudaMalloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldG));
-    TDS_CUDA(cudaMalloc(&x->vs, sizeof(float) * Mp));
-    TDS_CUDA(cudaMalloc(&x->vt, sizeof(float) * Mp));
+    float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw, &x->tcol, &x->vs, &x->vt};
+    for (float **v : vecs) TDS_CUDA(cudaMalloc(v, sizeof(float) * Mp));
+    TDS_CUDA(cudaMalloc(&x->absmax, sizeof(float) * 2));
     TDS_CUDA(cudaMalloc(&x->abcc, sizeof(float4) * R));
     TDS_CUDA(cudaMalloc(&x->fpart, sizeof(float) * (size_t)x->nfchunk * M));
     TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
     *mx.err_flag = 0;
     TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * colN));
     TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * colN));
+    TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * Mp));
     {
-        int nb = (int)std::min<long>((rowN + 255) / 256, 152L * 32);
-        k_prep_rows<<<nb, 256>>>(c->D, c->F, c->fpsi, R, M, Mp, mx.d_hi, mx.d_lo, mx.g32);
+        float *dmax = nullptr;
+        TDS_CUDA(cudaMalloc(&dmax, sizeof(float) * Mp));
+        TDS_CUDA(cudaMemset(dmax, 0, sizeof(float) * Mp));
+        TDS_CUDA(cudaMemset(x->fmx, 0, sizeof(float) * Mp));
+        long rpb = 512;
+        dim3 g(ceil_div(M, 128), ceil_div(R, rpb));
+        k_colmax<<<g, 128>>>(c->D, c->F, R, M, rpb, dmax, x->fmx);
         TDS_CHECK_LAUNCH();
-        dim3 g(ceil_div(Rp, 32), Mp / 32);
-        k_prep_cols<<<g, dim3(32, 8)>>>(c->D, c->F, c->fY, R, M, Rp, mx.ut_hi, mx.ut_lo, mx.ut32,
-                                        mx.ft32);
+        k_scales<<<ceil_div(Mp, 128), 128>>>(dmax, c->fY, M, Mp, x->sd, x->su, x->fmx);
+        TDS_CHECK_LAUNCH();
+        TDS_CUDA(cudaDeviceSynchronize());
+        cudaFree(dmax);
+        int nb = (int)std::min<long>((rowN + 255) / 256, 152L * 32);
+        k_prep_rows<<<nb, 256>>>(c->D, c->F, c->fpsi, x->sd, R, M, Mp, mx.d_hi, mx.d_lo, x->d32,
+                                 mx.g32);
+        TDS_CHECK_LAUNCH();
+        dim3 gc(ceil_div(Rp, 32), Mp / 32);
+        k_prep_cols<<<gc, dim3(32, 8)>>>(c->D, c->F, c->fY, x->su, R, M, Rp, mx.ut_hi, mx.ut_lo,
+                                         mx.ut32, mx.ft32);
         TDS_CHECK_LAUNCH();
     }
     TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
@@ -694,10 +832,10 @@ int mixed_release(tdscha_ctx *c) {
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (MixedExtra *x = extra(c)) {
-        if (x->vs) cudaFree(x->vs);
-        if (x->vt) cudaFree(x->vt);
-        if (x->abcc) cudaFree(x->abcc);
-        if (x->fpart) cudaFree(x->fpart);
+        void *xb[] = {x->sd, x->fmx, x->su, x->sw, x->tcol, x->vs, x->vt, x->absmax, x->d32,
+                      x->abcc, x->fpart};
+        for (void *p : xb)
+            if (p) cudaFree(p);
         delete x;
     }
     if (mx.err_flag) cudaFreeHost(mx.err_flag);
@@ -725,20 +863,19 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
     {
         ProfScope ps(c, 5, st);
-        int nb = std::max(1, std::min(ceil_div((long)Mp * Mp, 256), 1024));
-        k_prep_y1<<<nb, 256, 0, st>>>(c->Y1, c->R1, c->fY, c->fpsi, M, Mp, mx.y1_hi, mx.y1_lo,
-                                      x->vs, x->vt);
+        k_prep_y1<<<Mp, 256, 0, st>>>(c->Y1, c->R1, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi,
+                                      mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax);
         TDS_CHECK_LAUNCH();
     }
     GemmArgs ga{};
     ga.nkb = Mp / kBK;
     ga.R = R;
     ga.Mp = Mp;
-    ga.d_hi = mx.d_hi;
-    ga.d_lo = mx.d_lo;
+    ga.d32 = x->d32;
     ga.g32 = mx.g32;
     ga.vec_s = x->vs;
     ga.vec_t = x->vt;
+    ga.tcol = x->tcol;
     ga.qpst = mx.qp;
     ga.err = err_dev;
     ga.budget = x->budget;
@@ -761,14 +898,14 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 1, st);
         k_rows_mixed<<<ceil_div(R, 256), 256, 0, st>>>(mx.qp, mx.nctile, R, c->S, c->rho, apply_d4,
-                                                        x->abcc);
+                                                        x->abcc, x->absmax);
         TDS_CHECK_LAUNCH();
     }
     {
         ProfScope ps(c, 2, st);
         dim3 g(ceil_div(M, kWRows), x->nfchunk);
-        k_wbuild<<<g, 256, 0, st>>>(mx.ft32, mx.ut32, x->abcc, R, Rp, M, mx.wt_hi, mx.wt_lo,
-                                    x->fpart);
+        k_wbuild<<<g, 256, 0, st>>>(mx.ft32, mx.ut32, x->abcc, x->absmax, x->fmx, x->su, R, Rp, M,
+                                    mx.wt_hi, mx.wt_lo, x->sw, x->fpart);
         TDS_CHECK_LAUNCH();
     }
     GemmArgs gb{};
@@ -778,6 +915,8 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     gb.Mp = Mp;
     gb.ldG = x->ldG;
     gb.ntile = x->ntB;
+    gb.su = x->su;
+    gb.sw = x->sw;
     gb.gpart = mx.gpart;
     gb.err = err_dev;
     gb.budget = x->budget;

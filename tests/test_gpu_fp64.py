@@ -222,3 +222,24 @@ def test_ignore_v3_and_harmonic_switches(gpu_lib):
     lanc.shift_value = 3e-6
     ol.reverse_L, ol.shift_value = True, 3e-6
     close(lanc.apply_full_L(psi.copy()), ol.apply_full_L(psi.copy()), TOL_CALL)
+
+
+def test_full_reorth_keeps_biorthogonality(gpu_lib, golden):
+    """With full re-biorthogonalisation the early coefficients equal the plain
+    recurrence's (reference golden) and the stored bases stay biorthogonal."""
+    d = golden("runft_m21_n1000.npz")
+    ens = _ens(d)
+    lanc = _lanczos(ens, False)
+    lanc.full_reorth = True
+    lanc.prepare_perturbation(d["R1"], masses_exp=0)
+    lanc.run_FT(50, verbose=False)
+    a = np.array(lanc.a_coeffs)
+    ref = d["bilanczos/a"]
+    rel = np.abs(a[:15] - ref[:15]) / np.abs(ref[:15])
+    assert rel.max() <= TOL_RUN, rel.max()
+    Q = np.array(lanc.basis_Q)
+    Pm = np.array(lanc.basis_P)
+    G = Pm @ Q.T
+    dg = np.abs(np.diag(G))
+    off = np.abs(G - np.diag(np.diag(G))) / np.sqrt(np.outer(dg, dg))
+    assert off.max() < 1e-10, off.max()

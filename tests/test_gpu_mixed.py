@@ -58,10 +58,11 @@ def test_mixed_perturb_matches_oracle(gpu_lib, M, N, S):
     ctx.close()
 
 
-def _spectral_run(ens, precision, steps, R1):
+def _spectral_run(ens, precision, steps, R1, reorth=False):
     lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
                                use_wigner=False, precision=precision)
     lanc.init(use_symmetries=False)
+    lanc.full_reorth = reorth
     lanc.prepare_perturbation(R1, masses_exp=0)
     lanc.run_FT(steps, verbose=False)
     w = np.linspace(0, 600, 2000) / RY_TO_CM
@@ -69,12 +70,13 @@ def _spectral_run(ens, precision, steps, R1):
     return lanc, -G.imag
 
 
-@pytest.mark.parametrize("M,N,steps", [(48, 4000, 60), (96, 8000, 80)])
-def test_mixed_lanczos_spectral_error(gpu_lib, M, N, steps):
+@pytest.mark.parametrize("M,N,steps,reorth", [(48, 4000, 60, False), (96, 8000, 80, False),
+                                              (189, 10000, 150, True)])
+def test_mixed_lanczos_spectral_error(gpu_lib, M, N, steps, reorth):
     ens = make_ensemble(M, N, seed=7 + M, rho_sigma=0.1)
     R1 = random_R1(M, 3)
-    l64, A64 = _spectral_run(ens, "fp64", steps, R1)
-    lmx, Amx = _spectral_run(ens, "mixed", steps, R1)
+    l64, A64 = _spectral_run(ens, "fp64", steps, R1, reorth)
+    lmx, Amx = _spectral_run(ens, "mixed", steps, R1, reorth)
     err = rel(Amx, A64)
     a64, amx = np.array(l64.a_coeffs), np.array(lmx.a_coeffs)
     print("M=%d N=%d: spectral err %.2e, a_0..9 max rel %.2e" % (
