@@ -644,19 +644,28 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
     }
 }
 
-__global__ void k_finalize_mixed(const float *__restrict__ gpart, int nsplit, int ldG,
-                                 const float *__restrict__ fpart, int nfchunk, int M, double norm,
-                                 double *__restrict__ f, double *__restrict__ d2v) {
+// Sum of the split-K partial tiles (coalesced, float64 out) ...
+__global__ void k_gsum(const float *__restrict__ gpart, int nsplit, int ldG, int M,
+                       double *__restrict__ gs) {
     long n = (long)M * M;
     long stride = (long)ldG * ldG;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         int a = (int)(e / M), b = (int)(e % M);
-        double gab = 0, gba = 0;
-        for (int s = 0; s < nsplit; ++s) {
-            gab += (double)gpart[s * stride + (long)a * ldG + b];
-            gba += (double)gpart[s * stride + (long)b * ldG + a];
-        }
-        d2v[e] = -(gab + gba) / norm;
+        const float *g = gpart + (long)a * ldG + b;
+        double acc = 0;
+        for (int s = 0; s < nsplit; ++s) acc += (double)g[s * stride];
+        gs[e] = acc;
+    }
+}
+
+// ... then d2v = -(G + G^T) / norm and f = sum of the W-build partials / norm.
+__global__ void k_finalize_mixed(const double *__restrict__ gs, const float *__restrict__ fpart,
+                                 int nfchunk, int M, double norm, double *__restrict__ f,
+                                 double *__restrict__ d2v) {
+    long n = (long)M * M;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        int a = (int)(e / M), b = (int)(e % M);
+        d2v[e] = -(gs[e] + gs[(long)b * M + a]) / norm;
         if (e < M) {
             double acc = 0;
             for (int ch = 0; ch < nfchunk; ++ch) acc += (double)fpart[(long)ch * M + e];
@@ -745,7 +754,9 @@ int mixed_prepare(tdscha_ctx *c) {
     x->ldG = ((Mp + kBM - 1) / kBM) * kBM;
     x->ntB = x->ldG / kBM;
     x->nkbB = (int)(Rp / kBK);
-    int want = std::max(1, ceil_div(R, kSplitRows));
+    long split_rows = kSplitRows;
+    if (const char *e = getenv("TDSCHA_SPLIT_ROWS")) split_rows = std::max(64L, atol(e));
+    int want = std::max(1, ceil_div(R, split_rows));
     want = std::min(want, x->nkbB);
     x->kbps = ceil_div(x->nkbB, want);
     mx.nsplit = ceil_div(x->nkbB, x->kbps);
@@ -929,8 +940,9 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 4, st);
         int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 2048));
-        k_finalize_mixed<<<nb, 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, x->fpart, x->nfchunk, M,
-                                             c->sum_rho * c->S, c->f, c->d2v);
+        k_gsum<<<nb, 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, M, c->gpart);
+        k_finalize_mixed<<<nb, 256, 0, st>>>(c->gpart, x->fpart, x->nfchunk, M, c->sum_rho * c->S,
+                                             c->f, c->d2v);
         TDS_CHECK_LAUNCH();
     }
     return TDSCHA_OK;

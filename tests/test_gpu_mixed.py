@@ -1,10 +1,14 @@
-"""Tensor-core (split-bf16 x3, fp32 accumulate) perturbation averages and the
-mixed-precision Lanczos run, against the float64 oracle / float64 GPU path.
+"""Tensor-core (two-limb fp16 operands, fp32 accumulate) perturbation averages
+and the mixed-precision Lanczos run, against the float64 oracle / float64 GPU
+path.
 
-Tolerances: one perturbation-average call within 1e-3 of the largest entry
-(split-bf16 operands carry 16 significant bits); the spectral function of a
+Tolerances: one perturbation-average call within 2e-5 of the largest entry
+(the operands carry about 22 significant bits); the spectral function of a
 mixed-precision run within 1e-4 relative (max |dA| / max |A| over the
-frequency grid) of the float64 run -- the accuracy bar of the mixed path."""
+frequency grid) of the float64 run -- the accuracy bar of the mixed path --
+with full re-biorthogonalisation in both runs, or over a short window
+without it (the plain recurrence amplifies any rounding difference by about
+20x per step once biorthogonality is lost, between two float64 runs too)."""
 import os
 
 import numpy as np
@@ -17,7 +21,7 @@ from tdscha_gb300.synthetic import RY_TO_CM, make_ensemble, random_R1, random_sy
 
 pytestmark = pytest.mark.gpu
 
-TOL_CALL = 1e-3
+TOL_CALL = 2e-5
 TOL_SPECTRAL = 1e-4
 
 
@@ -70,7 +74,7 @@ def _spectral_run(ens, precision, steps, R1, reorth=False):
     return lanc, -G.imag
 
 
-@pytest.mark.parametrize("M,N,steps,reorth", [(48, 4000, 60, False), (96, 8000, 80, False),
+@pytest.mark.parametrize("M,N,steps,reorth", [(48, 4000, 30, False), (96, 8000, 80, True),
                                               (189, 10000, 150, True)])
 def test_mixed_lanczos_spectral_error(gpu_lib, M, N, steps, reorth):
     ens = make_ensemble(M, N, seed=7 + M, rho_sigma=0.1)
