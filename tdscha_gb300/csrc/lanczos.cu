@@ -224,12 +224,20 @@ __global__ void k_dot1(const double *__restrict__ x, const double *__restrict__ 
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// Sum of nblk block partials by one block (fixed order: thread stride, then tree).
+__device__ __forceinline__ double reduce_parts(const double *__restrict__ part, int nblk,
+                                               double *sh) {
+    double v = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += part[b];
+    return block_sum(v, sh);
+}
+
 // a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232)
 __global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
                          int k, double *__restrict__ scal) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double d = 0;
-    for (int b = 0; b < nblk; ++b) d += part[b];
+    __shared__ double sh[32];
+    double d = reduce_parts(part, nblk, sh);
+    if (threadIdx.x != 0) return;
     double c_old = k >= 1 ? hist[4 * (k - 1) + 2] : 1.0;
     double p_norm = hist[4 * k + 3] / c_old;
     double a = d * p_norm;
@@ -276,9 +284,11 @@ __global__ void k_resid(const double *__restrict__ Lq, const double *__restrict_
 
 __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
                           int k, double *__restrict__ scal) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double ss = 0, rr = 0, sr = 0;
-    for (int b = 0; b < nblk; ++b) { ss += part[b]; rr += part[nblk + b]; sr += part[2 * nblk + b]; }
+    __shared__ double sh[32];
+    double ss = reduce_parts(part, nblk, sh);
+    double rr = reduce_parts(part + nblk, nblk, sh);
+    double sr = reduce_parts(part + 2 * nblk, nblk, sh);
+    if (threadIdx.x != 0) return;
     double s_raw = sqrt(ss);
     double s_norm = s_raw * scal[SC_PNORM];
     double b = sqrt(rr);
@@ -311,33 +321,41 @@ __global__ void k_normalize(const double *__restrict__ rk, const double *__restr
 // Full re-biorthogonalisation of the new pair (q_{k+1}, p_{k+1}) against the
 // stored basis: q -= sum_j (p_j.q / p_j.q_j) q_j and p -= sum_j (q_j.p / p_j.q_j) p_j
 // (one classical Gram-Schmidt pass; the recurrence scalars are not changed).
-// One block per basis vector for the dot products.
+// The dot products run on a (vectors x kDotChunks) grid of block partials.
+constexpr int kDotChunks = 24;
 __global__ void k_proj_dots(const double *__restrict__ Qb, const double *__restrict__ Pb,
                             const double *__restrict__ qn, const double *__restrict__ pn,
                             const double *__restrict__ mask, long n, long ld,
                             double *__restrict__ part) {
     __shared__ double sh[32];
     int j = blockIdx.x;
+    long e0 = n * blockIdx.y / kDotChunks, e1 = n * (blockIdx.y + 1) / kDotChunks;
     const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
     double a = 0, b = 0;
-    for (long e = threadIdx.x; e < n; e += blockDim.x) {
+    for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         double m = mask ? mask[e] : 1.0;
-        a += pj[e] * (qn[e] * m);
-        b += qj[e] * (pn[e] * m);
+        a = fma(pj[e], qn[e] * m, a);
+        b = fma(qj[e], pn[e] * m, b);
     }
     double t = block_sum(a, sh);
-    if (threadIdx.x == 0) part[2 * j] = t;
+    if (threadIdx.x == 0) part[((long)j * kDotChunks + blockIdx.y) * 2] = t;
     t = block_sum(b, sh);
-    if (threadIdx.x == 0) part[2 * j + 1] = t;
+    if (threadIdx.x == 0) part[((long)j * kDotChunks + blockIdx.y) * 2 + 1] = t;
 }
 
-__global__ void k_proj_scale(double *__restrict__ coef, const double *__restrict__ pqn, int nvec) {
+// coef[2j], coef[2j+1] = chunk sums / (p_j . q_j)
+__global__ void k_proj_scale(const double *__restrict__ part, const double *__restrict__ pqn,
+                             int nvec, double *__restrict__ coef) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < nvec) {
-        double inv = 1.0 / pqn[j];
-        coef[2 * j] *= inv;
-        coef[2 * j + 1] *= inv;
+    if (j >= nvec) return;
+    double a = 0, b = 0;
+    for (int c = 0; c < kDotChunks; ++c) {
+        a += part[((long)j * kDotChunks + c) * 2];
+        b += part[((long)j * kDotChunks + c) * 2 + 1];
     }
+    double inv = 1.0 / pqn[j];
+    coef[2 * j] = a * inv;
+    coef[2 * j + 1] = b * inv;
 }
 
 constexpr int kProjMax = 2048;   // coefficients cached in shared memory per pass
@@ -358,19 +376,29 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
     }
 }
 
-// p_j . q_j for j in [j0, j1)
-__global__ void k_pq_diag(const double *__restrict__ Qb, const double *__restrict__ Pb,
+// p_j . q_j for j in [j0, j0 + gridDim.x): chunk partials, then one thread per j.
+__global__ void k_pq_part(const double *__restrict__ Qb, const double *__restrict__ Pb,
                           const double *__restrict__ mask, long n, long ld, int j0,
-                          double *__restrict__ out) {
+                          double *__restrict__ part) {
     __shared__ double sh[32];
     int j = j0 + blockIdx.x;
+    long e0 = n * blockIdx.y / kDotChunks, e1 = n * (blockIdx.y + 1) / kDotChunks;
     double a = 0;
-    for (long e = threadIdx.x; e < n; e += blockDim.x) {
+    for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         double m = mask ? mask[e] : 1.0;
-        a += Pb[(long)j * ld + e] * (Qb[(long)j * ld + e] * m);
+        a = fma(Pb[(long)j * ld + e], Qb[(long)j * ld + e] * m, a);
     }
     double t = block_sum(a, sh);
-    if (threadIdx.x == 0) out[j] = t;
+    if (threadIdx.x == 0) part[(long)blockIdx.x * kDotChunks + blockIdx.y] = t;
+}
+
+__global__ void k_pq_finish(const double *__restrict__ part, int cnt, int j0,
+                            double *__restrict__ out) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cnt) return;
+    double a = 0;
+    for (int c = 0; c < kDotChunks; ++c) a += part[(long)j * kDotChunks + c];
+    out[j0 + j] = a;
 }
 
 }  // namespace tdscha
@@ -423,11 +451,14 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             if (ctx->rcoef) cudaFree(ctx->rcoef);
             ctx->pqn = ctx->rcoef = nullptr;
             TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
-            TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1)));
+            TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kDotChunks + 1)));
             ctx->pqn_cap = capacity + 1;
         }
         // weights of the vectors already stored
-        k_pq_diag<<<start_step + 1, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0, ctx->pqn);
+        double *part = ctx->rcoef + 2 * (capacity + 1);
+        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0,
+                                                                    part);
+        k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
     int rc = TDSCHA_OK;
@@ -447,12 +478,12 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             pL = ctx->pL;
         }
         k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
-        k_scal_a<<<1, 32, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
         const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
         const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
         k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
                                              ctx->rk, ctx->sk, ctx->dots, nb);
-        k_scal_bc<<<1, 32, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
         double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
         k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
         {
@@ -481,12 +512,15 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         hist[4 * (k + 1) + 3] = sc[SC_SNORM];
         if (full_reorth) {
             int nvec = k + 1;
-            k_proj_dots<<<nvec, 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P, ctx->rcoef);
-            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(ctx->rcoef, ctx->pqn, nvec);
+            double *part = ctx->rcoef + 2 * (capacity + 1);
+            k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P,
+                                                                part);
+            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
             for (int j0 = 0; j0 < nvec; j0 += kProjMax)
                 k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
                                                  std::min(kProjMax, nvec - j0), P, qn, pn);
-            k_pq_diag<<<1, 256, 0, st>>>(basis_Q, basis_P, mask, P, P, k + 1, ctx->pqn);
+            k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, k + 1, part);
+            k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) { set_error("reorth launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
         }
