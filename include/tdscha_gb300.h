@@ -149,6 +149,33 @@ int tdscha_continued_fraction(const double *a, int n, const double *b, int n_b,
 int tdscha_ctx_profile(tdscha_ctx *ctx, int enable);
 int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, int *launches);
 
+/*
+ * Float64 perturbation averages that allocate no device memory (no
+ * counterpart in the reference).  For callers that cannot let a library call
+ * cudaMalloc: host programs that reserve the GPU's memory for their own pool
+ * and hand out fixed budgets, and latency-critical loops that cannot accept
+ * the device-wide synchronisation cudaMalloc / cudaFree may cause.
+ *
+ * All pointers are device memory owned by the caller: X, Y (N x M), w (M),
+ * rho (N), R1 (M), Y1 (M x M) in; f_out (M), d2v_out (M x M) out, written
+ * with the same convention as tdscha_perturb_averages (no symmetry images:
+ * one identity image per configuration).  Asynchronous on `stream`.
+ *
+ * Intermediate arrays live in one static 32 MiB device array that every
+ * process loading this library holds on each GPU it uses until exit.  Sizes
+ * whose scratch exceeds it (at M=573, N above about 100 000) are rejected
+ * with TDSCHA_ERR_ARG and a message giving the bytes needed.  Every call
+ * uses the same array (each call writes every word it reads, so nothing
+ * carries over), so calls that overlap on the GPU -- on different streams or
+ * from different host threads -- race and must be serialised by the caller.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.
+ */
+int tdscha_perturb_averages_noalloc(int M, int N, const double *X, const double *Y,
+                                    const double *w, const double *rho, const double *R1,
+                                    const double *Y1, double T, int apply_D4, double *f_out,
+                                    double *d2v_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

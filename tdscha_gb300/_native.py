@@ -21,6 +21,7 @@ EXPORTS = [
     "tdscha_ctx_create", "tdscha_ctx_destroy", "tdscha_ctx_set_options",
     "tdscha_perturb_averages", "tdscha_apply_full_L", "tdscha_lanczos_run",
     "tdscha_continued_fraction", "tdscha_ctx_profile", "tdscha_ctx_profile_read",
+    "tdscha_perturb_averages_noalloc",
 ]
 
 
@@ -66,6 +67,8 @@ def load():
         _c_int, _c_int, _c_double, _c_int, _d]
     lib.tdscha_ctx_profile.argtypes = [_vp, _c_int]
     lib.tdscha_ctx_profile_read.argtypes = [_vp, _c_int, _d, _i]
+    lib.tdscha_perturb_averages_noalloc.argtypes = [
+        _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_double, _c_int, _vp, _vp, _vp]
     for name in EXPORTS:
         fn = getattr(lib, name)
         if name not in ("tdscha_last_error", "tdscha_version"):
