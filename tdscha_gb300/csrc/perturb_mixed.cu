@@ -54,6 +54,11 @@ struct TmaQuad {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
 };
 
+// fp32 row tiles read by the stage A epilogue (d and g = f_psi * f)
+struct TmaEpi {
+    CUtensorMap d, g;
+};
+
 struct GemmArgs {
     // geometry
     int nkb;            // k-blocks per CTA (stage A); k-blocks per split (stage B)
@@ -212,6 +217,7 @@ __device__ __forceinline__ void tmem_combined(uint32_t lane_base, int col, int b
 // MODE 0: stage A (row dots epilogue).  MODE 1: stage B (split-K tile store).
 template <int BN, int STAGES, int MODE>
 __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQuad tm,
+                                                     const __grid_constant__ TmaEpi te,
                                                      const GemmArgs args) {
     constexpr uint32_t kBBytes = BN * kBK * 2;
     constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
@@ -221,7 +227,9 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * kStageBytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 1);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 3);
+    // stage A: per-column factors of this tile (t_n, f_Y R1, R1 / f_psi)
+    float *colv = reinterpret_cast<float *>(tmem_slot + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES),
                    done = smem_u32(bars + 2 * STAGES);
@@ -247,8 +255,18 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
             mbar_init(empty0 + 8 * s, 1);
         }
         mbar_init(done, 1);
+        mbar_init(done + 8, 1);
+        mbar_init(done + 16, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (MODE == 0) {
+        for (int c = threadIdx.x; c < BN; c += blockDim.x) {
+            int n = brow + c;
+            colv[c] = args.tcol[n];
+            colv[BN + c] = args.vec_s[n];
+            colv[2 * BN + c] = args.vec_t[n];
+        }
     }
     if (warp == 0) tmem_alloc<kCols>(smem_u32(tmem_slot));
     tc_fence_before();
@@ -257,7 +275,6 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
     const uint32_t tmem = *tmem_slot;
     const long long budget = args.budget;
     bool failed = false;
-
     if (warp == 0 && lane == 0) {
         // ---- TMA producer
         int issued = 0;
@@ -321,30 +338,63 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     const bool have_acc = nkb > 0 && ready;
     if (MODE == 0) {
-        long row = (long)arow + warp * 32 + lane;
+        // The pipeline buffers are free once `done` completed: the d and g row
+        // tiles of this CTA come in through TMA, 64 columns (two 32-column
+        // boxes per tensor, 128-byte swizzle) per part, double buffered.
+        constexpr int kParts = BN / 64;
+        constexpr uint32_t kBox = kBM * 32 * 4;          // one 128 x 32 fp32 box
+        constexpr uint32_t kPartBytes = 4 * kBox;        // d0 d1 g0 g1
+        const uint32_t epi0 = done + 8;
+        const int row_in = warp * 32 + lane;
+        const long row = (long)arow + row_in;
+        auto issue = [&](int part) {
+            uint32_t buf = smem_u32(smem + (part & 1) * kPartBytes);
+            uint32_t bar = epi0 + 8 * (part & 1);
+            int x = brow + part * 64;
+            mbar_expect_tx(bar, kPartBytes);
+            tma_load_2d(buf, &te.d, bar, x, arow);
+            tma_load_2d(buf + kBox, &te.d, bar, x + 32, arow);
+            tma_load_2d(buf + 2 * kBox, &te.g, bar, x, arow);
+            tma_load_2d(buf + 3 * kBox, &te.g, bar, x + 32, arow);
+        };
+        if (threadIdx.x == 0 && have_acc) {
+            issue(0);
+            if (kParts > 1) issue(1);
+        }
         float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
 #pragma unroll 1
-        for (int ch = 0; ch < BN / 32; ++ch) {
-            float v[32];
-            tmem_combined(lane_base, ch * 32, BN, v);
-            int col0 = brow + ch * 32;
-            if (row < args.R && have_acc) {
-                const float4 *pd = reinterpret_cast<const float4 *>(args.d32 + row * args.Mp + col0);
-                const float4 *pg = reinterpret_cast<const float4 *>(args.g32 + row * args.Mp + col0);
+        for (int part = 0; part < kParts; ++part) {
+            bool landed = have_acc && mbar_wait(epi0 + 8 * (part & 1), (part >> 1) & 1, budget);
+            if (have_acc && !landed && lane == 0) *(volatile int *)args.err = 3;
+            const uint8_t *buf = smem + (part & 1) * kPartBytes;
+#pragma unroll 1
+            for (int half = 0; half < 2; ++half) {
+                float v[32];
+                tmem_combined(lane_base, part * 64 + half * 32, BN, v);
+                if (landed) {
+                    const uint8_t *bd = buf + half * kBox + row_in * 128;
+                    const uint8_t *bg = buf + (2 + half) * kBox + row_in * 128;
+                    const int sw = row_in & 7;
 #pragma unroll
-                for (int j4 = 0; j4 < 8; ++j4) {
-                    float4 d4 = pd[j4], g4 = pg[j4];
-                    float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                    for (int ch = 0; ch < 8; ++ch) {
+                        float4 d4 = *reinterpret_cast<const float4 *>(bd + ((ch ^ sw) << 4));
+                        float4 g4 = *reinterpret_cast<const float4 *>(bg + ((ch ^ sw) << 4));
+                        float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        int j = 4 * j4 + e, c = col0 + j;
-                        float vv = v[j] * args.tcol[c];
-                        q = fmaf(dd[e], vv, q);
-                        p = fmaf(gg[e], vv, p);
-                        sacc = fmaf(args.vec_s[c], dd[e], sacc);
-                        tacc = fmaf(args.vec_t[c], gg[e], tacc);
+                        for (int e = 0; e < 4; ++e) {
+                            int j = 4 * ch + e, c = part * 64 + half * 32 + j;
+                            float vv = v[j] * colv[c];
+                            q = fmaf(dd[e], vv, q);
+                            p = fmaf(gg[e], vv, p);
+                            sacc = fmaf(colv[BN + c], dd[e], sacc);
+                            tacc = fmaf(colv[2 * BN + c], gg[e], tacc);
+                        }
                     }
                 }
+            }
+            if (part + 2 < kParts) {
+                __syncthreads();                       // everyone is done with this buffer
+                if (threadIdx.x == 0 && have_acc) issue(part + 2);
             }
         }
         if (row < args.R) {
@@ -584,7 +634,7 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, in
 // sw_b = max|alpha| fmax_b + max|beta|/2 su_b; and the force-average partials
 // fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
 constexpr int kWRows = 8;      // b rows per block
-constexpr int kWChunk = 2048;  // r per block
+constexpr int kWChunk = 2048;  // r per block (256 threads x 4 r x 2 passes)
 __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
                                                 const float *__restrict__ ut32,
                                                 const float4 *__restrict__ abcc,
@@ -609,22 +659,33 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
         facc[k] = 0.f;
         if (blockIdx.y == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
     }
-    for (int it = 0; it < kWChunk / 256; ++it) {
-        long r = r0 + it * 256 + threadIdx.x;
-        if (r >= R) break;
-        float4 w = abcc[r];
+    // Rp is a multiple of 64 and r0 of 2048, so each 4-group is in bounds of
+    // the padded rows; rows r >= R carry alpha = beta = c1 = c2 = 0 there.
+#pragma unroll
+    for (int pass = 0; pass < kWChunk / 1024; ++pass) {
+        long r = r0 + pass * 1024 + 4 * threadIdx.x;
+        if (r >= Rp) break;
+        float4 w4[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            w4[q] = (r + q < R) ? abcc[r + q] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < kWRows; ++k) {
             int b = b0 + k;
             if (b >= M) break;
             long o = (long)b * Rp + r;
-            float f = ft32[o], u = ut32[o];
-            float x = (w.x * f + 0.5f * w.y * u) * inv[k];
-            __half h, l;
-            split_f16(x, h, l);
-            wt_hi[o] = h;
-            wt_lo[o] = l;
-            facc[k] = fmaf(w.z, f, fmaf(w.w, u, facc[k]));
+            float4 f4 = *reinterpret_cast<const float4 *>(ft32 + o);
+            float4 u4 = *reinterpret_cast<const float4 *>(ut32 + o);
+            float ff[4] = {f4.x, f4.y, f4.z, f4.w}, uu[4] = {u4.x, u4.y, u4.z, u4.w};
+            __align__(8) __half hh[4], ll[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float x = (w4[q].x * ff[q] + 0.5f * w4[q].y * uu[q]) * inv[k];
+                split_f16(x, hh[q], ll[q]);
+                facc[k] = fmaf(w4[q].z, ff[q], fmaf(w4[q].w, uu[q], facc[k]));
+            }
+            *reinterpret_cast<uint2 *>(wt_hi + o) = *reinterpret_cast<const uint2 *>(hh);
+            *reinterpret_cast<uint2 *>(wt_lo + o) = *reinterpret_cast<const uint2 *>(ll);
         }
     }
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -710,9 +771,29 @@ static int make_map(CUtensorMap *m, const void *base, uint64_t inner, uint64_t o
     return TDSCHA_OK;
 }
 
+// 2D fp32 tensor (inner x outer), box 32 x 128, 128-byte swizzle.
+static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer) {
+    auto fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return TDSCHA_ERR_CUDA; }
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((inner * 4) & 15) || inner % 32) {
+        set_error("tensor map (fp32): misaligned base or pitch");
+        return TDSCHA_ERR_ARG;
+    }
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {inner * 4};
+    cuuint32_t box[2] = {32, (cuuint32_t)kBM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled (fp32) failed (%d)", (int)r); return TDSCHA_ERR_CUDA; }
+    return TDSCHA_OK;
+}
+
 template <int BN, int STAGES>
 static constexpr size_t gemm_smem() {
-    return 1024 + STAGES * (2 * (size_t)kABytes + 2 * (size_t)BN * kBK * 2) + 8 * (2 * STAGES + 1) + 16;
+    return 1024 + STAGES * (2 * (size_t)kABytes + 2 * (size_t)BN * kBK * 2) + 8 * (2 * STAGES + 3) +
+           16 + 3 * 4 * (size_t)BN;
 }
 
 // Stage A column tile: the widest multiple of 64 (<= 192) dividing Mp.
@@ -725,6 +806,7 @@ static int choose_bn(int Mp) {
 
 struct MixedExtra {
     TmaQuad tmA, tmB;
+    TmaEpi te;
     int bnA = 0;
     float *sd = nullptr, *fmx = nullptr, *su = nullptr, *sw = nullptr, *tcol = nullptr;
     float *vs = nullptr, *vt = nullptr, *absmax = nullptr;
@@ -758,6 +840,22 @@ int mixed_prepare(tdscha_ctx *c) {
     if (const char *e = getenv("TDSCHA_SPLIT_ROWS")) split_rows = std::max(64L, atol(e));
     int want = std::max(1, ceil_div(R, split_rows));
     want = std::min(want, x->nkbB);
+    {
+        // among split counts up to `want`, take the one whose grid fills the
+        // 152 SMs in whole waves best (ties: more splits)
+        const int tiles = x->ntB * x->ntB;
+        int best = want;
+        double best_fill = 0;
+        for (int n = std::max(1, want / 2); n <= want; ++n) {
+            long ctas = (long)tiles * n;
+            double fill = (double)ctas / (double)(ceil_div(ctas, 152) * 152L);
+            if (fill > best_fill + 1e-9 || (fill > best_fill - 1e-9 && n > best)) {
+                best_fill = fill;
+                best = n;
+            }
+        }
+        want = best;
+    }
     x->kbps = ceil_div(x->nkbB, want);
     mx.nsplit = ceil_div(x->nkbB, x->kbps);
     x->nfchunk = ceil_div(R, kWChunk);
@@ -816,6 +914,8 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_TRY(make_map(&x->tmB.a_lo, mx.ut_lo, Rp, Mp, kBM));
     TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, Mp, kBNB));
     TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, Mp, kBNB));
+    TDS_TRY(make_map_f32(&x->te.d, x->d32, Mp, R));
+    TDS_TRY(make_map_f32(&x->te.g, mx.g32, Mp, R));
     static bool attr_done = false;
     if (!attr_done) {
         TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<192, kStagesA, 0>,
@@ -895,13 +995,13 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
         dim3 grid(mx.nctile, ceil_div(R, kBM));
         switch (x->bnA) {
             case 192:
-                k_gemm_tc<192, kStagesA, 0><<<grid, 128, gemm_smem<192, kStagesA>(), st>>>(x->tmA, ga);
+                k_gemm_tc<192, kStagesA, 0><<<grid, 128, gemm_smem<192, kStagesA>(), st>>>(x->tmA, x->te, ga);
                 break;
             case 128:
-                k_gemm_tc<128, kStagesA, 0><<<grid, 128, gemm_smem<128, kStagesA>(), st>>>(x->tmA, ga);
+                k_gemm_tc<128, kStagesA, 0><<<grid, 128, gemm_smem<128, kStagesA>(), st>>>(x->tmA, x->te, ga);
                 break;
             default:
-                k_gemm_tc<64, kStagesA, 0><<<grid, 128, gemm_smem<64, kStagesA>(), st>>>(x->tmA, ga);
+                k_gemm_tc<64, kStagesA, 0><<<grid, 128, gemm_smem<64, kStagesA>(), st>>>(x->tmA, x->te, ga);
                 break;
         }
         TDS_CHECK_LAUNCH();
@@ -934,7 +1034,7 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 3, st);
         dim3 grid(x->ntB * x->ntB, mx.nsplit);
-        k_gemm_tc<kBNB, kStagesB, 1><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, gb);
+        k_gemm_tc<kBNB, kStagesB, 1><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, x->te, gb);
         TDS_CHECK_LAUNCH();
     }
     {
