@@ -84,6 +84,8 @@ struct tdscha_ctx {
     // per-mode (device)
     double *w = nullptr, *fY = nullptr, *fpsi = nullptr, *rho = nullptr;
     double *Yw = nullptr, *ReAw = nullptr;     // equilibrium Upsilon / ReA eigenvalues
+    double *Ywinv = nullptr;                    // 1 / Yw
+    int *tri = nullptr;                         // (row, column) of each upper-triangle pair
     // image rows (device), R x M
     double *D = nullptr, *F = nullptr;
     // per-pair coefficients (device), length H, rebuilt by set_options
@@ -102,6 +104,9 @@ struct tdscha_ctx {
     double *scal = nullptr;     // device scalars of the recurrence
     double *hist_dev = nullptr; // device copy of the coefficient history
     int hist_cap = 0;
+    double *stat_dev = nullptr; // per-step recurrence status (device)
+    double *stat_host = nullptr;// pinned read-back area (history rows + status)
+    int stat_cap = 0;
     double *pqn = nullptr;      // p_j . q_j of the stored basis (full reorthogonalisation)
     double *rcoef = nullptr;    // projection coefficients (2 per basis vector)
     int pqn_cap = 0;

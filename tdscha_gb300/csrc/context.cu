@@ -84,10 +84,13 @@ static void ctx_free(tdscha_ctx *c) {
     double *bufs[] = {c->w, c->fY, c->fpsi, c->rho, c->Yw, c->ReAw, c->D, c->F, c->pc,
                       c->R1, c->Y1, c->f, c->d2v, c->qp_part, c->alpha, c->beta, c->c1,
                       c->c2, c->gpart, c->fpart, c->Lq, c->pL, c->rk, c->sk, c->mask,
-                      c->dots, c->scal, c->hist_dev, c->pqn, c->rcoef};
+                      c->dots, c->scal, c->hist_dev, c->pqn, c->rcoef, c->Ywinv,
+                      c->stat_dev};
     for (double *p : bufs)
         if (p) cudaFree(p);
+    if (c->tri) cudaFree(c->tri);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
+    if (c->stat_host) cudaFreeHost(c->stat_host);
     delete c;
 }
 
@@ -276,9 +279,8 @@ __global__ void k_symmetrize(double *Y1, int M) {
     }
 }
 
-int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st) {
-    k_symmetrize<<<std::max(1, std::min(ceil_div((long)c->M * c->M, 256), 1024)), 256, 0, st>>>(c->Y1, c->M);
-    TDS_CHECK_LAUNCH();
+// Perturbation averages for a Y1 already symmetric in ctx->Y1.
+int run_perturb_sym(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st) {
     if (precision == TDSCHA_PREC_FP64) return perturb_fp64(c, apply_d4, st);
     if (precision == TDSCHA_PREC_MIXED) {
         if (!c->with_mixed) { set_error("mixed precision requested but the context was created without it"); return TDSCHA_ERR_STATE; }
@@ -286,6 +288,12 @@ int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st) {
     }
     set_error("unknown precision %d", precision);
     return TDSCHA_ERR_ARG;
+}
+
+int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st) {
+    k_symmetrize<<<std::max(1, std::min(ceil_div((long)c->M * c->M, 256), 1024)), 256, 0, st>>>(c->Y1, c->M);
+    TDS_CHECK_LAUNCH();
+    return run_perturb_sym(c, apply_d4, precision, st);
 }
 
 }  // namespace tdscha

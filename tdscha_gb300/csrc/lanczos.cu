@@ -20,6 +20,7 @@ namespace tdscha {
 enum { PC_X = 0, PC_Y, PC_X1, PC_Y1, PC_UA, PC_UB, PC_RA, PC_RB, PC_TY, PC_TRA, PC_I, PC_J };
 
 int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st);
+int run_perturb_sym(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st);
 
 int build_pair_coeffs(tdscha_ctx *c) {
     const int M = c->M;
@@ -80,6 +81,16 @@ int build_pair_coeffs(tdscha_ctx *c) {
         }
     }
     TDS_CUDA(cudaMemcpy(c->pc, pc.data(), sizeof(double) * 12 * H, cudaMemcpyHostToDevice));
+    std::vector<int> tri(2 * H);
+    std::vector<double> ywinv(M);
+    k = 0;
+    for (int i = 0; i < M; ++i)
+        for (int j = i; j < M; ++j, ++k) { tri[2 * k] = i; tri[2 * k + 1] = j; }
+    for (int m = 0; m < M; ++m) ywinv[m] = 1.0 / yw[m];
+    if (!c->tri) TDS_CUDA(cudaMalloc(&c->tri, sizeof(int) * 2 * H));
+    if (!c->Ywinv) TDS_CUDA(cudaMalloc(&c->Ywinv, sizeof(double) * M));
+    TDS_CUDA(cudaMemcpy(c->tri, tri.data(), sizeof(int) * 2 * H, cudaMemcpyHostToDevice));
+    TDS_CUDA(cudaMemcpy(c->Ywinv, ywinv.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
     // Wigner double-counting mask (mask_dot_wigner, :5905-5954)
     std::vector<double> mask(c->P, 1.0);
     k = 0;
@@ -119,7 +130,8 @@ __global__ void k_unpack(const double *__restrict__ psi, const double *__restric
 // out = L1 psi (+ anharmonic repack of f, d2v) then reverse / shift.
 __global__ void k_assemble(const double *__restrict__ psi, const double *__restrict__ f,
                            const double *__restrict__ d2v, const double *__restrict__ pc,
-                           const double *__restrict__ w, const double *__restrict__ Yw,
+                           const int *__restrict__ tri, const double *__restrict__ w,
+                           const double *__restrict__ Yw, const double *__restrict__ Ywinv,
                            const double *__restrict__ ReAw, int M, long H, int wigner,
                            int transpose, int ignore_harmonic, int with_anh, int reverse,
                            double shift, double *__restrict__ out) {
@@ -149,7 +161,7 @@ __global__ void k_assemble(const double *__restrict__ psi, const double *__restr
                 }
             }
             if (with_anh) {
-                int i = (int)pc[PC_I * H + k], j = (int)pc[PC_J * H + k];
+                int i = tri[2 * k], j = tri[2 * k + 1];
                 double dv = d2v[(long)i * M + j];
                 double v;
                 if (wigner) {
@@ -158,7 +170,7 @@ __global__ void k_assemble(const double *__restrict__ psi, const double *__restr
                     const double *ew = ysec ? Yw : ReAw;
                     v = dv * ew[i] + dv * ew[j];
                 } else if (ysec) {
-                    v = 0.5 * ((1.0 / Yw[i]) * dv * (1.0 / Yw[j]));
+                    v = 0.5 * (Ywinv[i] * dv * Ywinv[j]);
                     if (i != j) v *= 2;
                 } else {
                     v = 0.0;
@@ -183,10 +195,12 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
         k_unpack<<<nb, 256, 0, st>>>(psi_in, c->pc, M, H, c->use_wigner, transpose, c->ignore_v3,
                                      c->R1, c->Y1);
         TDS_CHECK_LAUNCH();
-        TDS_TRY(run_perturb(c, c->ignore_v4 ? 0 : 1, precision, st));
+        // Y1 from the unpack is symmetric by construction: no symmetrise pass
+        TDS_TRY(run_perturb_sym(c, c->ignore_v4 ? 0 : 1, precision, st));
     }
     int nb = std::max(1, std::min(ceil_div(c->P, 256), 4096));
-    k_assemble<<<nb, 256, 0, st>>>(psi_in, c->f, c->d2v, c->pc, c->w, c->Yw, c->ReAw, M, H,
+    k_assemble<<<nb, 256, 0, st>>>(psi_in, c->f, c->d2v, c->pc, c->tri, c->w, c->Yw, c->Ywinv,
+                                   c->ReAw, M, H,
                                    c->use_wigner, transpose, c->ignore_harmonic, with_anh,
                                    c->reverse_L, c->shift, psi_out);
     TDS_CHECK_LAUNCH();
@@ -195,7 +209,9 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
 
 // ---------------------------------------------------------------------------
 // Lanczos recurrence.  Device scalars (ctx->scal):
-enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN };
+enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN, SC_HALT };
+// per-step status written on the device: 0 running, 1 NaN in a, 2 converged
+enum { ST_OK = 0, ST_NAN = 1, ST_CONV = 2 };
 // hist_dev rows of 4: a_k, b_k, c_k, s_norm_k.
 
 constexpr int kDotThreads = 256;
@@ -234,16 +250,18 @@ __device__ __forceinline__ double reduce_parts(const double *__restrict__ part, 
 
 // a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232)
 __global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
-                         int k, double *__restrict__ scal) {
+                         int k, double *__restrict__ scal, double *__restrict__ status) {
     __shared__ double sh[32];
     double d = reduce_parts(part, nblk, sh);
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x != 0 || scal[SC_HALT] != 0.0) return;
     double c_old = k >= 1 ? hist[4 * (k - 1) + 2] : 1.0;
     double p_norm = hist[4 * k + 3] / c_old;
     double a = d * p_norm;
     scal[SC_A] = a;
     scal[SC_PNORM] = p_norm;
     scal[SC_NAN] = isnan(a) ? 1.0 : 0.0;
+    status[k] = isnan(a) ? ST_NAN : ST_OK;
+    if (isnan(a)) scal[SC_HALT] = 1.0;
     double cq = 0, cp = 0;
     if (k >= 1) {
         cq = hist[4 * (k - 1) + 2];
@@ -283,12 +301,12 @@ __global__ void k_resid(const double *__restrict__ Lq, const double *__restrict_
 }
 
 __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
-                          int k, double *__restrict__ scal) {
+                          int k, double *__restrict__ scal, double *__restrict__ status) {
     __shared__ double sh[32];
     double ss = reduce_parts(part, nblk, sh);
     double rr = reduce_parts(part + nblk, nblk, sh);
     double sr = reduce_parts(part + 2 * nblk, nblk, sh);
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x != 0 || scal[SC_HALT] != 0.0) return;
     double s_raw = sqrt(ss);
     double s_norm = s_raw * scal[SC_PNORM];
     double b = sqrt(rr);
@@ -299,6 +317,10 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
     scal[SC_SRAW] = s_raw;
     bool conv = fabs(b) < kEps || fabs(c) < kEps;
     scal[SC_CONV] = conv ? 1.0 : 0.0;
+    if (conv) {
+        status[k] = ST_CONV;
+        scal[SC_HALT] = 1.0;
+    }
     hist[4 * k + 0] = scal[SC_A];
     if (!conv) {
         hist[4 * k + 1] = b;
@@ -310,11 +332,12 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
 __global__ void k_normalize(const double *__restrict__ rk, const double *__restrict__ sk,
                             const double *__restrict__ scal, long n, double *__restrict__ qn,
                             double *__restrict__ pn) {
-    if (scal[SC_CONV] != 0.0) return;
-    double b = scal[SC_B], s = scal[SC_SRAW];
+    if (scal[SC_HALT] != 0.0) return;
+    // one reciprocal per vector: float64 division is slow on this part
+    const double ib = 1.0 / scal[SC_B], is = 1.0 / scal[SC_SRAW];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        qn[e] = rk[e] / b;
-        pn[e] = sk[e] / s;
+        qn[e] = rk[e] * ib;
+        pn[e] = sk[e] * is;
     }
 }
 
@@ -461,9 +484,25 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
+    // the recurrence's stop conditions are evaluated on the device (per-step
+    // status + a halt flag that turns later steps into no-ops), so steps are
+    // launched back to back and read back every kSyncEvery steps
+    constexpr int kSyncEvery = 16;
+    if (ctx->stat_cap < capacity + 1) {
+        if (ctx->stat_dev) cudaFree(ctx->stat_dev);
+        if (ctx->stat_host) cudaFreeHost(ctx->stat_host);
+        ctx->stat_dev = ctx->stat_host = nullptr;
+        ctx->stat_cap = 0;
+        TDS_CUDA(cudaMalloc(&ctx->stat_dev, sizeof(double) * (capacity + 1)));
+        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 5 * (capacity + 1)));
+        ctx->stat_cap = capacity + 1;
+    }
+    TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
     int rc = TDSCHA_OK;
     int nb = std::max(1, std::min(ceil_div(P, kDotThreads), nblk));
-    for (int it = 0; it < n_iter; ++it) {
+    int next = start_step;          // first step not yet read back
+    bool stop = false;
+    for (int it = 0; it < n_iter && !stop; ++it) {
         int k = start_step + it;
         if (k + 1 >= capacity) {
             set_error("lanczos_run: basis capacity %d exhausted at step %d", capacity, k);
@@ -478,38 +517,14 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             pL = ctx->pL;
         }
         k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
-        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
         const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
         const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
         k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
                                              ctx->rk, ctx->sk, ctx->dots, nb);
-        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal);
+        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
         double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
         k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
-        {
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
-        }
-        if (cudaMemcpyAsync(ctx->host_pinned, ctx->scal, sizeof(double) * 16,
-                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) {
-            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
-            rc = TDSCHA_ERR_CUDA;
-            break;
-        }
-        const double *sc = ctx->host_pinned;
-        if ((rc = mixed_check_error(ctx)) != TDSCHA_OK) break;
-        if (sc[SC_NAN] != 0.0) {
-            set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", k);
-            rc = TDSCHA_ERR_NAN;
-            break;
-        }
-        hist[4 * k + 0] = sc[SC_A];
-        *steps_done = it + 1;
-        if (sc[SC_CONV] != 0.0) { *converged = 1; break; }
-        hist[4 * k + 1] = sc[SC_B];
-        hist[4 * k + 2] = sc[SC_C];
-        hist[4 * (k + 1) + 3] = sc[SC_SNORM];
         if (full_reorth) {
             int nvec = k + 1;
             double *part = ctx->rcoef + 2 * (capacity + 1);
@@ -521,9 +536,45 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
                                                  std::min(kProjMax, nvec - j0), P, qn, pn);
             k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, k + 1, part);
             k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) { set_error("reorth launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
         }
+        {
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
+        }
+        if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
+        // read back steps next..k: hist rows next..k+1 and their status
+        int cnt = k - next + 1;
+        double *hh = ctx->stat_host, *hs = ctx->stat_host + 4 * (capacity + 1);
+        if (cudaMemcpyAsync(hh, ctx->hist_dev + 4 * next, sizeof(double) * 4 * (cnt + 1),
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(hs, ctx->stat_dev + next, sizeof(double) * cnt,
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+            rc = TDSCHA_ERR_CUDA;
+            break;
+        }
+        if ((rc = mixed_check_error(ctx)) != TDSCHA_OK) break;
+        for (int j = 0; j < cnt; ++j) {
+            int kj = next + j;
+            if (hs[j] == ST_NAN) {
+                set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", kj);
+                rc = TDSCHA_ERR_NAN;
+                stop = true;
+                break;
+            }
+            hist[4 * kj + 0] = hh[4 * j + 0];
+            *steps_done = kj - start_step + 1;
+            if (hs[j] == ST_CONV) {
+                *converged = 1;
+                stop = true;
+                break;
+            }
+            hist[4 * kj + 1] = hh[4 * j + 1];
+            hist[4 * kj + 2] = hh[4 * j + 2];
+            hist[4 * (kj + 1) + 3] = hh[4 * (j + 1) + 3];
+        }
+        next = k + 1;
     }
     return rc;
 }

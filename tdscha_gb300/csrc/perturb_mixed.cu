@@ -566,7 +566,7 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
     int n = blockIdx.x;
     float mx = 0.f;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x)
-        if (n < M && m < M) mx = fmaxf(mx, fabsf((float)(Y1[(long)n * M + m] * (double)sd[m])));
+        if (n < M && m < M) mx = fmaxf(mx, fabsf((float)Y1[(long)n * M + m] * sd[m]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
@@ -579,9 +579,9 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
     }
     __syncthreads();
     float t = red[0] > 0.f ? red[0] : 1.f;
-    double inv = 1.0 / (double)t;
+    float inv = 1.f / t;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
-        float x = (n < M && m < M) ? (float)(Y1[(long)n * M + m] * (double)sd[m] * inv) : 0.f;
+        float x = (n < M && m < M) ? (float)Y1[(long)n * M + m] * sd[m] * inv : 0.f;
         __half h, l;
         split_f16(x, h, l);
         y_hi[(long)n * Mp + m] = h;
@@ -624,7 +624,18 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, in
         ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
         mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, o));
     }
+    // one atomic per block and value (same-address atomics serialise)
+    __shared__ float red[2][32];
     if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = ma;
+        red[1][threadIdx.x >> 5] = mb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            ma = fmaxf(ma, red[0][k]);
+            mb = fmaxf(mb, red[1][k]);
+        }
         atomic_max_pos(absmax, ma);
         atomic_max_pos(absmax + 1, mb);
     }
@@ -713,9 +724,15 @@ __global__ void k_gsum(const float *__restrict__ gpart, int nsplit, int ldG, int
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         int a = (int)(e / M), b = (int)(e % M);
         const float *g = gpart + (long)a * ldG + b;
-        double acc = 0;
-        for (int s = 0; s < nsplit; ++s) acc += (double)g[s * stride];
-        gs[e] = acc;
+        // compensated fp32 sum (float64 adds are slow on this part)
+        float sum = 0.f, comp = 0.f;
+        for (int s = 0; s < nsplit; ++s) {
+            float y = g[s * stride] - comp;
+            float t = sum + y;
+            comp = (t - sum) - y;
+            sum = t;
+        }
+        gs[e] = (double)sum - (double)comp;
     }
 }
 
