@@ -337,6 +337,19 @@ def run_ours(args):
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak, "traffic": None, "peak_source": src,
                     "avg_launch_ms": tot_ms / cnt}
+            if prec_name == "mixed":
+                # three tensor products per K step (hi*hi, hi*lo, lo*hi) on the
+                # padded mode count: the tensor-pipe work behind `achieved`
+                Mp = ((M + 63) // 64) * 64
+                roof["tensor_work_incl_split_tflops"] = 3 * 2.0 * R * Mp * Mp / per_launch_s / 1e12
+                roof["frac_incl_split"] = roof["tensor_work_incl_split_tflops"] / peak
+                # DRAM bytes per launch from the ncu capture of the same kernel at
+                # N=20 000 (profiles/k_gemm_tc_m573_n20k.md), scaled by image rows
+                per_row = {0: 143.8e6 / 20000, 3: 95.9e6 / 20000}[kid]
+                if M == 573:
+                    roof["traffic"] = per_row * R
+                    roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"
+                    roof["hbm_frac"] = per_row * R / per_launch_s / 1e9 / peaks.get("hbm_gbs", 6800.0)
         else:
             nbytes = 2.0 * R * M * 8
             achieved = nbytes / per_launch_s / 1e9
