@@ -39,6 +39,7 @@ extern "C" {
 #define TDSCHA_PREC_MIXED 1      /* split-bf16 x3 tensor-core GEMMs, fp32 accumulate */
 
 typedef struct tdscha_ctx tdscha_ctx;
+typedef struct tdscha_qctx tdscha_qctx;
 
 /* Text of the last error on this thread ("" if none). */
 const char *tdscha_last_error(void);
@@ -175,6 +176,65 @@ int tdscha_perturb_averages_noalloc(int M, int N, const double *X, const double 
                                     const double *w, const double *rho, const double *R1,
                                     const double *Y1, double T, int apply_D4, double *f_out,
                                     double *d2v_out, void *stream);
+
+/*
+ * q-space (Bloch basis) operator, float64 complex, Wigner only
+ * (QSpaceLanczos, Modules/QSpaceLanczos.py; perturbation averages
+ * get_perturb_averages_qspace_fused, Modules/tdscha_qspace.jl:455-712).
+ * Complex numbers are interleaved (re, im) doubles everywhere.
+ *
+ * tdscha_qctx_create: X_q, Y_q host (n_q, N, nb) complex, the Bloch-transformed
+ *   mass-scaled displacements and anharmonic forces projected on the q
+ *   polarisation vectors (_bloch_transform_ensemble, :221-296); w_q host
+ *   (nb, n_q) frequencies in Ry; valid (nb, n_q) 0/1 or NULL (all valid;
+ *   valid_modes_q, :181-191); rho (N); n_syms == 0 means the identity only,
+ *   otherwise n_syms sparse complex (n_q nb)^2 matrices in CSR form acting on
+ *   vectors indexed iq * nb + nu (the q-space symmetry matrices of
+ *   prepare_symmetrization, :1472-1657): sym_rowptr (n_syms x (n_q nb + 1)),
+ *   each row pointer array indexing sym_col / sym_val (complex) from 0.
+ *   nb is limited to 32.  Replaces the Julia-side ensemble cache of
+ *   _call_julia_qspace (:775-830).
+ */
+int tdscha_qctx_create(tdscha_qctx **ctx, int n_q, int nb, int N, const double *X_q,
+                       const double *Y_q, const double *w_q, const int *valid,
+                       const double *rho, double T, int n_syms, const int *sym_rowptr,
+                       const int *sym_col, const double *sym_val);
+int tdscha_qctx_destroy(tdscha_qctx *ctx);
+
+/*
+ * Perturbation q-point and pairing (build_q_pair_map, :298-333, with the
+ * pairing given as q_pair_map[n_q], an involution; pairs (iq1 <= iq2) and the
+ * psi layout [R (nb) | a' blocks | b' blocks] follow _compute_block_layout,
+ * :335-364).  Writes the complex psi length and the number of pairs.
+ */
+int tdscha_qctx_set_pert(tdscha_qctx *ctx, int iq_pert, const int *q_pair_map,
+                         int ignore_harmonic, int ignore_v3, int ignore_v4, long *psi_size,
+                         int *n_pairs);
+
+/*
+ * get_perturb_averages_qspace (tdscha_qspace.jl:639-712): R1 (nb complex),
+ * alpha1 (n_pairs blocks of nb x nb complex, row-major) in; f_out (nb) and
+ * d2v_out (n_pairs x nb x nb) out.  device_ptrs selects device or host
+ * buffers; host calls synchronise.
+ */
+int tdscha_qperturb_averages(tdscha_qctx *ctx, const double *R1, const double *alpha1,
+                             int apply_d4, double *f_out, double *d2v_out, int device_ptrs,
+                             void *stream);
+
+/* apply_full_L (QSpaceLanczos.py:941-961): device psi_in / psi_out of psi_size complex. */
+int tdscha_qapply_full_L(tdscha_qctx *ctx, const double *psi_in, double *psi_out, void *stream);
+
+/*
+ * Hermitian Lanczos (run_FT, QSpaceLanczos.py:967-1182): basis_Q, basis_P
+ * distinct device buffers of capacity x (2 psi_size) doubles, rows 0..start_step
+ * filled (row 0 the start vector normalised in the mask product, P = Q).
+ * reorthogonalize != 0 is the reference's default Gram-Schmidt against all Q
+ * vectors with P = Q and s_norm = c (:1110-1125); 0 is its plain recurrence
+ * (n_rep_orth = 0).  hist / steps_done / converged as tdscha_lanczos_run.
+ */
+int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                        int start_step, int n_iter, int reorthogonalize, double *hist,
+                        int *steps_done, int *converged, void *stream);
 
 #ifdef __cplusplus
 }

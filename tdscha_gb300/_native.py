@@ -22,6 +22,8 @@ EXPORTS = [
     "tdscha_perturb_averages", "tdscha_apply_full_L", "tdscha_lanczos_run",
     "tdscha_continued_fraction", "tdscha_ctx_profile", "tdscha_ctx_profile_read",
     "tdscha_perturb_averages_noalloc",
+    "tdscha_qctx_create", "tdscha_qctx_destroy", "tdscha_qctx_set_pert",
+    "tdscha_qperturb_averages", "tdscha_qapply_full_L", "tdscha_qlanczos_run",
 ]
 
 
@@ -69,6 +71,16 @@ def load():
     lib.tdscha_ctx_profile_read.argtypes = [_vp, _c_int, _d, _i]
     lib.tdscha_perturb_averages_noalloc.argtypes = [
         _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_double, _c_int, _vp, _vp, _vp]
+    lib.tdscha_qctx_create.argtypes = [
+        ctypes.POINTER(_vp), _c_int, _c_int, _c_int, _d, _d, _d, _i, _d, _c_double, _c_int, _i,
+        _i, _d]
+    lib.tdscha_qctx_destroy.argtypes = [_vp]
+    lib.tdscha_qctx_set_pert.argtypes = [_vp, _c_int, _i, _c_int, _c_int, _c_int,
+                                         ctypes.POINTER(ctypes.c_long), _i]
+    lib.tdscha_qperturb_averages.argtypes = [_vp, _vp, _vp, _c_int, _vp, _vp, _c_int, _vp]
+    lib.tdscha_qapply_full_L.argtypes = [_vp, _vp, _vp, _vp]
+    lib.tdscha_qlanczos_run.argtypes = [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _d, _i,
+                                        _i, _vp]
     for name in EXPORTS:
         fn = getattr(lib, name)
         if name not in ("tdscha_last_error", "tdscha_version"):
@@ -149,6 +161,99 @@ class Context:
     def close(self):
         if getattr(self, "handle", None):
             load().tdscha_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def csr_symmetries(symmetries, L):
+    """q-space symmetry matrices (dense or scipy.sparse, (L, L) complex) -> the
+    C-ABI CSR tables: row pointers (n_syms x (L + 1)) into one shared column /
+    value list."""
+    rowptr, cols, vals = [], [], []
+    base = 0
+    for S in symmetries:
+        if hasattr(S, "tocsr"):
+            S = S.tocsr()
+            S.sort_indices()
+            rp, ci, v = S.indptr, S.indices, S.data
+        else:
+            S = np.asarray(S)
+            nz = [np.nonzero(S[a])[0] for a in range(S.shape[0])]
+            rp = np.concatenate([[0], np.cumsum([len(z) for z in nz])])
+            ci = np.concatenate(nz) if len(nz) else np.zeros(0, dtype=int)
+            v = np.concatenate([S[a, z] for a, z in enumerate(nz)]) if len(nz) else np.zeros(0)
+        if S.shape != (L, L):
+            raise ValueError("symmetry matrix of shape %s, expected (%d, %d)" % (S.shape, L, L))
+        rowptr.append(np.asarray(rp, dtype=np.int64) + base)
+        cols.append(np.asarray(ci, dtype=np.int64))
+        vals.append(np.asarray(v, dtype=np.complex128))
+        base += len(ci)
+    if base >= 2 ** 31:
+        raise ValueError("symmetry tables too large")
+    return (i32(np.concatenate(rowptr)), i32(np.concatenate(cols) if cols else np.zeros(1)),
+            f64(np.concatenate(vals).view(np.float64) if vals else np.zeros(2)))
+
+
+class QContext:
+    """Owns a tdscha_qctx: the Bloch-transformed ensemble resident on the GPU."""
+
+    def __init__(self, X_q, Y_q, w_q, rho, T, valid=None, symmetries=None):
+        lib = load()
+        X_q = np.ascontiguousarray(X_q, dtype=np.complex128)
+        Y_q = np.ascontiguousarray(Y_q, dtype=np.complex128)
+        if X_q.ndim != 3 or Y_q.shape != X_q.shape:
+            raise ValueError("X_q and Y_q must be (n_q, N, n_bands) arrays of the same shape")
+        n_q, N, nb = X_q.shape
+        w_q = f64(w_q)
+        if w_q.shape != (nb, n_q):
+            raise ValueError("w_q must be (n_bands, n_q) = (%d, %d), got %s" % (nb, n_q, w_q.shape))
+        rho = f64(rho)
+        if rho.shape != (N,):
+            raise ValueError("len(rho) = %d does not match N = %d" % (rho.shape[0], N))
+        vptr = None
+        if valid is not None:
+            valid = i32(np.asarray(valid).astype(np.intc))
+            if valid.shape != (nb, n_q):
+                raise ValueError("valid must be (n_bands, n_q)")
+            vptr = ip(valid)
+        n_syms, rp, ci, sv = 0, None, None, None
+        if symmetries is not None and len(symmetries) > 0:
+            rp, ci, sv = csr_symmetries(symmetries, n_q * nb)
+            n_syms = len(symmetries)
+        self.n_q, self.N, self.nb = n_q, N, nb
+        self.n_syms = max(1, n_syms)
+        h = _vp()
+        Xf, Yf = X_q.view(np.float64), Y_q.view(np.float64)
+        check(lib.tdscha_qctx_create(ctypes.byref(h), n_q, nb, N, dp(Xf), dp(Yf), dp(w_q), vptr,
+                                     dp(rho), float(T), n_syms,
+                                     ip(rp) if rp is not None else None,
+                                     ip(ci) if ci is not None else None,
+                                     dp(sv) if sv is not None else None))
+        self.handle = h
+        self.P = None
+        self.n_pairs = None
+
+    def set_pert(self, iq_pert, q_pair_map, ignore_harmonic=False, ignore_v3=False,
+                 ignore_v4=False):
+        qm = i32(q_pair_map)
+        if qm.shape != (self.n_q,):
+            raise ValueError("q_pair_map must have n_q = %d entries" % self.n_q)
+        P = ctypes.c_long()
+        npairs = ctypes.c_int()
+        check(load().tdscha_qctx_set_pert(self.handle, int(iq_pert), ip(qm), int(bool(ignore_harmonic)),
+                                          int(bool(ignore_v3)), int(bool(ignore_v4)),
+                                          ctypes.byref(P), ctypes.byref(npairs)))
+        self.P, self.n_pairs = int(P.value), int(npairs.value)
+        return self.P
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().tdscha_qctx_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

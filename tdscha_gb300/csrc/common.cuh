@@ -118,6 +118,40 @@ struct tdscha_ctx {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[8];
 };
 
+// q-space (Bloch basis) context, see qspace.cu
+struct tdscha_qctx {
+    int n_q = 0, nb = 0, N = 0, S = 1;
+    long R = 0;          // image rows N * S
+    int L = 0;           // n_q * nb (length of one image row)
+    double T = 0, sum_rho = 0;
+    double2 *Xr = nullptr, *Yr = nullptr;      // R x L image rows
+    double *fY = nullptr, *fpsi = nullptr;     // [q][nu] (0 for masked modes)
+    double *rho = nullptr;
+    std::vector<double> w_q;                   // [nu][q] host copy
+    std::vector<int> valid;                    // [nu][q]
+    // perturbation layout (tdscha_qctx_set_pert)
+    int iq_pert = -1, n_pairs = 0;
+    long P = 0;                                // complex psi length
+    int ignore_harmonic = 0, ignore_v3 = 0, ignore_v4 = 0;
+    int *qpair = nullptr, *qrole = nullptr, *qpartner = nullptr;   // per q
+    int *pair_q = nullptr;                     // 2 per pair
+    int *elem = nullptr;                       // per psi element: sector | pair | nu1 | nu2
+    double *pcoef = nullptr;                   // per pair block element: 6 coefficients
+    double *mask = nullptr;                    // 2P (per real component)
+    long *q_off = nullptr;                     // block offsets: a' (n_pairs), b' (n_pairs)
+    double *wpert = nullptr;                   // -(w^2) at q_pert (0 for masked modes)
+    // per-call scratch
+    double2 *R1 = nullptr, *alpha = nullptr, *f = nullptr, *d2v = nullptr;
+    double2 *rowc = nullptr;                   // 4 per image row
+    double2 *fpart = nullptr, *dpart = nullptr;
+    int nfchunk = 0, nbchunk = 0;
+    // Lanczos scratch (2P doubles each)
+    double *Lq = nullptr, *rk = nullptr, *sk = nullptr;
+    double *dots = nullptr, *scal = nullptr, *hist_dev = nullptr, *stat_dev = nullptr;
+    double *stat_host = nullptr, *pqn = nullptr, *rcoef = nullptr;
+    int hist_cap = 0;
+};
+
 namespace tdscha {
 
 // perturb_fp64.cu
@@ -132,6 +166,8 @@ int mixed_check_error(tdscha_ctx *c);
 int build_pair_coeffs(tdscha_ctx *c);
 int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,
                      int precision, cudaStream_t st);
+// qspace.cu
+int q_apply_full_L_dev(tdscha_qctx *c, const double *psi_in, double *psi_out, cudaStream_t st);
 // shared: f / d2v finalisation from the row scalars and G partials
 int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t st);
 

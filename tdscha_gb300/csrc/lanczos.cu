@@ -209,7 +209,8 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
 
 // ---------------------------------------------------------------------------
 // Lanczos recurrence.  Device scalars (ctx->scal):
-enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN, SC_HALT };
+enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN, SC_HALT,
+       SC_NEXT };   // SC_NEXT: the last re-orthogonalised vector had zero norm
 // per-step status written on the device: 0 running, 1 NaN in a, 2 converged
 enum { ST_OK = 0, ST_NAN = 1, ST_CONV = 2 };
 // hist_dev rows of 4: a_k, b_k, c_k, s_norm_k.
@@ -315,7 +316,7 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
     scal[SC_C] = c;
     scal[SC_SNORM] = s_norm;
     scal[SC_SRAW] = s_raw;
-    bool conv = fabs(b) < kEps || fabs(c) < kEps;
+    bool conv = fabs(b) < kEps || fabs(c) < kEps || scal[SC_NEXT] != 0.0;
     scal[SC_CONV] = conv ? 1.0 : 0.0;
     if (conv) {
         status[k] = ST_CONV;
@@ -422,6 +423,69 @@ __global__ void k_pq_finish(const double *__restrict__ part, int cnt, int j0,
     double a = 0;
     for (int c = 0; c < kDotChunks; ++c) a += part[(long)j * kDotChunks + c];
     out[j0 + j] = a;
+}
+
+// q-space Hermitian re-orthogonalisation tail: q_{k+1} /= |q_{k+1}|, p_{k+1} = q_{k+1}
+// and s_norm_{k+1} = c_k (QSpaceLanczos.py:1110-1125).  Every block reduces the
+// same partials in the same order, so all blocks scale by the same factor.
+__global__ void k_qrenorm(const double *__restrict__ part, int nblk, double *__restrict__ scal,
+                          double *__restrict__ hist, int k, long n, double *__restrict__ qn,
+                          double *__restrict__ pn) {
+    __shared__ double sh[32];
+    __shared__ double inv_s;
+    if (scal[SC_HALT] != 0.0) return;
+    double s = reduce_parts(part, nblk, sh);
+    if (threadIdx.x == 0) {
+        double nrm = sqrt(s);
+        inv_s = 1.0 / nrm;
+        if (blockIdx.x == 0) {
+            if (nrm < kEps) scal[SC_NEXT] = 1.0;
+            hist[4 * (k + 1) + 3] = scal[SC_C];
+        }
+    }
+    __syncthreads();
+    const double iv = inv_s;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        double v = qn[e] * iv;
+        qn[e] = v;
+        pn[e] = v;
+    }
+}
+
+// Copies hist rows / status of steps next..k back to the host and applies the
+// stop conditions; returns TDSCHA_OK or an error and sets *stop.
+static int read_back_steps(double *hist_dev, double *stat_dev, double *stat_host, int capacity,
+                           int next, int k, cudaStream_t st, double *hist, int start_step,
+                           int *steps_done, int *converged, bool *stop) {
+    int cnt = k - next + 1;
+    double *hh = stat_host, *hs = stat_host + 4 * (capacity + 1);
+    if (cudaMemcpyAsync(hh, hist_dev + 4 * next, sizeof(double) * 4 * (cnt + 1),
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(hs, stat_dev + next, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+        return TDSCHA_ERR_CUDA;
+    }
+    for (int j = 0; j < cnt; ++j) {
+        int kj = next + j;
+        if (hs[j] == ST_NAN) {
+            set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", kj);
+            *stop = true;
+            return TDSCHA_ERR_NAN;
+        }
+        hist[4 * kj + 0] = hh[4 * j + 0];
+        *steps_done = kj - start_step + 1;
+        if (hs[j] == ST_CONV) {
+            *converged = 1;
+            *stop = true;
+            return TDSCHA_OK;
+        }
+        hist[4 * kj + 1] = hh[4 * j + 1];
+        hist[4 * kj + 2] = hh[4 * j + 2];
+        hist[4 * (kj + 1) + 3] = hh[4 * (j + 1) + 3];
+    }
+    return TDSCHA_OK;
 }
 
 }  // namespace tdscha
@@ -542,38 +606,12 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
         }
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
-        // read back steps next..k: hist rows next..k+1 and their status
-        int cnt = k - next + 1;
-        double *hh = ctx->stat_host, *hs = ctx->stat_host + 4 * (capacity + 1);
-        if (cudaMemcpyAsync(hh, ctx->hist_dev + 4 * next, sizeof(double) * 4 * (cnt + 1),
-                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaMemcpyAsync(hs, ctx->stat_dev + next, sizeof(double) * cnt,
-                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) {
-            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
-            rc = TDSCHA_ERR_CUDA;
-            break;
-        }
-        if ((rc = mixed_check_error(ctx)) != TDSCHA_OK) break;
-        for (int j = 0; j < cnt; ++j) {
-            int kj = next + j;
-            if (hs[j] == ST_NAN) {
-                set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", kj);
-                rc = TDSCHA_ERR_NAN;
-                stop = true;
-                break;
-            }
-            hist[4 * kj + 0] = hh[4 * j + 0];
-            *steps_done = kj - start_step + 1;
-            if (hs[j] == ST_CONV) {
-                *converged = 1;
-                stop = true;
-                break;
-            }
-            hist[4 * kj + 1] = hh[4 * j + 1];
-            hist[4 * kj + 2] = hh[4 * j + 2];
-            hist[4 * (kj + 1) + 3] = hh[4 * (j + 1) + 3];
-        }
+        rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
+                             hist, start_step, steps_done, converged, &stop);
+        // a timed-out tensor-core wait outranks whatever the read-back saw
+        int mrc = mixed_check_error(ctx);
+        if (mrc != TDSCHA_OK) { rc = mrc; break; }
+        if (rc != TDSCHA_OK) break;
         next = k + 1;
     }
     return rc;
@@ -682,4 +720,100 @@ extern "C" int tdscha_continued_fraction(const double *a, int n, const double *b
     cudaFree(d_a); cudaFree(d_b); cudaFree(d_c); cudaFree(d_w); cudaFree(d_g);
     if (e != cudaSuccess) { set_error("continued_fraction: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
     return TDSCHA_OK;
+}
+
+extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                                   int start_step, int n_iter, int reorthogonalize, double *hist,
+                                   int *steps_done, int *converged, void *stream) {
+    set_error("");
+    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
+        set_error("qlanczos_run: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    if (ctx->n_pairs == 0) { set_error("qlanczos_run: call tdscha_qctx_set_pert first"); return TDSCHA_ERR_STATE; }
+    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
+        set_error("qlanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
+        return TDSCHA_ERR_ARG;
+    }
+    if (basis_Q == basis_P) { set_error("qlanczos_run: basis_Q and basis_P must be distinct"); return TDSCHA_ERR_ARG; }
+    *steps_done = 0;
+    *converged = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const long n = 2 * ctx->P;           // interleaved (re, im) doubles
+    const double *mask = ctx->mask;
+    if (ctx->hist_cap < capacity + 1) {
+        if (ctx->hist_dev) cudaFree(ctx->hist_dev);
+        if (ctx->stat_dev) cudaFree(ctx->stat_dev);
+        if (ctx->stat_host) cudaFreeHost(ctx->stat_host);
+        if (ctx->pqn) cudaFree(ctx->pqn);
+        if (ctx->rcoef) cudaFree(ctx->rcoef);
+        ctx->hist_dev = ctx->stat_dev = ctx->stat_host = ctx->pqn = ctx->rcoef = nullptr;
+        ctx->hist_cap = 0;
+        TDS_CUDA(cudaMalloc(&ctx->hist_dev, sizeof(double) * 4 * (capacity + 1)));
+        TDS_CUDA(cudaMalloc(&ctx->stat_dev, sizeof(double) * (capacity + 1)));
+        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 5 * (capacity + 1)));
+        TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
+        TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kDotChunks + 1)));
+        ctx->hist_cap = capacity + 1;
+    }
+    TDS_CUDA(cudaMemcpyAsync(ctx->hist_dev, hist, sizeof(double) * 4 * (start_step + 1),
+                             cudaMemcpyHostToDevice, st));
+    double *part = ctx->rcoef + 2 * (capacity + 1);
+    if (reorthogonalize) {
+        // Q is orthonormal in the mask product; the weights q_j . q_j are kept exact
+        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, 0, part);
+        k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
+        TDS_CHECK_LAUNCH();
+    }
+    TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
+    constexpr int kSyncEvery = 16;
+    int rc = TDSCHA_OK;
+    const int nb = std::max(1, std::min(ceil_div(n, kDotThreads), 296));
+    int next = start_step;
+    bool stop = false;
+    for (int it = 0; it < n_iter && !stop; ++it) {
+        int k = start_step + it;
+        if (k + 1 >= capacity) {
+            set_error("qlanczos_run: basis capacity %d exhausted at step %d", capacity, k);
+            rc = TDSCHA_ERR_ARG;
+            break;
+        }
+        double *q = basis_Q + (long)k * n, *p = basis_P + (long)k * n;
+        // Hermitian operator: p_L = L q (QSpaceLanczos.py:1055-1057)
+        if ((rc = q_apply_full_L_dev(ctx, q, ctx->Lq, st)) != TDSCHA_OK) break;
+        k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, n, ctx->dots);
+        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+        const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * n : nullptr;
+        const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * n : nullptr;
+        k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, ctx->Lq, q, p, qprev, pprev, mask, ctx->scal, n,
+                                             ctx->rk, ctx->sk, ctx->dots, nb);
+        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+        double *qn = basis_Q + (long)(k + 1) * n, *pn = basis_P + (long)(k + 1) * n;
+        k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, n, qn, pn);
+        if (reorthogonalize) {
+            // one classical Gram-Schmidt pass of q_{k+1} against q_0..q_k with the
+            // real mask product (the p side of the shared kernels runs on the
+            // p_{k+1} slot, which the renormalisation then overwrites)
+            int nvec = k + 1;
+            k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, qn, pn, mask, n, n, part);
+            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
+            for (int j0 = 0; j0 < nvec; j0 += kProjMax)
+                k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_Q, ctx->rcoef, n, j0,
+                                                 std::min(kProjMax, nvec - j0), n, qn, pn);
+            k_dot1<<<nb, kDotThreads, 0, st>>>(qn, qn, mask, n, ctx->dots);
+            k_qrenorm<<<nb, kDotThreads, 0, st>>>(ctx->dots, nb, ctx->scal, ctx->hist_dev, k, n, qn, pn);
+            k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);
+            k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
+        }
+        {
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) { set_error("qlanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
+        }
+        if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
+        rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
+                             hist, start_step, steps_done, converged, &stop);
+        if (rc != TDSCHA_OK) break;
+        next = k + 1;
+    }
+    return rc;
 }

@@ -142,3 +142,84 @@ WORKLOADS = {
     # whole context stays under 1 GB (used for full profiler captures)
     "m573_n20k": dict(M=573, N=20000, n_syms=1, rho_sigma=0.1, steps=300),
 }
+
+
+def qgrid(dims):
+    """Monkhorst-Pack-style Gamma-centred grid in crystal coordinates."""
+    d = list(dims) + [1] * (3 - len(dims))
+    return np.array([[i / d[0], j / d[1], k / d[2]] for i in range(d[0]) for j in range(d[1])
+                     for k in range(d[2])])
+
+
+def make_qspace_ensemble(dims, nb, N, seed=0, T=300.0, w_min_cm=50.0, w_max_cm=500.0,
+                         dispersion=0.0, anh_scale=0.05, rho_sigma=0.0, rank=None):
+    """Seeded supercell ensemble and its Bloch transform.
+
+    Real-space cells R on the grid `dims` (n_q cells), nb bands per cell with
+    frequencies w_q[nu, q] = w_nu * (1 + dispersion * (1 - cos 2 pi q.1)/2);
+    displacements drawn in q space with X_{-q} = conj(X_q) (so the supercell
+    data are real), transformed back to real space, forces from a fully
+    symmetric CP cubic + quartic potential of the real-space coordinates,
+    then Bloch transformed:
+        X_q[iq, i, nu] = n_q^{-1/2} sum_R exp(-2 pi i q.R) u[i, R, nu].
+    Returns the q-space arrays and the matching real-space ones (modes ordered
+    band-major: index nu * n_q + R).
+    """
+    rng = np.random.default_rng(seed)
+    q = qgrid(dims)
+    n_q = len(q)
+    R = q * np.array(list(dims) + [1] * (3 - len(dims)))[None, :]   # integer cell coords
+    d = list(dims) + [1] * (3 - len(dims))
+    cells = np.array([[i, j, k] for i in range(d[0]) for j in range(d[1]) for k in range(d[2])])
+    wb = np.sort(rng.uniform(w_min_cm, w_max_cm, nb)) / RY_TO_CM
+    w_q = np.zeros((nb, n_q))
+    for iq in range(n_q):
+        w_q[:, iq] = wb * (1 + dispersion * (1 - np.cos(2 * np.pi * q[iq].sum())) / 2)
+    phase = np.exp(-2j * np.pi * (q @ cells.T))              # (n_q, n_cells)
+    # displacements: real-space Gaussian with the per-q covariance, via q space
+    X_q = np.zeros((n_q, N, nb), dtype=np.complex128)
+    minus = np.array([np.argmin(np.abs(((q + q[i] + 0.5) % 1.0) - 0.5).sum(1)) for i in range(n_q)])
+    for iq in range(n_q):
+        jq = minus[iq]
+        sig = np.sqrt(f_psi(w_q[:, iq], T))
+        if jq == iq:
+            X_q[iq] = rng.standard_normal((N, nb)) * sig
+        elif iq < jq:
+            z = (rng.standard_normal((N, nb)) + 1j * rng.standard_normal((N, nb))) / np.sqrt(2)
+            X_q[iq] = z * sig
+            X_q[jq] = np.conj(X_q[iq])
+    u = np.real(np.einsum("qc,qin->icn", np.conj(phase), X_q)) / np.sqrt(n_q)   # (N, cells, nb)
+    M = n_q * nb
+    ureal = np.ascontiguousarray(np.transpose(u, (0, 2, 1)).reshape(N, M))     # band-major
+    Rk = rank if rank is not None else max(8, min(M, 64))
+    wreal = np.repeat(wb, n_q)
+    h_rms = np.sqrt(np.mean((ureal * wreal ** 2) ** 2))
+    f3 = _cp_force(ureal, 3, Rk, rng)
+    f3 *= anh_scale * h_rms / max(np.sqrt(np.mean(f3 ** 2)), 1e-300)
+    f4 = _cp_force(ureal, 4, Rk, rng)
+    f4 *= anh_scale * h_rms / max(np.sqrt(np.mean(f4 ** 2)), 1e-300)
+    freal = f3 + f4
+    rho = np.exp(rng.normal(0.0, rho_sigma, N)) if rho_sigma > 0 else np.ones(N)
+    freal -= (rho[:, None] * freal).sum(0) / rho.sum()
+    fcell = np.transpose(freal.reshape(N, nb, n_q), (0, 2, 1))                  # (N, cells, nb)
+    Y_q = np.einsum("qc,icn->qin", phase, fcell) / np.sqrt(n_q)
+    return dict(X_q=X_q, Y_q=Y_q, w_q=w_q, rho=rho, T=float(T), q=q, dims=tuple(d),
+                X_real=ureal, Y_real=freal, w_real=wreal, n_q=n_q, nb=nb, cells=cells)
+
+
+def translation_tables(n_q, nb, cells, dims):
+    """Real-space symmetry tables of all lattice translations (band-major modes):
+    one block per band (its n_q cell copies), each translation a permutation."""
+    d = np.array(dims)
+    idx = {tuple(c): i for i, c in enumerate(cells)}
+    blocks = []
+    for nu in range(nb):
+        mats = np.zeros((n_q, n_q, n_q))
+        for t, tc in enumerate(cells):
+            for r, rc in enumerate(cells):
+                s = idx[tuple((rc + tc) % d)]
+                mats[t, s, r] = 1.0
+        blocks.append(mats)
+    spaces = [np.arange(nu * n_q, (nu + 1) * n_q, dtype=np.intc) for nu in range(nb)]
+    bid = np.repeat(np.arange(nb), n_q).astype(np.intc)
+    return blocks, spaces, bid
