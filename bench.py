@@ -48,6 +48,9 @@ def parse():
                     help="steps of the mixed-vs-float64 spectral check (default: the workload's)")
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="timed steps of the float64 comparison arm")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the secondary measurements of the other operator paths")
+    ap.add_argument("--qworkload", default="q444_nb12_n10k")
     ap.add_argument("--no-reorth", action="store_true",
                     help="plain recurrence (the reference default); without full "
                          "re-biorthogonalisation the spectral check is not reproducible "
@@ -374,10 +377,13 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(ens, 15.0, 2)
+    rows = {}
+    if not args.no_rows:
+        rows["qspace"] = qspace_leg(args.qworkload, K, W, dev, peaks, with_cpu=not args.no_cpu)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "bf16x3+f64",
+                "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "fp16x3+f64",
                 "data": "synthetic (seeded ensemble with the workload's shapes)",
                 "precision": prec_name,
                 "config": {"workload": args.workload, "M": M, "N": N, "n_syms": spec["n_syms"],
@@ -388,7 +394,7 @@ def run_ours(args):
                            "l2": "inputs larger than L2 (ensemble %.0f MB)" % (2 * R * M * 8 / 1e6)},
                 "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
                 "fp64_gpu": fp64, "accuracy_vs_fp64": check,
-                "clocks": clocks, "gpu_launches": gpu_launches,
+                "clocks": clocks, "gpu_launches": gpu_launches, "other_paths": rows,
                 "flops_per_application": flops_app}
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -484,6 +490,86 @@ def fp64_arm_and_check(args, ens, spec, syms, spaces, bid, dev, local):
         out["full_run_steps_per_s"] = {"fp64": n_check / t64, "mixed": n_check / tmx}
     ctx64.close()
     return out, check
+
+
+def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):
+    """q-space (Bloch basis) operator and Hermitian Lanczos, float64 complex:
+    steps/s through QSpaceLanczos.run_FT, per-application device time of
+    tdscha_qapply_full_L (CUDA events), FP64 roofline, CPU oracle sample."""
+    import torch
+    from tdscha_gb300 import _native as nat
+    from tdscha_gb300.QSpaceLanczos import QSpaceLanczos
+    from tdscha_gb300.synthetic import QWORKLOADS, make_qspace_ensemble
+    spec = QWORKLOADS[qname]
+    e = make_qspace_ensemble(spec["dims"], spec["nb"], spec["N"], seed=7, rho_sigma=0.1,
+                             dispersion=0.3)
+    nb, n_q, N = spec["nb"], e["n_q"], spec["N"]
+    lz = QSpaceLanczos.from_arrays(e["X_q"], e["Y_q"], e["w_q"], e["rho"], e["T"],
+                                   q_points=e["q"])
+    lz.init(use_symmetries=False)
+    lz.prepare_mode_q(0, nb // 2)
+    stream = torch.cuda.current_stream()
+    lz.run_FT(W, verbose=False)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    lz.run_FT(K, verbose=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    steps_s = K / (e0.elapsed_time(e1) / 1e3)
+    # one application at a time on device buffers
+    ctx = lz._qcontext()
+    P = ctx.P
+    rng = np.random.default_rng(3)
+    psi = torch.from_numpy(rng.standard_normal(2 * P)).to(dev)
+    out = torch.empty_like(psi)
+    lib = nat.load()
+    st = stream.cuda_stream
+    for _ in range(3):
+        nat.check(lib.tdscha_qapply_full_L(ctx.handle, psi.data_ptr(), out.data_ptr(), st))
+    torch.cuda.synchronize()
+    reps = max(K, 10)
+    e0.record(stream)
+    for _ in range(reps):
+        nat.check(lib.tdscha_qapply_full_L(ctx.handle, psi.data_ptr(), out.data_ptr(), st))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    app_s = e0.elapsed_time(e1) / 1e3 / reps
+    n_pairs = ctx.n_pairs
+    R = N
+    L = n_q * nb
+    # complex FMA = 8 flops: u = A x on every q (n_q nb^2), x^H u and u^H g (2 L),
+    # d2v two FMAs per block element per row
+    flops = R * (8.0 * n_q * nb * nb + 16.0 * L) + R * n_pairs * nb * nb * 16.0
+    achieved = flops / app_s / 1e12
+    out_d = {"workload": qname, "dims": list(spec["dims"]), "n_bands": nb, "N": N,
+             "n_pairs": n_pairs, "psi_size": P,
+             "lanczos_steps_per_s": steps_s,
+             "lanczos": "Hermitian, Gram-Schmidt against all stored vectors (reference default)",
+             "application_ms": app_s * 1e3,
+             "roofline": {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                          "frac": achieved / 1.25,
+                          "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
+                          "flops_per_application": flops},
+             "ensemble_bytes": 2 * e["X_q"].nbytes}
+    if with_cpu:
+        import oracle.qspace as oq
+        ns = min(N, 400)
+        R1 = np.zeros(nb, dtype=complex)
+        R1[nb // 2] = 1
+        blocks = [np.ones((nb, nb), dtype=complex)] * n_pairs
+        pairs = [(q1, int(lz.q_pair_map[q1])) for q1 in range(n_q) if q1 <= lz.q_pair_map[q1]]
+        t0 = time.perf_counter()
+        oq.perturb_averages_qspace(e["X_q"][:, :ns], e["Y_q"][:, :ns], e["w_q"], e["rho"][:ns],
+                                   R1, blocks, e["T"], True, 0, pairs)
+        dt = (time.perf_counter() - t0) * N / ns
+        out_d["cpu_baseline"] = {"value": 1.0 / dt, "unit": "applications/s", "cores": os.cpu_count(),
+                                 "kind": "port",
+                                 "sample": "oracle q-space averages (numpy) over %d of %d "
+                                           "configurations, scaled" % (ns, N)}
+    lz._invalidate()
+    return out_d
 
 
 def measure_e2e(ens, spec, prec_name, K, W, reorth):

@@ -32,6 +32,21 @@ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {   // a * conj(b
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// acc + a b and acc + conj(a) b as four explicit FMAs each
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 acc) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+    return acc;
+}
+__device__ __forceinline__ double2 cfma_conj(double2 a, double2 b, double2 acc) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+    return acc;
+}
 
 // x_rot = S_j x_i for every image row, S_j in CSR (identity when n_syms == 0).
 __global__ void k_q_expand(const double2 *__restrict__ X, const double2 *__restrict__ Y, int N,
@@ -97,62 +112,93 @@ __global__ void k_q_unpack(const double2 *__restrict__ psi, const int *__restric
     }
 }
 
-// Per image row: q-space row scalars; one warp per row.
-__global__ void k_q_rows(const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
-                         const double *__restrict__ fY, const double *__restrict__ fpsi,
-                         const double *__restrict__ rho, const double2 *__restrict__ R1,
-                         const double2 *__restrict__ alpha, const int *__restrict__ qpair,
-                         const int *__restrict__ qrole, const int *__restrict__ qpartner,
-                         int n_q, int nb, int S, long R, int iq_pert, int apply_d4,
-                         double2 *__restrict__ rowc) {
-    int lane = threadIdx.x & 31;
-    long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (r >= R) return;
+// Per image row: q-space row scalars.  A block of 256 threads takes
+// rows_per_block rows; the lw = 256 / rows_per_block threads of a row stride
+// over its n_q nb entries and reduce through warp shuffles + shared memory.
+// One row per block when n_q nb >= 128 (the grid is then many waves deep).
+inline int q_rows_per_block(int L) {
+    int lw = std::min(256, ((L + 31) / 32) * 32);
+    return 256 / lw;
+}
+__global__ void __launch_bounds__(256, 4) k_q_rows(
+        const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
+        const double *__restrict__ fY, const double *__restrict__ fpsi,
+        const double *__restrict__ rho, const double2 *__restrict__ R1,
+        const double2 *__restrict__ alpha, const int *__restrict__ qpair,
+        const int *__restrict__ qrole, const int *__restrict__ qpartner,
+        int n_q, int nb, int S, long R, int iq_pert, int apply_d4, int rpb,
+        double2 *__restrict__ rowc) {
+    __shared__ double red[8][8];   // per warp: tot, bfw, wR, wRf (re, im)
+    const int lw = blockDim.x / rpb;
+    const int g = threadIdx.x / lw, t = threadIdx.x % lw;
+    long r = (long)blockIdx.x * rpb + g;
+    const bool live = r < R;
     const int L = n_q * nb;
-    const double2 *x = Xr + r * L, *y = Yr + r * L;
     double2 tot = make_double2(0, 0), bfw = make_double2(0, 0);
-    for (int a = lane; a < L; a += 32) {
-        int q = a / nb, nu = a % nb;
-        int p = qpair[q], role = qrole[q], q2 = qpartner[q];
-        const double2 *blk = alpha + (long)p * nb * nb;
-        double2 u = make_double2(0, 0);
-        for (int k = 0; k < nb; ++k) {
-            // role 0: alpha[nu][k]; role 1: conj(alpha[k][nu])
-            double2 av = role == 0 ? blk[nu * nb + k] : cconj(blk[k * nb + nu]);
-            u = cadd(u, cmul(av, x[q2 * nb + k]));
-        }
-        tot = cadd(tot, cmulc(u, x[a]));      // conj(x) u
-        double2 g = cscale(y[a], fpsi[a]);
-        bfw = cadd(bfw, cmulc(g, u));          // conj(u) g
-    }
     double2 wR = make_double2(0, 0), wRf = make_double2(0, 0);
-    for (int nu = lane; nu < nb; nu += 32) {
-        int a = iq_pert * nb + nu;
-        wR = cadd(wR, cmulc(cscale(x[a], fY[a]), R1[nu]));    // fY x conj(R1)
-        wRf = cadd(wRf, cmulc(y[a], R1[nu]));                   // conj(R1) y
+    if (live) {
+        const double2 *x = Xr + r * L, *y = Yr + r * L;
+        for (int a = t; a < L; a += lw) {
+            int q = a / nb, nu = a - q * nb;
+            int p = qpair[q], role = qrole[q], q2 = qpartner[q];
+            const double2 *blk = alpha + (long)p * nb * nb;
+            const double2 *xp = x + q2 * nb;
+            double2 u = make_double2(0, 0), u2 = make_double2(0, 0);
+            // role 0: alpha[nu][k]; role 1: conj(alpha[k][nu])
+            if (role == 0) {
+                const double2 *ar = blk + nu * nb;
+                int k = 0;
+                for (; k + 1 < nb; k += 2) {
+                    u = cfma(ar[k], xp[k], u);
+                    u2 = cfma(ar[k + 1], xp[k + 1], u2);
+                }
+                if (k < nb) u = cfma(ar[k], xp[k], u);
+            } else {
+                int k = 0;
+                for (; k + 1 < nb; k += 2) {
+                    u = cfma_conj(blk[k * nb + nu], xp[k], u);
+                    u2 = cfma_conj(blk[(k + 1) * nb + nu], xp[k + 1], u2);
+                }
+                if (k < nb) u = cfma_conj(blk[k * nb + nu], xp[k], u);
+            }
+            u = cadd(u, u2);
+            tot = cfma_conj(x[a], u, tot);                        // conj(x) u
+            bfw = cfma_conj(u, cscale(y[a], fpsi[a]), bfw);       // conj(u) g
+        }
+        for (int nu = t; nu < nb; nu += lw) {
+            int a = iq_pert * nb + nu;
+            wR = cadd(wR, cmulc(cscale(x[a], fY[a]), R1[nu]));    // fY x conj(R1)
+            wRf = cadd(wRf, cmulc(y[a], R1[nu]));                   // conj(R1) y
+        }
     }
+    double v[8] = {tot.x, tot.y, bfw.x, bfw.y, wR.x, wR.y, wRf.x, wRf.y};
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        tot.x += __shfl_xor_sync(0xffffffffu, tot.x, o);
-        tot.y += __shfl_xor_sync(0xffffffffu, tot.y, o);
-        bfw.x += __shfl_xor_sync(0xffffffffu, bfw.x, o);
-        bfw.y += __shfl_xor_sync(0xffffffffu, bfw.y, o);
-        wR.x += __shfl_xor_sync(0xffffffffu, wR.x, o);
-        wR.y += __shfl_xor_sync(0xffffffffu, wR.y, o);
-        wRf.x += __shfl_xor_sync(0xffffffffu, wRf.x, o);
-        wRf.y += __shfl_xor_sync(0xffffffffu, wRf.y, o);
-    }
-    if (lane == 0) {
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) red[wid][k] = v[k];
+    __syncthreads();
+    if (live && t == 0) {
+        // the warps of this row: lw / 32 consecutive warps starting at its first
+        const int w0 = (g * lw) >> 5, nw = lw >> 5;
+        double s[8];
+        for (int k = 0; k < 8; ++k) {
+            s[k] = 0;
+            for (int w = 0; w < nw; ++w) s[k] += red[w0 + w][k];
+        }
+        tot = make_double2(s[0], s[1]);
+        bfw = make_double2(s[2], s[3]);
+        wR = make_double2(s[4], s[5]);
+        wRf = make_double2(s[6], s[7]);
         double rw = rho[r / S];
         double d4 = apply_d4 ? 1.0 : 0.0;
-        double2 w1 = cscale(tot, -0.5 * rw / 3.0);
-        double2 w2 = cscale(bfw, -rw / 3.0);
-        double2 wc = cadd(cscale(wR, rw / 3.0), cscale(tot, -d4 * rw / 8.0));
-        double2 wd = cadd(cscale(wRf, rw / 3.0), cscale(bfw, -d4 * rw / 4.0));
-        rowc[4 * r + 0] = w1;
-        rowc[4 * r + 1] = w2;
-        rowc[4 * r + 2] = wc;
-        rowc[4 * r + 3] = wd;
+        rowc[4 * r + 0] = cscale(tot, -0.5 * rw / 3.0);
+        rowc[4 * r + 1] = cscale(bfw, -rw / 3.0);
+        rowc[4 * r + 2] = cadd(cscale(wR, rw / 3.0), cscale(tot, -d4 * rw / 8.0));
+        rowc[4 * r + 3] = cadd(cscale(wRf, rw / 3.0), cscale(bfw, -d4 * rw / 4.0));
     }
 }
 
@@ -184,59 +230,75 @@ __global__ void k_q_favg(const double2 *__restrict__ Xr, const double2 *__restri
     }
 }
 
-// d2v partials per pair: block (pair, chunk), one thread per block element.
+// d2v partials per pair: block (pair, chunk).  Rows are staged kQRows at a
+// time as A1 = -w_cross u1, A2 = -(w_cross f1 + w_diag u1), conj(f2), conj(u2),
+// so every block element takes two complex FMAs per row:
+//   d2v_ij += A1_i conj(f2_j) + A2_i conj(u2_j)
+// Thread t owns element t % nbb for the rows of phase t / nbb (blocks with
+// nbb <= blockDim / 2 run several phases), phases summed in a fixed order.
 constexpr int kQRows = 16;   // rows staged in shared memory per pass
+inline int q_d2v_threads(int nb) {
+    int nbb = nb * nb;
+    return nbb <= 128 ? 256 : ((nbb + 31) / 32) * 32;
+}
 __global__ void k_q_d2v(const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
                         const double *__restrict__ fY, const double2 *__restrict__ rowc,
                         const int *__restrict__ pair_q, int L, int nb, long R, long chunk,
                         int n_pairs, double2 *__restrict__ dpart) {
-    extern __shared__ double2 sm[];   // kQRows x (4 nb + 2)
+    extern __shared__ double2 sm[];   // kQRows x 4 nb, reused for the phase sum
     const int p = blockIdx.x;
     const int q1 = pair_q[2 * p], q2 = pair_q[2 * p + 1];
-    const int stride = 4 * nb + 2;
-    long rb = (long)blockIdx.y * chunk, re = min(R, rb + chunk);
+    const int stride = 4 * nb;
     const int nbb = nb * nb;
-    double2 acc[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) acc[t] = make_double2(0, 0);
+    const int nph = max(1, (int)blockDim.x / nbb);
+    const int e = threadIdx.x % nbb, ph = threadIdx.x / nbb;
+    const bool active = ph < nph && (int)threadIdx.x < nph * nbb;
+    const int i = e / nb, j = e % nb;
+    long rb = (long)blockIdx.y * chunk, re = min(R, rb + chunk);
+    // two accumulators (the A1 and A2 products) to shorten the FMA chains
+    double2 acc = make_double2(0, 0), acc2 = make_double2(0, 0);
     for (long r0 = rb; r0 < re; r0 += kQRows) {
         int nr = (int)min((long)kQRows, re - r0);
         __syncthreads();
-        for (int t = threadIdx.x; t < nr * stride; t += blockDim.x) {
-            int rr = t / stride, c = t % stride;
+        for (int t = threadIdx.x; t < nr * 2 * nb; t += blockDim.x) {
+            int rr = t / (2 * nb), c = t % (2 * nb);
             long r = r0 + rr;
-            double2 v;
-            if (c < nb) v = cscale(Xr[r * L + q1 * nb + c], fY[q1 * nb + c]);                 // u1
-            else if (c < 2 * nb) v = Yr[r * L + q1 * nb + (c - nb)];                          // f1
-            else if (c < 3 * nb) v = cscale(Xr[r * L + q2 * nb + (c - 2 * nb)], fY[q2 * nb + (c - 2 * nb)]);  // u2
-            else if (c < 4 * nb) v = Yr[r * L + q2 * nb + (c - 3 * nb)];                      // f2
-            else v = rowc[4 * r + 2 + (c - 4 * nb)];                                          // w_cross, w_diag
-            sm[rr * stride + c] = v;
+            double2 *s = sm + rr * stride;
+            if (c < nb) {
+                double2 x1 = Xr[r * L + q1 * nb + c], f1 = Yr[r * L + q1 * nb + c];
+                double2 u1 = cscale(x1, fY[q1 * nb + c]);
+                double2 wc = rowc[4 * r + 2], wd = rowc[4 * r + 3];
+                double2 a1 = cmul(wc, u1);
+                double2 a2 = cadd(cmul(wc, f1), cmul(wd, u1));
+                s[c] = make_double2(-a1.x, -a1.y);
+                s[nb + c] = make_double2(-a2.x, -a2.y);
+            } else {
+                int cc = c - nb;
+                double2 x2 = Xr[r * L + q2 * nb + cc], f2 = Yr[r * L + q2 * nb + cc];
+                s[2 * nb + cc] = cconj(f2);
+                s[3 * nb + cc] = cconj(cscale(x2, fY[q2 * nb + cc]));
+            }
         }
         __syncthreads();
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            int e = threadIdx.x + t * blockDim.x;
-            if (e >= nbb) break;
-            int i = e / nb, j = e % nb;
-            double2 a = acc[t];
-            for (int rr = 0; rr < nr; ++rr) {
+        if (active) {
+            for (int rr = ph; rr < nr; rr += nph) {
                 const double2 *s = sm + rr * stride;
-                double2 u1 = s[i], f1 = s[nb + i], u2 = s[2 * nb + j], f2 = s[3 * nb + j];
-                double2 wc = s[4 * nb], wd = s[4 * nb + 1];
-                double2 cross = cadd(cmulc(u1, f2), cmulc(f1, u2));
-                double2 t1 = cmul(wc, cross), t2 = cmul(wd, cmulc(u1, u2));
-                a.x -= t1.x + t2.x;
-                a.y -= t1.y + t2.y;
+                double2 a1 = s[i], a2 = s[nb + i], cf = s[2 * nb + j], cu = s[3 * nb + j];
+                acc = cfma(a1, cf, acc);
+                acc2 = cfma(a2, cu, acc2);
             }
-            acc[t] = a;
         }
     }
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        int e = threadIdx.x + t * blockDim.x;
-        if (e < nbb) dpart[((long)blockIdx.y * n_pairs + p) * nbb + e] = acc[t];
+    acc = cadd(acc, acc2);
+    __syncthreads();
+    if (nph > 1) {
+        if (active) sm[threadIdx.x] = acc;
+        __syncthreads();
+        if (ph == 0 && active) {
+            for (int k = 1; k < nph; ++k) acc = cadd(acc, sm[k * nbb + e]);
+        }
     }
+    if (ph == 0 && active) dpart[((long)blockIdx.y * n_pairs + p) * nbb + e] = acc;
 }
 
 __global__ void k_q_finalize(const double2 *__restrict__ fpart, int nfchunk,
@@ -385,6 +447,10 @@ static int q_build_layout(tdscha_qctx *c, const int *q_pair_map) {
         if (*b) { cudaFree(*b); *b = nullptr; }
     TDS_CUDA(cudaMalloc(&c->alpha, sizeof(double2) * (size_t)n_pairs * nb * nb));
     TDS_CUDA(cudaMalloc(&c->d2v, sizeof(double2) * (size_t)n_pairs * nb * nb));
+    // d2v split over configurations: about four waves of eight blocks per SM
+    // over all pairs (a short last wave), at least 64 image rows per block
+    c->nbchunk = (int)std::max<long>(1, std::min<long>((152L * 8 * 4 + n_pairs - 1) / n_pairs,
+                                                       (c->R + 63) / 64));
     TDS_CUDA(cudaMalloc(&c->dpart, sizeof(double2) * (size_t)c->nbchunk * n_pairs * nb * nb));
     double **bufs[] = {&c->Lq, &c->rk, &c->sk};
     for (double **b : bufs) {
@@ -403,17 +469,19 @@ namespace tdscha {
 static int q_perturb(tdscha_qctx *c, int apply_d4, cudaStream_t st) {
     const int nb = c->nb, L = c->L;
     const long R = c->R;
-    k_q_rows<<<ceil_div(R, 8), 256, 0, st>>>(c->Xr, c->Yr, c->fY, c->fpsi, c->rho, c->R1, c->alpha,
-                                              c->qpair, c->qrole, c->qpartner, c->n_q, nb, c->S,
-                                              R, c->iq_pert, apply_d4, c->rowc);
+    const int rpb = q_rows_per_block(L);
+    k_q_rows<<<ceil_div(R, rpb), 256, 0, st>>>(c->Xr, c->Yr, c->fY, c->fpsi, c->rho, c->R1,
+                                                c->alpha, c->qpair, c->qrole, c->qpartner, c->n_q,
+                                                nb, c->S, R, c->iq_pert, apply_d4, rpb, c->rowc);
     TDS_CHECK_LAUNCH();
     long fchunk = (R + c->nfchunk - 1) / c->nfchunk;
     k_q_favg<<<dim3(nb, c->nfchunk), 256, 0, st>>>(c->Xr, c->Yr, c->fY, c->rowc, L, nb, c->iq_pert,
                                                    R, fchunk, c->fpart);
     TDS_CHECK_LAUNCH();
     long bchunk = (R + c->nbchunk - 1) / c->nbchunk;
-    size_t smem = sizeof(double2) * kQRows * (4 * nb + 2);
-    k_q_d2v<<<dim3(c->n_pairs, c->nbchunk), 256, smem, st>>>(c->Xr, c->Yr, c->fY, c->rowc,
+    const int dthreads = q_d2v_threads(nb);
+    size_t smem = sizeof(double2) * std::max(kQRows * 4 * nb, dthreads);
+    k_q_d2v<<<dim3(c->n_pairs, c->nbchunk), dthreads, smem, st>>>(c->Xr, c->Yr, c->fY, c->rowc,
                                                               c->pair_q, L, nb, R, bchunk,
                                                               c->n_pairs, c->dpart);
     TDS_CHECK_LAUNCH();
@@ -551,7 +619,6 @@ extern "C" int tdscha_qctx_create(tdscha_qctx **out, int n_q, int nb, int N, con
     QCU(cudaMemcpy(c->fpsi, fp.data(), sizeof(double) * L, cudaMemcpyHostToDevice));
     QCU(cudaMemcpy(c->rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice));
     c->nfchunk = (int)std::min<long>(std::max<long>(1, c->R / 1024), 256);
-    c->nbchunk = (int)std::min<long>(std::max<long>(1, c->R / 2048), 64);
     QCU(cudaMalloc(&c->R1, sizeof(double2) * nb));
     QCU(cudaMalloc(&c->f, sizeof(double2) * nb));
     QCU(cudaMalloc(&c->rowc, sizeof(double2) * 4 * (size_t)c->R));

@@ -188,7 +188,7 @@ def make_qspace_ensemble(dims, nb, N, seed=0, T=300.0, w_min_cm=50.0, w_max_cm=5
             z = (rng.standard_normal((N, nb)) + 1j * rng.standard_normal((N, nb))) / np.sqrt(2)
             X_q[iq] = z * sig
             X_q[jq] = np.conj(X_q[iq])
-    u = np.real(np.einsum("qc,qin->icn", np.conj(phase), X_q)) / np.sqrt(n_q)   # (N, cells, nb)
+    u = np.real(np.einsum("qc,qin->icn", np.conj(phase), X_q, optimize=True)) / np.sqrt(n_q)   # (N, cells, nb)
     M = n_q * nb
     ureal = np.ascontiguousarray(np.transpose(u, (0, 2, 1)).reshape(N, M))     # band-major
     Rk = rank if rank is not None else max(8, min(M, 64))
@@ -202,7 +202,7 @@ def make_qspace_ensemble(dims, nb, N, seed=0, T=300.0, w_min_cm=50.0, w_max_cm=5
     rho = np.exp(rng.normal(0.0, rho_sigma, N)) if rho_sigma > 0 else np.ones(N)
     freal -= (rho[:, None] * freal).sum(0) / rho.sum()
     fcell = np.transpose(freal.reshape(N, nb, n_q), (0, 2, 1))                  # (N, cells, nb)
-    Y_q = np.einsum("qc,icn->qin", phase, fcell) / np.sqrt(n_q)
+    Y_q = np.einsum("qc,icn->qin", phase, fcell, optimize=True) / np.sqrt(n_q)
     return dict(X_q=X_q, Y_q=Y_q, w_q=w_q, rho=rho, T=float(T), q=q, dims=tuple(d),
                 X_real=ureal, Y_real=freal, w_real=wreal, n_q=n_q, nb=nb, cells=cells)
 
@@ -223,3 +223,11 @@ def translation_tables(n_q, nb, cells, dims):
     spaces = [np.arange(nu * n_q, (nu + 1) * n_q, dtype=np.intc) for nu in range(nb)]
     bid = np.repeat(np.arange(nb), n_q).astype(np.intc)
     return blocks, spaces, bid
+
+
+# q-space workloads: Gamma-centred grid, bands per q-point, configurations
+QWORKLOADS = {
+    # a 4x4x4 supercell of a 4-atom cell (768 real-space modes), 10 000 configurations
+    "q444_nb12_n10k": dict(dims=(4, 4, 4), nb=12, N=10000, steps=100),
+    "q222_nb6_n2k": dict(dims=(2, 2, 2), nb=6, N=2000, steps=50),
+}
