@@ -178,6 +178,35 @@ int tdscha_perturb_averages_noalloc(int M, int N, const double *X, const double 
                                     double *d2v_out, void *stream);
 
 /*
+ * Static (free-energy Hessian) operator, batched: psi_out[v] = L_static psi_in[v]
+ * for v < nvec, device buffers of nvec x (M + M(M+1)/2) doubles (psi = [R | upper-
+ * triangle rows of W]).  what = 1: harmonic part apply_L1_static(psi, power)
+ * (Modules/DynamicalLanczos.py:2562-2624; power < 0 is its inverse=True form);
+ * 2: anharmonic part apply_anharmonic_static (:3369-3430), R1 = psi_R,
+ * Y1 = -2 Upsilon psi_W Upsilon, output [-f | d2v upper]; 3: both (the matvec of
+ * run_hessian_calculation, :4129-4138, and StaticHessian.apply_L,
+ * Modules/StaticHessian.py:561-620).  Asynchronous on stream; ignore_v4 from
+ * tdscha_ctx_set_options selects apply_d4.
+ */
+int tdscha_static_L(tdscha_ctx *ctx, int nvec, const double *psi_in, double *psi_out, int what,
+                    double power, int precision, void *stream);
+
+/*
+ * StaticHessian vector <-> batch of M static psi rows (StaticHessian.apply_L,
+ * Modules/StaticHessian.py:561-691): vec = [G upper-triangle rows (M(M+1)/2) |
+ * W_ijk for i <= j <= k (M(M+1)(M+2)/6)], X / Y = M rows of M + M(M+1)/2
+ * doubles, row i = [G_i | upper-triangle rows of W_i].  expand fills every
+ * row from the symmetric G and W; collect writes G_ij (j >= i) from Y[i][j] and
+ * W_ijk (i <= j <= k) from row i.  Device buffers, asynchronous on stream.
+ */
+int tdscha_static_hessian_expand(tdscha_ctx *ctx, const double *vec, double *X, void *stream);
+int tdscha_static_hessian_collect(tdscha_ctx *ctx, const double *Y, double *vec, void *stream);
+
+/* Synchronise stream and report asynchronous failures (CUDA errors, an expired
+ * bounded wait of the tensor-core path). */
+int tdscha_ctx_sync(tdscha_ctx *ctx, void *stream);
+
+/*
  * q-space (Bloch basis) operator, float64 complex, Wigner only
  * (QSpaceLanczos, Modules/QSpaceLanczos.py; perturbation averages
  * get_perturb_averages_qspace_fused, Modules/tdscha_qspace.jl:455-712).

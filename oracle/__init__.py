@@ -429,3 +429,121 @@ def continued_fraction(a_coeffs, b_coeffs, c_coeffs, w_array, use_wigner, modulu
     if not use_wigner:
         return gf * modulus
     return (-np.real(gf) + 1j * np.imag(gf)) * modulus
+
+
+# --- static response (free-energy Hessian) ----------------------------------
+def static_lambda(w, T):
+    """Pair factor Lambda of apply_L1_static (DynamicalLanczos.py:2588-2622), one
+    value per upper-triangle pair (row i, column j): w_a = w[j], w_b = w[i];
+    both population masks from w_a (:2603-2604); on w_a == w_b the derivative
+    term multiplies n_equal^2, read before the occupations are set (:2608-2619)."""
+    M = len(w)
+    iu_r, iu_c = np.triu_indices(M)
+    wa, wb = w[iu_c], w[iu_r]
+    na = np.zeros_like(wa)
+    nb = np.zeros_like(wa)
+    unpop = 0.01 * wa * RY_TO_K > T
+    equal = np.abs(wa - wb) < 1e-8
+    diff = np.zeros_like(wa)
+    if T > 0:
+        beta = RY_TO_K / T
+        na = 1 / (np.exp(wa * beta) - 1)
+        nb = 1 / (np.exp(wb * beta) - 1)
+        na[unpop] = 0
+        nb[unpop] = 0
+        with np.errstate(divide="ignore", invalid="ignore"):
+            diff = (na - nb) / (wa - wb)
+        diff[equal] = -beta * np.exp(wa[equal] * beta) * 0.0
+    lam = (na + nb + 1) / (wa + wb) - diff
+    return lam / (4 * wa * wb)
+
+
+def static_L1(w, T, psi, inverse=False, power=1):
+    """apply_L1_static (DynamicalLanczos.py:2562-2624)."""
+    M = len(w)
+    if inverse:
+        power = -power
+    out = np.zeros(len(psi))
+    out[:M] = psi[:M] * w ** (2 * power)
+    out[M:] = psi[M:] / static_lambda(w, T) ** power
+    return out
+
+
+def upsilon(w, T):
+    n = np.zeros_like(w) if T <= 1e-12 else 1.0 / (np.exp(w * RY_TO_K / T) - 1.0)
+    return 2 * w / (2 * n + 1)
+
+
+def static_anharmonic(ol, psi):
+    """apply_anharmonic_static (DynamicalLanczos.py:3369-3430) on an OracleLanczos:
+    R1 = psi_R, Y1 = -2 Upsilon psi_W Upsilon, output [-f | d2v upper rows]."""
+    M = ol.n_modes
+    Y1 = ol._sym_from_triangle(psi[M:])
+    Yw = upsilon(ol.w, ol.T)
+    Y1 = -2 * np.einsum("ab, a, b -> ab", Y1, Yw, Yw)
+    f, d2v = ol.perturb(np.ascontiguousarray(psi[:M]), np.ascontiguousarray(Y1))
+    out = np.zeros(len(psi))
+    out[:M] = -f
+    out[M:] = d2v[ol.iu_row, ol.iu_col]
+    return out
+
+
+def minimum_residual(apply_A, b, x0, max_iters=100, conv_thr=1e-6):
+    """The minimal-residual iteration of Tools.minimum_residual_algorithm
+    (Modules/Tools.py:265-414) without preconditioner; returns (x, iterations,
+    converged)."""
+    r1 = b - apply_A(x0)
+    b_norm = np.sqrt(b.dot(b))
+    r1_bar = apply_A(r1)
+    z1 = r1.copy()
+    p1 = r1.copy()
+    p1_bar = r1_bar.copy()
+    x = x0.copy()
+    iters, converged = 1, False
+    while iters < max_iters and not converged:
+        Ap = p1_bar
+        Ap_bar = apply_A(p1_bar)
+        alpha = r1_bar.dot(z1) / p1_bar.dot(Ap)
+        x = x + alpha * p1
+        r = r1 - alpha * Ap
+        rbar = r1_bar - alpha * Ap_bar
+        r_norm = np.sqrt(r.dot(r)) / b_norm
+        beta = rbar.dot(r) / r1_bar.dot(z1)
+        p1 = r + beta * p1
+        p1_bar = rbar + beta * p1_bar
+        r1, r1_bar, z1 = r, rbar, r
+        converged = r_norm < conv_thr
+        iters += 1
+    return x, iters, converged
+
+
+def run_hessian_calculation(ol, eigen_shift=1.0, max_iters=1000, use_preconditioning=True):
+    """Lanczos.run_hessian_calculation with the 'cg' algorithm
+    (DynamicalLanczos.py:4054-4330): one minimal-residual solve per unit vector,
+    G_ij = x_i[j], returns inv((G + G^T) / 2)."""
+    M = ol.n_modes
+    Ps = M + M * (M + 1) // 2
+
+    def L(psi):
+        p = psi.copy()
+        p[M:] *= eigen_shift
+        ret = static_L1(ol.w, ol.T, p) + static_anharmonic(ol, p)
+        ret[M:] *= eigen_shift
+        return ret
+
+    def P(x):
+        return static_L1(ol.w, ol.T, x, inverse=True, power=0.5)
+
+    G = np.zeros((M, M))
+    for i in range(M):
+        b = np.zeros(Ps)
+        b[i] = 1
+        if use_preconditioning:
+            bt = P(b)
+            xt, _, _ = minimum_residual(lambda x: P(L(P(x))), bt, bt.copy(), max_iters)
+            res = P(xt)
+        else:
+            res, _, _ = minimum_residual(L, b, b.copy(), max_iters)
+        G[i, :] = res[:M]
+    G = 0.5 * (G + G.T)
+    return np.linalg.inv(G)

@@ -405,6 +405,146 @@ class Lanczos(object):
         self.psi = out
         return self.psi
 
+    # ------------------------------------------------------- static response
+    def _static_size(self):
+        return self.n_modes + (self.n_modes * (self.n_modes + 1)) // 2
+
+    def _static_dev(self, X, what, power=1.0):
+        """Batched static operator on a (k, M + M(M+1)/2) float64 device tensor."""
+        torch = _torch()
+        ctx = self._context()
+        X = X.contiguous()
+        Y = torch.empty_like(X)
+        st = torch.cuda.current_stream().cuda_stream
+        nat.check(nat.load().tdscha_static_L(ctx.handle, X.shape[0], X.data_ptr(), Y.data_ptr(),
+                                             what, float(power), self._prec(), st))
+        return Y
+
+    def _static_host(self, psi, what, power=1.0):
+        torch = _torch()
+        expected_dim = self._static_size()
+        psi = np.asarray(psi, dtype=np.float64)
+        if psi.ndim != 1 or len(psi) != expected_dim:
+            raise AssertionError("\nError, for the static calculation the vector must be of "
+                                 "dimension {}, got {}\n".format(expected_dim, len(psi)))
+        X = torch.from_numpy(np.ascontiguousarray(psi)).cuda()[None, :]
+        Y = self._static_dev(X, what, power)
+        nat.check(nat.load().tdscha_ctx_sync(self._ctx.handle,
+                                             torch.cuda.current_stream().cuda_stream))
+        return Y[0].cpu().numpy()
+
+    def apply_L1_static(self, psi, inverse=False, power=1):
+        """Harmonic part of the static operator (:2562-2624): psi_R w^(2p) and
+        psi_W / Lambda^p, p = -power when inverse."""
+        if inverse:
+            power = -power
+        return self._static_host(psi, 1, power)
+
+    def apply_anharmonic_static(self):
+        """Anharmonic part of the static operator on self.psi (:3369-3430):
+        R1 = psi_R, Y1 = -2 Upsilon psi_W Upsilon, output [-f | d2v upper rows]."""
+        return self._static_host(self.psi, 2)
+
+    def run_hessian_calculation(self, verbose=True, eigen_shift=1, tol=5e-4, max_iters=1000,
+                                save_g=None, save_each=1, use_preconditioning=True,
+                                algorithm="cg"):
+        """Free-energy Hessian from the static response (:4054-4330).
+
+        One minimal-residual solve per mode as in the reference (threshold 1e-6
+        of Tools.minimum_residual_algorithm; `tol` is unused there too), all
+        n_modes solves advanced together on the GPU (each system keeps its own
+        scalars and stops at its own convergence).  Returns the mass-rescaled
+        Hessian inv((G + G^T)/2)."""
+        from . import Tools
+        torch = _torch()
+        if not self.initialized:
+            self.prepare_symmetrization()
+        M = self.n_modes
+        Ps = self._static_size()
+        self.psi = np.zeros(Ps, dtype=TYPE_DP)
+        dev = torch.device("cuda")
+        if algorithm.lower() != "cg":
+            if algorithm.lower() not in ("minimize", "minimize-quad"):
+                raise ValueError("\nError, algorithm type '{}' in subroutine run_biconjugate_gradient "
+                                 "not implemented.\n       the only supported algorithms are "
+                                 "['bicgstab', 'bicg']\n".format(algorithm))
+            return self._run_hessian_minimize(eigen_shift, tol, max_iters, save_g, algorithm,
+                                              verbose)
+
+        def L(X):
+            Xs = X.clone()
+            Xs[:, M:] *= eigen_shift
+            Y = self._static_dev(Xs, 3)
+            Y[:, M:] *= eigen_shift
+            return Y
+
+        def Ph(X):
+            return self._static_dev(X, 1, -0.5)
+
+        B = torch.zeros((M, Ps), dtype=torch.float64, device=dev)
+        B[torch.arange(M), torch.arange(M)] = 1.0
+        t1 = time.time()
+        if use_preconditioning:
+            Bt = Ph(B)
+            Xt, iters, conv = Tools.batched_minimum_residual(lambda Z: Ph(L(Ph(Z))), Bt,
+                                                             Bt.clone(), max_iters, 1e-6,
+                                                             verbose=verbose)
+            res = Ph(Xt)
+        else:
+            res, iters, conv = Tools.batched_minimum_residual(L, B, B.clone(), max_iters, 1e-6,
+                                                              verbose=verbose)
+        nat.check(nat.load().tdscha_ctx_sync(self._ctx.handle,
+                                             torch.cuda.current_stream().cuda_stream))
+        G_one_phonon = res[:, :M].cpu().numpy()
+        if verbose:
+            print("Static response: %d systems, %d-%d iterations, %.3f s"
+                  % (M, iters.min(), iters.max(), time.time() - t1))
+        for i in np.where(~conv)[0]:
+            print("WARNING: cg did not converge after {} iterations.".format(max_iters))
+        if save_g is not None:
+            np.save(save_g, G_one_phonon)
+        disp = np.max(np.abs(G_one_phonon - G_one_phonon.T))
+        assert disp < 1e-4, "Error, the resulting one-phonon Green function is not Hermitian."
+        G = 0.5 * (G_one_phonon + G_one_phonon.T)
+        return np.linalg.inv(G)
+
+    def _run_hessian_minimize(self, eigen_shift, tol, max_iters, save_g, algorithm, verbose):
+        """The scipy BFGS variants of run_hessian_calculation (:4191-4265), with
+        the static operator on the GPU."""
+        import scipy.optimize
+        M = self.n_modes
+        Ps = self._static_size()
+
+        def L(x):
+            p = np.array(x, dtype=np.float64)
+            p[M:] *= eigen_shift
+            ret = self._static_host(p, 3)
+            ret[M:] *= eigen_shift
+            return ret
+
+        def func_quad(x, b):
+            r = L(x) - b
+            return 0.5 * np.sum(r ** 2), L(r)
+
+        def func_standard(x, b):
+            Lx = L(x)
+            return 0.5 * x.dot(Lx) - b.dot(x), Lx - b
+
+        G = np.zeros((M, M))
+        options = {"gtol": tol, "maxiter": max_iters, "disp": verbose, "norm": 2}
+        fun = func_quad if algorithm.lower() == "minimize-quad" else func_standard
+        for i in range(M):
+            b = np.zeros(Ps)
+            b[i] = 1
+            res = scipy.optimize.minimize(fun, b.copy(), args=(b,), method="bfgs", jac=True,
+                                          options=options)
+            G[i, :] = res.x[:M]
+            if save_g is not None:
+                np.save(save_g, G)
+        disp = np.max(np.abs(G - G.T))
+        assert disp < 1e-4, "Error, the resulting one-phonon Green function is not Hermitian."
+        return np.linalg.inv(0.5 * (G + G.T))
+
     def get_perturb_averages(self, R1, Y1, apply_d4=True):
         """(f_pert_av, d2v_pert_av) of the resident ensemble (GetPerturbAverageSym)."""
         ctx = self._context()

@@ -24,6 +24,8 @@ EXPORTS = [
     "tdscha_perturb_averages_noalloc",
     "tdscha_qctx_create", "tdscha_qctx_destroy", "tdscha_qctx_set_pert",
     "tdscha_qperturb_averages", "tdscha_qapply_full_L", "tdscha_qlanczos_run",
+    "tdscha_static_L", "tdscha_ctx_sync", "tdscha_static_hessian_expand",
+    "tdscha_static_hessian_collect",
 ]
 
 
@@ -81,6 +83,10 @@ def load():
     lib.tdscha_qapply_full_L.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_qlanczos_run.argtypes = [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _d, _i,
                                         _i, _vp]
+    lib.tdscha_static_L.argtypes = [_vp, _c_int, _vp, _vp, _c_int, _c_double, _c_int, _vp]
+    lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
+    lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
+    lib.tdscha_static_hessian_collect.argtypes = [_vp, _vp, _vp, _vp]
     for name in EXPORTS:
         fn = getattr(lib, name)
         if name not in ("tdscha_last_error", "tdscha_version"):

@@ -86,6 +86,7 @@ struct tdscha_ctx {
     double *Yw = nullptr, *ReAw = nullptr;     // equilibrium Upsilon / ReA eigenvalues
     double *Ywinv = nullptr;                    // 1 / Yw
     int *tri = nullptr;                         // (row, column) of each upper-triangle pair
+    double *lam_static = nullptr;               // static pair factor Lambda (H), on first use
     // image rows (device), R x M
     double *D = nullptr, *F = nullptr;
     // per-pair coefficients (device), length H, rebuilt by set_options

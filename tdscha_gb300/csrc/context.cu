@@ -89,6 +89,7 @@ static void ctx_free(tdscha_ctx *c) {
     for (double *p : bufs)
         if (p) cudaFree(p);
     if (c->tri) cudaFree(c->tri);
+    if (c->lam_static) cudaFree(c->lam_static);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
     if (c->stat_host) cudaFreeHost(c->stat_host);
     delete c;
@@ -376,4 +377,12 @@ extern "C" int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *t
     *total_ms = tot;
     *launches = (int)ctx->prof_ev[kernel_id].size();
     return TDSCHA_OK;
+}
+
+extern "C" int tdscha_ctx_sync(tdscha_ctx *ctx, void *stream) {
+    set_error("");
+    if (!ctx) { set_error("ctx_sync: null context"); return TDSCHA_ERR_ARG; }
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) { set_error("ctx_sync: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
+    return mixed_check_error(ctx);
 }

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, HERE)
 
-from ref_harness import load_reference, make_reference_lanczos  # noqa: E402
+from ref_harness import load_reference, make_reference_lanczos, static_adapter  # noqa: E402
 from tdscha_gb300.synthetic import (make_ensemble, random_R1, random_sym,  # noqa: E402
                                     RY_TO_CM)
 
@@ -115,6 +115,52 @@ def run_case(fname, M, N, S, sig, seed, n_steps, variants):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def static_case(fname, M, N, seed, sh_steps):
+    """The reference's static response (apply_L1_static, apply_anharmonic_static,
+    run_hessian_calculation, StaticHessian.run) through static_adapter."""
+    import importlib
+    load_reference()
+    SH = importlib.import_module("tdscha.StaticHessian")
+    # frequencies of 0.36-1 Ry keep the static susceptibility O(1): the
+    # reference asserts |G - G^T| < 1e-4 in absolute terms (:4319-4320), which
+    # meV-scale modes (G ~ 1/w^2 ~ 1e5) cannot meet at its 1e-6 solver threshold
+    ens = make_ensemble(M, N, seed=seed, n_syms=1, rho_sigma=0.1, w_min_cm=40000.0,
+                        w_max_cm=110000.0)
+    lanc = make_reference_lanczos(ens, use_wigner=True)
+    Ps = M + M * (M + 1) // 2
+    rng = np.random.default_rng(seed + 3)
+    psi = rng.standard_normal(Ps)
+    psi[:M] *= 10
+    out = dict(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"], psi_s=psi)
+    with static_adapter(lanc), contextlib.redirect_stdout(io.StringIO()):
+        out["L1"] = lanc.apply_L1_static(psi.copy())
+        out["L1_inv_half"] = lanc.apply_L1_static(psi.copy(), inverse=True, power=0.5)
+        lanc.psi = psi.copy()
+        out["anh"] = lanc.apply_anharmonic_static().copy()
+        lanc.ignore_v4 = True
+        lanc.psi = psi.copy()
+        out["anh_nod4"] = lanc.apply_anharmonic_static().copy()
+        lanc.ignore_v4 = False
+        out["hessian"] = lanc.run_hessian_calculation(verbose=False)
+        out["hessian_noprec"] = lanc.run_hessian_calculation(verbose=False,
+                                                             use_preconditioning=False)
+        sh = SH.StaticHessian()
+        sh.lanczos = lanc
+        n_g = M * (M + 1) // 2
+        n_w = M * (M * M + 3 * M + 2) // 6
+        v0 = np.zeros(n_g + n_w)
+        counter = 0
+        for i in range(M):           # the preconditioned initial guess of StaticHessian.init
+            v0[counter] = 1 / ens["w"][i]
+            counter += M - i
+        sh.vector = v0.copy()
+        sh.run(sh_steps, threshold=1e-8, algorithm="cg-prec")
+        out["sh_vector"] = sh.vector.copy()
+        out["sh_hessian"] = sh.retrieve_hessian(noq=True)
+        out["sh_steps"] = sh_steps
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -124,6 +170,7 @@ def main():
     # moves the coefficients by O(1).
     run_case("runft_m12_n120_s48.npz", 12, 120, 48, 0.1, 31, 12,
              [("bilanczos", False, True), ("wigner", True, True)])
+    static_case("static_m12_n800.npz", 12, 800, 41, 25)
     print("fixtures written to", HERE)
 
 

@@ -10,6 +10,7 @@ C kernels, CModules/odd_corr_module.c). The stubs below provide only the
 names the Lanczos driver touches on the perturbation-average path; the
 C module is the reference's own, compiled from source by oracle/build_ref.sh.
 """
+import contextlib
 import importlib
 import os
 import sys
@@ -67,7 +68,8 @@ def load_reference():
     cc.Methods = _stub("cellconstructor.Methods")
     sscha = _stub("sscha")
     sscha.Ensemble = _stub("sscha.Ensemble", Bohr=1.889725989)
-    sscha.Parallel = _stub("sscha.Parallel", pprint=lambda *a, **k: None)
+    sscha.Parallel = _stub("sscha.Parallel", pprint=lambda *a, **k: None,
+                           am_i_the_master=lambda: True)
     _stub("spglib")
 
     pkg = types.ModuleType("tdscha")
@@ -124,3 +126,43 @@ def make_reference_lanczos(ens, use_wigner, mode=1):
         shape=(len(lanc.psi), len(lanc.psi)),
         matvec=lanc.apply_full_L, rmatvec=L_transp, dtype=np.double)
     return lanc
+
+
+@contextlib.contextmanager
+def static_adapter(lanc):
+    """Route the reference's static-response call to its own C module.
+
+    apply_anharmonic_static (Modules/DynamicalLanczos.py:3369-3430) still passes
+    the 13-argument form (..., T, apply_d4, symmetries, N_degeneracy,
+    deg_space, f, d2v) while GetPerturbAverageSym parses 15 arguments
+    (CModules/odd_corr_module.c:519-521: ..., T, apply_D4, N_syms, symmetries,
+    n_deg, degenerate_space, blocks_ids, f, d2v), so the reference's static path
+    raises TypeError as shipped.  Inside this context (fixture generation only)
+    13-argument calls are forwarded with the lanczos object's block tables and
+    15-argument calls pass through, so the rest of the reference's static path
+    -- apply_L1_static, the Y1 scaling, the output repack,
+    Tools.minimum_residual_algorithm, run_hessian_calculation and StaticHessian
+    -- runs unchanged.  Valid for one-mode blocks (identity symmetries), the
+    only layout whose deg_space loop (:3398-3409) works."""
+    import sscha_HP_odd as real
+    DL = load_reference()
+
+    class _Adapter:
+        @staticmethod
+        def GetPerturbAverageSym(*args):
+            if len(args) == 15:
+                return real.GetPerturbAverageSym(*args)
+            X, Y, w, rho, R1, Y1, T, apply_d4, symmetries, n_deg, deg_space, f, d2v = args
+            return real.GetPerturbAverageSym(X, Y, w, rho, R1, Y1, T, apply_d4,
+                                             int(symmetries[0].shape[0]), symmetries, n_deg,
+                                             lanc.degenerate_space, lanc.sym_block_id, f, d2v)
+
+    mods = [DL] + [m for n, m in sys.modules.items() if n == "tdscha.StaticHessian"]
+    saved = [m.sscha_HP_odd for m in mods]
+    for m in mods:
+        m.sscha_HP_odd = _Adapter
+    try:
+        yield DL
+    finally:
+        for m, v in zip(mods, saved):
+            m.sscha_HP_odd = v
