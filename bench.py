@@ -314,6 +314,9 @@ def run_ours(args):
         nat.check(lib.tdscha_ctx_profile_read(ctx.handle, kid, ctypes.byref(tot), ctypes.byref(cnt)))
         if cnt.value:
             kern[kid] = (tot.value, cnt.value)
+    static = None
+    if not args.no_rows and prec_name == "mixed":
+        static = static_leg(lib, nat, ctx, M, spec["n_syms"] * N, dev)
     ctx.close()
     apps = 2 * K
     R = N * spec["n_syms"]
@@ -378,6 +381,8 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(ens, 15.0, 2)
     rows = {}
+    if static is not None:
+        rows["static"] = static
     if not args.no_rows:
         rows["qspace"] = qspace_leg(args.qworkload, K, W, dev, peaks, with_cpu=not args.no_cpu)
     if rank == 0:
@@ -492,6 +497,35 @@ def fp64_arm_and_check(args, ens, spec, syms, spaces, bid, dev, local):
     return out, check
 
 
+def static_leg(lib, nat, ctx, M, R, dev):
+    """Static (Hessian) operator L1_static + anharmonic_static through
+    tdscha_static_L: one StaticHessian / run_hessian_calculation matvec is M
+    such applications.  Device time per application, mixed and float64."""
+    import torch
+    Ps = M + M * (M + 1) // 2
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    g = torch.Generator(device=dev).manual_seed(5)
+    out = {"what": "static operator (harmonic + anharmonic), batched rows of M + M(M+1)/2"}
+    for name, prec, nvec in (("mixed", nat.PREC_MIXED, min(M, 96)), ("fp64", nat.PREC_FP64, 2)):
+        X = torch.randn((nvec, Ps), dtype=torch.float64, device=dev, generator=g)
+        Y = torch.empty_like(X)
+        nat.check(lib.tdscha_static_L(ctx.handle, 1, X.data_ptr(), Y.data_ptr(), 3, 1.0, prec, st))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        nat.check(lib.tdscha_static_L(ctx.handle, nvec, X.data_ptr(), Y.data_ptr(), 3, 1.0, prec,
+                                      st))
+        e1.record(stream)
+        nat.check(lib.tdscha_ctx_sync(ctx.handle, st))
+        ms = e0.elapsed_time(e1) / nvec
+        out[name] = {"ms_per_application": ms, "applications_per_s": 1e3 / ms,
+                     "rows_timed": nvec, "matvec_s_at_M_rows": ms * M / 1e3,
+                     "achieved_tflops": 4.0 * R * M * M / (ms / 1e3) / 1e12}
+    return out
+
+
 def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):
     """q-space (Bloch basis) operator and Hermitian Lanczos, float64 complex:
     steps/s through QSpaceLanczos.run_FT, per-application device time of
@@ -553,6 +587,21 @@ def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):
                           "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
                           "flops_per_application": flops},
              "ensemble_bytes": 2 * e["X_q"].nbytes}
+    # kernel polynomial method on the same operator: two moments per application
+    from tdscha_gb300.QSpaceKPM import QSpaceKPM
+    kpm = QSpaceKPM.from_qspace_lanczos(lz)
+    kpm.prepare_mode_q(0, nb // 2)
+    kpm.run_KPM(8, verbose=False)
+    kpm.reset_q()
+    kpm.prepare_mode_q(0, nb // 2)
+    n_mom = 2 * K + 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    kpm.run_KPM(n_mom, verbose=False)
+    torch.cuda.synchronize()
+    out_d["kpm"] = {"moments": n_mom, "moments_per_s": n_mom / (time.perf_counter() - t0),
+                    "timer": "host wall clock around QSpaceKPM.run_KPM (one read-back)"}
+    kpm._invalidate()
     if with_cpu:
         import oracle.qspace as oq
         ns = min(N, 400)

@@ -265,6 +265,21 @@ int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int 
                         int start_step, int n_iter, int reorthogonalize, double *hist,
                         int *steps_done, int *converged, void *stream);
 
+/*
+ * Chebyshev moments of the q-space operator (QSpaceKPM.run_KPM,
+ * Modules/QSpaceKPM.py:260-454, main loop :413-440): for k = n_start, ... while
+ * 2k < n_moments: moments[2k] = 2 <v, v>_M - moments[0]; then
+ * vp = 2 (L v - b v)/a - vm, moments[2k+1] = 2 <vp, v>_M - moments[1] and
+ * (vm, v) <- (v, vp).  vm, v, work: distinct device buffers of 2 psi_size
+ * doubles (T_{k-1}, T_k applied to the start vector); moments: device, with
+ * moments[0], moments[1] set.  On return the final (vm, v) pair is in (vm, v)
+ * when *swapped == 0, in (v, vm) otherwise.  <x, y>_M is the Wigner metric
+ * Re(x^H (mask y)).
+ */
+int tdscha_qkpm_run(tdscha_qctx *ctx, double *vm, double *v, double *work, int n_start,
+                    int n_moments, double rescale_a, double rescale_b, double *moments,
+                    int *swapped, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

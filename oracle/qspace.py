@@ -309,3 +309,103 @@ def q_pair_map_grid(q_crys, iq_pert, tol=1e-6):
             raise ValueError("no partner for q-point %d" % i)
         out[i] = j[0]
     return out
+
+
+# --- kernel polynomial method (Modules/QSpaceKPM.py) -------------------------
+def kpm_bounds(w_q, valid, bound_factor=1.2, edge_buffer=1e-8, use_wigner=True):
+    """_get_kpm_bounds without explicit bounds (QSpaceKPM.py:156-176)."""
+    max_w = np.max(np.abs(np.asarray(w_q)[np.asarray(valid, dtype=bool)]))
+    width = (2 * max_w) ** 2
+    margin = (bound_factor - 1) * width
+    lmin, lmax = (-width - margin, margin) if use_wigner else (-margin, width + margin)
+    span = lmax - lmin
+    return lmin - edge_buffer * span, lmax + edge_buffer * span
+
+
+def kpm_moments(apply_L, psi, mask, n_moments, lmin, lmax):
+    """run_KPM's fresh path (QSpaceKPM.py:377-440): returns (moments, norm, vm, v)."""
+    dot = lambda x, y: np.real(np.conj(x).dot(y * mask))
+    a = 0.5 * (lmax - lmin)
+    b = 0.5 * (lmax + lmin)
+    resc = lambda v: (apply_L(v) - b * v) / a
+    norm = np.sqrt(dot(psi, psi))
+    v0 = psi / norm
+    mom = np.zeros(n_moments)
+    mom[0] = 1.0
+    vm, v = v0, v0
+    if n_moments > 1:
+        v1 = resc(v0)
+        mom[1] = dot(v0, v1)
+        vm, v = v0, v1
+        n = 1
+        while 2 * n < n_moments:
+            mom[2 * n] = 2 * dot(v, v) - mom[0]
+            if 2 * n + 1 >= n_moments:
+                break
+            vp = 2 * resc(v) - vm
+            mom[2 * n + 1] = 2 * dot(vp, v) - mom[1]
+            vm, v = v, vp
+            n += 1
+    return mom, norm, vm, v
+
+
+def jackson_kernel(n_moments):
+    """QSpaceKPM._jackson_kernel (:516-519)."""
+    n = np.arange(n_moments, dtype=np.float64)
+    phi = np.pi / (n_moments + 1)
+    return ((n_moments - n + 1) * np.cos(n * phi) + np.sin(n * phi) / np.tan(phi)) / (n_moments + 1)
+
+
+def kpm_spectral(w_array, moments, norm, lmin, lmax, g=None, use_wigner=True):
+    """get_spectral_function_KPM (QSpaceKPM.py:536-559)."""
+    n_m = len(moments)
+    g = jackson_kernel(n_m) if g is None else g
+    a = 0.5 * (lmax - lmin)
+    b = 0.5 * (lmax + lmin)
+    w = np.asarray(w_array, dtype=np.float64)
+    lam = -(w ** 2) if use_wigner else w ** 2
+    x = (lam - b) / a
+    inside = np.abs(x) < 1
+    out = np.zeros_like(w)
+    if not np.any(inside):
+        return out
+    xin = np.clip(x[inside], -1 + 1e-15, 1 - 1e-15)
+    t0 = np.ones_like(xin)
+    rho = g[0] * moments[0] * t0
+    if n_m > 1:
+        t1 = xin.copy()
+        rho += 2 * g[1] * moments[1] * t1
+        for i in range(2, n_m):
+            t2 = 2 * xin * t1 - t0
+            rho += 2 * g[i] * moments[i] * t2
+            t0, t1 = t1, t2
+    rho /= np.pi * a * np.sqrt(1 - xin ** 2)
+    rho *= norm ** 2
+    out[inside] = np.pi * rho
+    return out
+
+
+def moments_from_tridiagonal(a_c, b_c, c_c, n_moments, lmin, lmax):
+    """Chebyshev moments e0^T T_n((T - b)/a) e0 of the Lanczos tridiagonal
+    (diagonal a_k, T[k+1,k] = b_k, T[k,k+1] = c_k): equal to the KPM moments of
+    the start vector for n < 2 (number of steps) + 1 in exact arithmetic."""
+    k = len(a_c)
+    T = np.diag(np.asarray(a_c, dtype=np.float64))
+    for i in range(k - 1):
+        T[i + 1, i] = b_c[i]
+        T[i, i + 1] = c_c[i]
+    a = 0.5 * (lmax - lmin)
+    b = 0.5 * (lmax + lmin)
+    Ts = (T - b * np.eye(k)) / a
+    e0 = np.zeros(k)
+    e0[0] = 1
+    mom = np.zeros(n_moments)
+    t_prev, t_cur = e0, Ts @ e0
+    mom[0] = 1.0
+    if n_moments > 1:
+        mom[1] = t_cur[0]
+    for n in range(2, n_moments):
+        t_next = 2 * Ts @ t_cur - t_prev
+        mom[n] = t_next[0]
+        t_prev, t_cur = t_cur, t_next
+    return mom

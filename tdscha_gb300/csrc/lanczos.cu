@@ -452,6 +452,22 @@ __global__ void k_qrenorm(const double *__restrict__ part, int nblk, double *__r
     }
 }
 
+// Kernel polynomial method (QSpaceKPM.run_KPM, Modules/QSpaceKPM.py:260-454):
+// vp = 2 (L v - b v) / a - vm written over vm, and the moment finishers
+// moments[idx] = 2 <x, y>_M - moments[ref].
+__global__ void k_kpm_combine(const double *__restrict__ Lv, const double *__restrict__ v,
+                              double *__restrict__ vm, double a, double b, long n) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        vm[e] = 2 * ((Lv[e] - b * v[e]) / a) - vm[e];
+}
+
+__global__ void k_kpm_moment(const double *__restrict__ part, int nblk, double *__restrict__ moments,
+                             int idx, int ref) {
+    __shared__ double sh[32];
+    double s = reduce_parts(part, nblk, sh);
+    if (threadIdx.x == 0) moments[idx] = 2 * s - moments[ref];
+}
+
 // Copies hist rows / status of steps next..k back to the host and applies the
 // stop conditions; returns TDSCHA_OK or an error and sets *stop.
 static int read_back_steps(double *hist_dev, double *stat_dev, double *stat_host, int capacity,
@@ -816,4 +832,38 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
         next = k + 1;
     }
     return rc;
+}
+
+extern "C" int tdscha_qkpm_run(tdscha_qctx *ctx, double *vm, double *v, double *work, int n_start,
+                               int n_moments, double rescale_a, double rescale_b, double *moments,
+                               int *swapped, void *stream) {
+    set_error("");
+    if (!ctx || !vm || !v || !work || !moments || !swapped) { set_error("qkpm_run: null pointer"); return TDSCHA_ERR_ARG; }
+    if (ctx->n_pairs == 0) { set_error("qkpm_run: call tdscha_qctx_set_pert first"); return TDSCHA_ERR_STATE; }
+    if (n_start < 1 || n_moments < 2 || !(rescale_a != 0) || !std::isfinite(rescale_a) || !std::isfinite(rescale_b)) {
+        set_error("qkpm_run: bad arguments (n_start %d, n_moments %d, a %g)", n_start, n_moments, rescale_a);
+        return TDSCHA_ERR_ARG;
+    }
+    if (vm == v || vm == work || v == work) { set_error("qkpm_run: buffers must be distinct"); return TDSCHA_ERR_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    const long n = 2 * ctx->P;
+    const int nb = std::max(1, std::min(ceil_div(n, kDotThreads), 296));
+    double *a = vm, *b = v;
+    *swapped = 0;
+    for (int k = n_start; 2 * k < n_moments; ++k) {
+        k_dot1<<<nb, kDotThreads, 0, st>>>(b, b, ctx->mask, n, ctx->dots);
+        k_kpm_moment<<<1, 256, 0, st>>>(ctx->dots, nb, moments, 2 * k, 0);
+        if (2 * k + 1 >= n_moments) break;
+        TDS_TRY(q_apply_full_L_dev(ctx, b, work, st));
+        k_kpm_combine<<<nb, kDotThreads, 0, st>>>(work, b, a, rescale_a, rescale_b, n);
+        k_dot1<<<nb, kDotThreads, 0, st>>>(a, b, ctx->mask, n, ctx->dots);
+        k_kpm_moment<<<1, 256, 0, st>>>(ctx->dots, nb, moments, 2 * k + 1, 1);
+        TDS_CHECK_LAUNCH();
+        double *t = a;   // (vm, v) <- (v, vp)
+        a = b;
+        b = t;
+        *swapped ^= 1;
+    }
+    TDS_CHECK_LAUNCH();
+    return TDSCHA_OK;
 }
