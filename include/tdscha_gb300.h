@@ -127,6 +127,16 @@ int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int ca
                        void *stream);
 
 /*
+ * tdscha_lanczos_run with host-memory basis arrays (capacity x P doubles each):
+ * rows 0 .. start_step are uploaded, the new rows are copied back; device
+ * buffers are allocated and freed inside the call.  For host programs without
+ * a CUDA runtime of their own (the input-file executable).  Synchronous.
+ */
+int tdscha_lanczos_run_hostbuf(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                               int start_step, int n_iter, int run_simm, int precision,
+                               int full_reorth, double *hist, int *steps_done, int *converged);
+
+/*
  * Continued-fraction Green function on the GPU, one thread per frequency
  * (get_green_function_continued_fraction, Modules/DynamicalLanczos.py:
  * 5032-5162).  a[n], b[n_b], c[n_c] host arrays; c is used when n_c == n_b,

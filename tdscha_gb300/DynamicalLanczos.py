@@ -712,6 +712,100 @@ class Lanczos(object):
             float(smearing), int(smooth_ramp), nat.dp(out)))
         return (out[0::2] + 1j * out[1::2]).reshape(w_array.shape)
 
+    # ------------------------------------------- input files of the executable
+    def prepare_input_files(self, root_name="tdscha", n_steps=100, start_from_scratch=True,
+                            directory=".", run_symm=False):
+        """Write the input of the input-file Lanczos program (:873-975): the same
+        files and formats as the reference, read by tdscha-lanczos-gb300 (and by
+        the reference's tdscha-lanczos.x)."""
+        import json
+        if not self.initialized:
+            self.prepare_symmetrization()
+        Nsyms = int(np.shape(self.symmetries[0])[0])
+        json_data = {"T": self.T, "n_steps": n_steps, "ignore_v2": self.ignore_harmonic,
+                     "ignore_v3": self.ignore_v3, "ignore_v4": self.ignore_v4,
+                     "use_wigner": self.use_wigner, "run_sym": run_symm,
+                     "data": {"n_configs": int(self.N), "n_modes": int(self.n_modes),
+                              "n_syms": Nsyms, "n_blocks": len(self.symmetries),
+                              "perturbation_modulus": self.perturbation_modulus,
+                              "reverse": self.reverse_L, "shift": self.shift_value}}
+        if not start_from_scratch:
+            raise NotImplementedError("Error, restarting from a previous calculation is not yet "
+                                      "implemented.")
+        root = os.path.join(directory, root_name)
+        if not os.path.exists(directory):
+            os.makedirs(directory)
+        with open(root + ".json", "w") as fp:
+            json.dump(json_data, fp)
+        np.savetxt(root + ".ndegs", self.N_degeneracy, fmt="%d")
+        np.savetxt(root + ".blockid", self.sym_block_id, fmt="%d")
+        np.savetxt(root + ".masses", self.m)
+        np.savetxt(root + ".freqs", self.w)
+        np.savetxt(root + ".rho", self.rho)
+        np.savetxt(root + ".X.dat", self.X)
+        np.savetxt(root + ".Y.dat", self.Y)
+        np.savetxt(root + ".psi", self.psi)
+        for i, sym in enumerate(self.symmetries):
+            np.savetxt(root + ".block{:d}".format(i), self.degenerate_space[i], fmt="%d")
+            ns, b1, b2 = sym.shape
+            with open(root + ".symsb{:d}".format(i), "w") as fp:
+                for isym in range(ns):
+                    for k1 in range(b1):
+                        fp.write("".join(" {:22.16f}".format(sym[isym, k1, k2])
+                                         for k2 in range(b2)))
+                        fp.write("\n")
+                    fp.write("\n")
+
+    def load_from_input_files(self, root_name="tdscha", directory="."):
+        """Read the output of the input-file Lanczos program (:978-1057)."""
+        import json
+        import warnings
+        if not os.path.exists(directory):
+            raise IOError("Error, the specified directory '{}' does not exist".format(directory))
+        abc_file = os.path.join(directory, "{}.abc".format(root_name))
+        if not os.path.exists(abc_file):
+            errmsg = ("\nError, the file '{}' does not exist. \n       please, check if you "
+                      "correctly run the tdscha-lanczos.x executable.\n".format(abc_file))
+            print(errmsg)
+            raise IOError(errmsg)
+        with open(abc_file) as fp:
+            rows = [l.split() for l in fp if l.strip()]
+        full = [r for r in rows if len(r) == 3]
+        self.a_coeffs = [float(r[0]) for r in rows]
+        self.b_coeffs = [float(r[1]) for r in full]
+        self.c_coeffs = [float(r[2]) for r in full]
+        q_file = os.path.join(directory, "{}.qbasis.out".format(root_name))
+        p_file = os.path.join(directory, "{}.pbasis.out".format(root_name))
+        s_file = os.path.join(directory, "{}.snorm.out".format(root_name))
+        Qb = Pb = None
+        if os.path.exists(q_file):
+            Qb = np.atleast_2d(np.loadtxt(q_file, dtype=np.double))
+        else:
+            warnings.warn("\nFile {} not found. basis_Q not loaded.\n".format(q_file))
+        if os.path.exists(p_file):
+            Pb = np.atleast_2d(np.loadtxt(p_file, dtype=np.double))
+        else:
+            warnings.warn("\nFile {} not found. basis_P not loaded.\n".format(p_file))
+        if Qb is not None or Pb is not None:
+            self._Qd = self._Pd = None
+            self._basis_host = (list(Qb) if Qb is not None else [],
+                                list(Pb) if Pb is not None else [])
+        if os.path.exists(s_file):
+            self.s_norm = list(np.loadtxt(s_file, dtype=np.double).ravel())
+        else:
+            warnings.warn("\nFile {} not found. S norm not loaded.\n".format(s_file))
+        with open(os.path.join(directory, root_name + ".json"), "r") as fp:
+            js = json.load(fp)
+        self.perturbation_modulus = js["data"]["perturbation_modulus"]
+        self.T = js["T"]
+        self.ignore_harmonic = js["ignore_v2"]
+        self.ignore_v3 = js["ignore_v3"]
+        self.ignore_v4 = js["ignore_v4"]
+        self.N = js["data"]["n_configs"]
+        self.n_modes = js["data"]["n_modes"]
+        self.reverse_L = js["data"]["reverse"]
+        self.shift_value = js["data"]["shift"]
+
     # ------------------------------------------------------------ I/O
     def save_abc(self, file):
         total = len(self.a_coeffs)

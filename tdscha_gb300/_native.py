@@ -25,7 +25,7 @@ EXPORTS = [
     "tdscha_qctx_create", "tdscha_qctx_destroy", "tdscha_qctx_set_pert",
     "tdscha_qperturb_averages", "tdscha_qapply_full_L", "tdscha_qlanczos_run",
     "tdscha_static_L", "tdscha_ctx_sync", "tdscha_static_hessian_expand",
-    "tdscha_static_hessian_collect", "tdscha_qkpm_run",
+    "tdscha_static_hessian_collect", "tdscha_qkpm_run", "tdscha_lanczos_run_hostbuf",
 ]
 
 
@@ -86,6 +86,8 @@ def load():
     lib.tdscha_static_L.argtypes = [_vp, _c_int, _vp, _vp, _c_int, _c_double, _c_int, _vp]
     lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
+    lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
+                                               _c_int, _d, _i, _i]
     lib.tdscha_qkpm_run.argtypes = [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_double, _c_double, _vp,
                                     _i, _vp]
     lib.tdscha_static_hessian_collect.argtypes = [_vp, _vp, _vp, _vp]

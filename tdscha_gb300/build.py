@@ -16,6 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtdscha_gb300.so")
+EXE_SRC = os.path.join(HERE, "exe", "tdscha_lanczos.cpp")
+EXE = os.path.join(HERE, "tdscha-lanczos-gb300")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -63,7 +65,24 @@ def build(verbose=False, force=False):
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
         os.replace(tmp, LIB)
+    build_exe(force)
     return LIB
+
+
+def build_exe(force=False):
+    """The input-file Lanczos program: host C++ linked against the library."""
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    if not (force or _needs(EXE, [EXE_SRC, LIB, os.path.join(inc, "tdscha_gb300.h")])):
+        return EXE
+    tmp = EXE + ".tmp%d" % os.getpid()
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", inc, EXE_SRC, "-o", tmp,
+           "-L", HERE, "-ltdscha_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("executable build failed: " + " ".join(cmd))
+    os.replace(tmp, EXE)
+    return EXE
 
 
 if __name__ == "__main__":

@@ -867,3 +867,49 @@ extern "C" int tdscha_qkpm_run(tdscha_qctx *ctx, double *vm, double *v, double *
     TDS_CHECK_LAUNCH();
     return TDSCHA_OK;
 }
+
+extern "C" int tdscha_lanczos_run_hostbuf(tdscha_ctx *ctx, double *basis_Q, double *basis_P,
+                                          int capacity, int start_step, int n_iter, int run_simm,
+                                          int precision, int full_reorth, double *hist,
+                                          int *steps_done, int *converged) {
+    set_error("");
+    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
+        set_error("lanczos_run_hostbuf: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
+        set_error("lanczos_run_hostbuf: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
+        return TDSCHA_ERR_ARG;
+    }
+    const long P = ctx->P;
+    const size_t row = sizeof(double) * P;
+    double *dQ = nullptr, *dP = nullptr;
+    int rc = TDSCHA_OK;
+    auto cleanup = [&]() { if (dQ) cudaFree(dQ); if (dP) cudaFree(dP); };
+    if (cudaMalloc(&dQ, row * capacity) != cudaSuccess || cudaMalloc(&dP, row * capacity) != cudaSuccess) {
+        cleanup();
+        set_error("lanczos_run_hostbuf: cannot allocate %zu bytes for the basis", 2 * row * capacity);
+        return TDSCHA_ERR_CUDA;
+    }
+    if (cudaMemcpy(dQ, basis_Q, row * (start_step + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dP, basis_P, row * (start_step + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cleanup();
+        set_error("lanczos_run_hostbuf: %s", cudaGetErrorString(cudaGetLastError()));
+        return TDSCHA_ERR_CUDA;
+    }
+    rc = tdscha_lanczos_run(ctx, dQ, dP, capacity, start_step, n_iter, run_simm, precision,
+                            full_reorth, hist, steps_done, converged, 0);
+    int nrows = *steps_done - (*converged ? 1 : 0);   // new basis rows written
+    if (nrows > 0) {
+        size_t off = (size_t)(start_step + 1) * P;
+        if (cudaMemcpy(basis_Q + off, dQ + off, row * nrows, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(basis_P + off, dP + off, row * nrows, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            if (rc == TDSCHA_OK) {
+                set_error("lanczos_run_hostbuf: %s", cudaGetErrorString(cudaGetLastError()));
+                rc = TDSCHA_ERR_CUDA;
+            }
+        }
+    }
+    cleanup();
+    return rc;
+}

@@ -161,6 +161,25 @@ def static_case(fname, M, N, seed, sh_steps):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def input_files_case(fname, M, N, S, seed):
+    """Text of every file the reference's prepare_input_files writes."""
+    import tempfile
+    ens = make_ensemble(M, N, seed=seed, n_syms=S, rho_sigma=0.1)
+    lanc = make_reference_lanczos(ens, use_wigner=False)
+    lanc.psi[:M] = random_R1(M, seed + 1)
+    lanc.perturbation_modulus = float(lanc.psi[:M].dot(lanc.psi[:M]))
+    out = dict(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"], psi=lanc.psi.copy())
+    if S > 1:
+        n_deg, deg_flat, sym_flat = _pack_syms(ens["symmetries"], ens["degenerate_space"])
+        out.update(n_deg=n_deg, deg_space=deg_flat, sym=sym_flat, S=S)
+    with tempfile.TemporaryDirectory() as d:
+        lanc.prepare_input_files(root_name="case", n_steps=7, directory=d)
+        for f in sorted(os.listdir(d)):
+            with open(os.path.join(d, f)) as fp:
+                out["file:" + f[len("case"):]] = np.array(fp.read())
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -171,6 +190,7 @@ def main():
     run_case("runft_m12_n120_s48.npz", 12, 120, 48, 0.1, 31, 12,
              [("bilanczos", False, True), ("wigner", True, True)])
     static_case("static_m12_n800.npz", 12, 800, 41, 25)
+    input_files_case("input_files_m6_n5_s48.npz", 6, 5, 48, 51)
     print("fixtures written to", HERE)
 
 
