@@ -276,6 +276,35 @@ int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int 
                         int *steps_done, int *converged, void *stream);
 
 /*
+ * Ensemble preprocessing on the GPU (one call per run; host buffers in and out).
+ * tdscha_project_modes (Modules/DynamicalLanczos.py:392-452): u, f (N x n_cart)
+ * displacements and forces minus SSCHA forces, f_mean (n_cart, may be NULL),
+ * masses (n_cart), pols (n_cart x M) ->
+ *   X = (u u_scale sqrt(m)) . pols,  Y = ((f f_scale - f_mean f_scale) / sqrt(m)) . pols
+ * tdscha_project_bloch (Modules/QSpaceLanczos.py:221-296): complex interleaved
+ * u_q, f_q (n_q x N x n_cart), pols_q (n_q x n_cart x nb), f_mean_gamma (n_cart,
+ * subtracted at q index 0, may be NULL) ->
+ *   X_q = (u_q u_scale sqrt(m)) . conj(pols_q),  Y_q = ((f_q - f_mean) f_scale / sqrt(m)) . conj(pols_q)
+ */
+int tdscha_project_modes(int N, int n_cart, int M, const double *u, const double *f,
+                         const double *f_mean, const double *masses, const double *pols,
+                         double u_scale, double f_scale, double *X_out, double *Y_out);
+int tdscha_project_bloch(int n_q, int N, int n_cart, int nb, const double *u_q, const double *f_q,
+                         const double *f_mean_gamma, const double *masses, const double *pols_q,
+                         double u_scale, double f_scale, double *X_q, double *Y_q);
+
+/*
+ * gamma_only (DynamicalLanczos.py:746-786, :3173-3191): the supercell's lattice
+ * translations as Cartesian index permutations perms (n_trans x n_cart, the
+ * reference's trans_cart_perms) and pols (n_cart x M).  Every later operator
+ * application (tdscha_apply_full_L, tdscha_lanczos_run) projects the averages:
+ * f <- P_t f, d2v <- pols^T mean_R Perm_R(pols d2v pols^T) pols.  n_trans = 0
+ * removes it.
+ */
+int tdscha_ctx_set_translations(tdscha_ctx *ctx, int n_cart, const double *pols, int n_trans,
+                                const int *perms);
+
+/*
  * Chebyshev moments of the q-space operator (QSpaceKPM.run_KPM,
  * Modules/QSpaceKPM.py:260-454, main loop :413-440): for k = n_start, ... while
  * 2k < n_moments: moments[2k] = 2 <v, v>_M - moments[0]; then

@@ -275,6 +275,8 @@ class OracleLanczos:
         M = self.n_modes
         R1, Y1 = self.get_R1_Y1(psi, transpose)
         f, d2v = self.perturb(R1, Y1)
+        if getattr(self, "trans", None) is not None:
+            f, d2v = translation_project(f, d2v, *self.trans)
         return self.repack(f, d2v, transpose)
 
     def repack(self, f, d2v, transpose=False):
@@ -547,3 +549,30 @@ def run_hessian_calculation(ol, eigen_shift=1.0, max_iters=1000, use_preconditio
         G[i, :] = res[:M]
     G = 0.5 * (G + G.T)
     return np.linalg.inv(G)
+
+
+# --- ensemble preprocessing and gamma_only -----------------------------------
+def project_modes(u, f, masses, pols, f_mean=None, u_scale=1.0, f_scale=1.0):
+    """X, Y of Lanczos.__init__ (DynamicalLanczos.py:392-452) from Cartesian data."""
+    sq = np.sqrt(masses)
+    uu = u * u_scale
+    ff = f * f_scale
+    if f_mean is not None:
+        ff = ff - f_mean * f_scale
+    return (uu * sq).dot(pols), (ff / sq).dot(pols)
+
+
+def translation_projector(pols, perms):
+    """trans_projector = mean_R pols^T P_R pols (DynamicalLanczos.py:764-785)."""
+    return np.mean([pols.T @ pols[p, :] for p in perms], axis=0)
+
+
+def translation_project(f, d2v, pols, perms):
+    """gamma_only projection of the averages (DynamicalLanczos.py:3173-3191)."""
+    f = translation_projector(pols, perms) @ f
+    d2v_cart = pols @ d2v @ pols.T
+    avg = np.zeros_like(d2v_cart)
+    for p in perms:
+        avg += d2v_cart[np.ix_(p, p)]
+    avg /= len(perms)
+    return f, pols.T @ avg @ pols

@@ -103,6 +103,8 @@ class Lanczos(object):
         self.unwrapped = False
         self.precision = precision
         self.full_reorth = False
+        self.trans_projector = None
+        self.trans_cart_perms = None
         self._ctx = None
         self._ctx_key = None
         self._Qd = None
@@ -118,6 +120,30 @@ class Lanczos(object):
         self = cls(use_wigner=use_wigner, precision=precision)
         self.set_ensemble(X, Y, w, rho, T, pols, m)
         return self
+
+    @classmethod
+    def from_cartesian(cls, u_disps, forces, sscha_forces, masses, pols, w, rho, T, f_mean=None,
+                       use_wigner=True, precision="fp64"):
+        """Ensemble in Cartesian coordinates (Angstrom, Ry/Angstrom) as python-sscha
+        stores it: the mode projection of Lanczos.__init__ (:392-452) on the GPU.
+        masses per Cartesian coordinate (3 nat), pols (3 nat, n_modes), f_mean the
+        symmetrised average force tiled on the supercell (3 nat) or None."""
+        from .preprocessing import project_modes
+        f = np.asarray(forces, dtype=np.float64) - np.asarray(sscha_forces, dtype=np.float64)
+        X, Y = project_modes(u_disps, f, masses, pols, f_mean)
+        self = cls(use_wigner=use_wigner, precision=precision)
+        self.set_ensemble(X, Y, w, rho, T, pols, masses)
+        return self
+
+    def set_translations(self, trans_cart_perms):
+        """gamma_only: project the averages on translation-invariant quantities
+        (:746-786, :3173-3191) given the supercell's lattice translations as
+        Cartesian index permutations (the reference's trans_cart_perms)."""
+        perms = [np.asarray(p, dtype=np.intp) for p in trans_cart_perms]
+        self.trans_cart_perms = perms
+        self.trans_projector = np.mean([self.pols.T @ self.pols[p, :] for p in perms], axis=0)
+        self.gamma_only = True
+        self._invalidate()
 
     def set_ensemble(self, X, Y, w, rho, T, pols=None, m=None):
         X = np.ascontiguousarray(X, dtype=TYPE_DP)
@@ -173,10 +199,10 @@ class Lanczos(object):
             u /= Ensemble.Bohr
             f *= Ensemble.Bohr
         f[:, :] -= np.tile(f_mean, (N, 1))
-        u *= np.tile(np.sqrt(mm), (N, 1))
-        f /= np.tile(np.sqrt(mm), (N, 1))
+        from .preprocessing import project_modes
+        X, Y = project_modes(u, f, mm, pols, u_scale=1.0, f_scale=1.0)
         self.dyn = dyn
-        self.set_ensemble(u.dot(pols), f.dot(pols), w, rho, ensemble.current_T, pols, mm)
+        self.set_ensemble(X, Y, w, rho, ensemble.current_T, pols, mm)
         self.nat = nat_sc
 
     def _invalidate(self):
@@ -349,7 +375,8 @@ class Lanczos(object):
             raise ValueError("Error, this class must be initialized before lunching the "
                              "computation:\n Use the .init()")
         want_mixed = self.precision == "mixed"
-        key = (id(self.X), id(self.Y), id(self.rho), self.T, id(self.symmetries))
+        key = (id(self.X), id(self.Y), id(self.rho), self.T, id(self.symmetries),
+               bool(self.gamma_only), id(self.trans_cart_perms))
         if self._ctx is not None and (self._ctx_key != key or (want_mixed and not self._ctx.with_mixed)):
             self._invalidate()
         if self._ctx is None:
@@ -358,6 +385,11 @@ class Lanczos(object):
                                     self.degenerate_space, self.sym_block_id,
                                     with_mixed=want_mixed)
             self._ctx_key = key
+            if self.gamma_only and self.trans_cart_perms is not None:
+                perms = np.ascontiguousarray(np.array(self.trans_cart_perms), dtype=np.intc)
+                pols = nat.f64(self.pols)
+                nat.check(nat.load().tdscha_ctx_set_translations(
+                    self._ctx.handle, pols.shape[0], nat.dp(pols), perms.shape[0], nat.ip(perms)))
         self._ctx.set_options(self.use_wigner, self.ignore_harmonic, self.ignore_v3,
                               self.ignore_v4, self.reverse_L, self.shift_value)
         return self._ctx

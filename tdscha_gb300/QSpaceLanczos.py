@@ -158,16 +158,12 @@ class QSpaceLanczos(Lanczos):
         qe_sym.SymmetrizeVector(f_mean)
         n_cell = np.prod(dyn.GetSupercell())
         f_mean_g = np.sqrt(n_cell) * f_mean.ravel()
-        self.X_q = np.zeros((self.n_q, self.N, self.n_bands), dtype=np.complex128)
-        self.Y_q = np.zeros_like(self.X_q)
-        for iq in range(self.n_q):
-            u = ensemble.u_disps_qspace[:, :, iq] * (u_conv * sqrt_m3[None, :])
-            df = ensemble.forces_qspace[:, :, iq] - ensemble.sscha_forces_qspace[:, :, iq]
-            if iq == 0:
-                df = df - f_mean_g[None, :]
-            f = df * (f_conv / sqrt_m3[None, :])
-            self.X_q[iq] = u @ np.conj(pols_q[:, :, iq])
-            self.Y_q[iq] = f @ np.conj(pols_q[:, :, iq])
+        # projection on the q modes on the GPU (:271-296)
+        from .preprocessing import project_bloch
+        u_q = np.transpose(ensemble.u_disps_qspace, (2, 0, 1))
+        f_q = np.transpose(ensemble.forces_qspace - ensemble.sscha_forces_qspace, (2, 0, 1))
+        self.X_q, self.Y_q = project_bloch(u_q, f_q, sqrt_m3 ** 2, np.transpose(pols_q, (2, 0, 1)),
+                                           f_mean_gamma=f_mean_g, u_scale=u_conv, f_scale=f_conv)
         self.n_modes = self.n_q * self.n_bands
 
     # --------------------------------------------------------- pair layout

@@ -26,6 +26,7 @@ EXPORTS = [
     "tdscha_qperturb_averages", "tdscha_qapply_full_L", "tdscha_qlanczos_run",
     "tdscha_static_L", "tdscha_ctx_sync", "tdscha_static_hessian_expand",
     "tdscha_static_hessian_collect", "tdscha_qkpm_run", "tdscha_lanczos_run_hostbuf",
+    "tdscha_project_modes", "tdscha_project_bloch", "tdscha_ctx_set_translations",
 ]
 
 
@@ -88,6 +89,11 @@ def load():
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
                                                _c_int, _d, _i, _i]
+    lib.tdscha_project_modes.argtypes = [_c_int, _c_int, _c_int, _d, _d, _d, _d, _d, _c_double,
+                                         _c_double, _d, _d]
+    lib.tdscha_project_bloch.argtypes = [_c_int, _c_int, _c_int, _c_int, _d, _d, _d, _d, _d,
+                                         _c_double, _c_double, _d, _d]
+    lib.tdscha_ctx_set_translations.argtypes = [_vp, _c_int, _d, _c_int, _i]
     lib.tdscha_qkpm_run.argtypes = [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_double, _c_double, _vp,
                                     _i, _vp]
     lib.tdscha_static_hessian_collect.argtypes = [_vp, _vp, _vp, _vp]

@@ -87,6 +87,11 @@ struct tdscha_ctx {
     double *Ywinv = nullptr;                    // 1 / Yw
     int *tri = nullptr;                         // (row, column) of each upper-triangle pair
     double *lam_static = nullptr;               // static pair factor Lambda (H), on first use
+    // gamma-only translation projection (tdscha_ctx_set_translations)
+    int tr_ncart = 0, tr_ntrans = 0;
+    double *tr_pols = nullptr, *tr_proj = nullptr, *tr_w1 = nullptr, *tr_w2 = nullptr,
+           *tr_w3 = nullptr, *tr_f = nullptr;
+    int *tr_perms = nullptr;
     // image rows (device), R x M
     double *D = nullptr, *F = nullptr;
     // per-pair coefficients (device), length H, rebuilt by set_options
@@ -169,6 +174,9 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
                      int precision, cudaStream_t st);
 // qspace.cu
 int q_apply_full_L_dev(tdscha_qctx *c, const double *psi_in, double *psi_out, cudaStream_t st);
+// preprocess.cu
+int apply_translation_projection(tdscha_ctx *c, cudaStream_t st);
+void free_translations(tdscha_ctx *c);
 // shared: f / d2v finalisation from the row scalars and G partials
 int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t st);
 

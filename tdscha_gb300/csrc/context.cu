@@ -90,6 +90,7 @@ static void ctx_free(tdscha_ctx *c) {
         if (p) cudaFree(p);
     if (c->tri) cudaFree(c->tri);
     if (c->lam_static) cudaFree(c->lam_static);
+    free_translations(c);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
     if (c->stat_host) cudaFreeHost(c->stat_host);
     delete c;

@@ -197,6 +197,8 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
         TDS_CHECK_LAUNCH();
         // Y1 from the unpack is symmetric by construction: no symmetrise pass
         TDS_TRY(run_perturb_sym(c, c->ignore_v4 ? 0 : 1, precision, st));
+        // gamma_only: translation projection of f and d2v (DynamicalLanczos.py:3173-3191)
+        if (c->tr_ntrans > 0) TDS_TRY(apply_translation_projection(c, st));
     }
     int nb = std::max(1, std::min(ceil_div(c->P, 256), 4096));
     k_assemble<<<nb, 256, 0, st>>>(psi_in, c->f, c->d2v, c->pc, c->tri, c->w, c->Yw, c->Ywinv,
