@@ -219,8 +219,8 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     TRYC(dev_alloc(&c->Lq, c->P)); TRYC(dev_alloc(&c->pL, c->P));
     TRYC(dev_alloc(&c->rk, c->P)); TRYC(dev_alloc(&c->sk, c->P));
     TRYC(dev_alloc(&c->mask, c->P)); TRYC(dev_alloc(&c->pc, 12 * c->H + 2 * (size_t)M * M));
-    c->nblk_dot = 296;
-    TRYC(dev_alloc(&c->dots, 4 * (size_t)c->nblk_dot)); TRYC(dev_alloc(&c->scal, 64));
+    c->nblk_dot = 296;    // block partials of the fused dot kernels (two blocks per SM)
+    TRYC(dev_alloc(&c->dots, 4 * (size_t)std::max(c->nblk_dot, 1216))); TRYC(dev_alloc(&c->scal, 64));
     CUC(cudaMemset(c->scal, 0, sizeof(double) * 64));
     CUC(cudaMallocHost((void **)&c->host_pinned, sizeof(double) * 64));
     TRYC(build_pair_coeffs(c));

@@ -385,12 +385,17 @@ __global__ void k_proj_scale(const double *__restrict__ part, const double *__re
 }
 
 constexpr int kProjMax = 2048;   // coefficients cached in shared memory per pass
+// q -= sum_j c_j Q_j, p -= sum_j d_j P_j; with pq_part != nullptr (the last
+// pass) also the block partials of p . q (mask) for the new pair's weight.
 __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__restrict__ Pb,
                              const double *__restrict__ coef, long n, int j0, int nvec, long ld,
-                             double *__restrict__ qn, double *__restrict__ pn) {
+                             double *__restrict__ qn, double *__restrict__ pn,
+                             const double *__restrict__ mask, double *__restrict__ pq_part) {
     __shared__ double cs[2 * kProjMax];
+    __shared__ double sh[32];
     for (int t = threadIdx.x; t < 2 * nvec; t += blockDim.x) cs[t] = coef[2 * j0 + t];
     __syncthreads();
+    double pq = 0;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         double q = qn[e], p = pn[e];
         for (int j = 0; j < nvec; ++j) {
@@ -399,7 +404,20 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
         }
         qn[e] = q;
         pn[e] = p;
+        pq = fma(p, q * (mask ? mask[e] : 1.0), pq);
     }
+    if (pq_part) {
+        double t = block_sum(pq, sh);
+        if (threadIdx.x == 0) pq_part[blockIdx.x] = t;
+    }
+}
+
+// pqn[k] = sum of nblk block partials (one block)
+__global__ void k_pq_reduce(const double *__restrict__ part, int nblk, double *__restrict__ pqn,
+                            int k) {
+    __shared__ double sh[32];
+    double s = reduce_parts(part, nblk, sh);
+    if (threadIdx.x == 0) pqn[k] = s;
 }
 
 // p_j . q_j for j in [j0, j0 + gridDim.x): chunk partials, then one thread per j.
@@ -582,6 +600,8 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
     TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
     int rc = TDSCHA_OK;
     int nb = std::max(1, std::min(ceil_div(P, kDotThreads), nblk));
+    // elementwise passes over the vectors and the basis: eight blocks per SM
+    int nbw = std::max(1, std::min(ceil_div(P, kDotThreads), 1216));
     int next = start_step;          // first step not yet read back
     bool stop = false;
     for (int it = 0; it < n_iter && !stop; ++it) {
@@ -606,18 +626,21 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
                                              ctx->rk, ctx->sk, ctx->dots, nb);
         k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
         double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
-        k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
+        k_normalize<<<nbw, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
         if (full_reorth) {
             int nvec = k + 1;
             double *part = ctx->rcoef + 2 * (capacity + 1);
             k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P,
                                                                 part);
             k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
-            for (int j0 = 0; j0 < nvec; j0 += kProjMax)
-                k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
-                                                 std::min(kProjMax, nvec - j0), P, qn, pn);
-            k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, k + 1, part);
-            k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
+            for (int j0 = 0; j0 < nvec; j0 += kProjMax) {
+                bool last = j0 + kProjMax >= nvec;
+                k_proj_apply<<<nbw, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
+                                                  std::min(kProjMax, nvec - j0), P, qn, pn, mask,
+                                                  last ? ctx->dots : nullptr);
+            }
+            // weight p_{k+1} . q_{k+1} of the new pair from the apply pass's partials
+            k_pq_reduce<<<1, 512, 0, st>>>(ctx->dots, nbw, ctx->pqn, k + 1);
         }
         {
             cudaError_t e = cudaGetLastError();
@@ -817,7 +840,8 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
             k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
             for (int j0 = 0; j0 < nvec; j0 += kProjMax)
                 k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_Q, ctx->rcoef, n, j0,
-                                                 std::min(kProjMax, nvec - j0), n, qn, pn);
+                                                 std::min(kProjMax, nvec - j0), n, qn, pn, nullptr,
+                                                 nullptr);
             k_dot1<<<nb, kDotThreads, 0, st>>>(qn, qn, mask, n, ctx->dots);
             k_qrenorm<<<nb, kDotThreads, 0, st>>>(ctx->dots, nb, ctx->scal, ctx->hist_dev, k, n, qn, pn);
             k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);

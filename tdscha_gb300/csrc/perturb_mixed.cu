@@ -613,8 +613,12 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, in
         }
         double rw = rho[r / S];
         double d4 = apply_d4 ? 1.0 : 0.0;
-        float4 v = make_float4((float)(rw * (s / 3 - d4 * q / 8)), (float)(rw * (t / 3 - d4 * p / 4)),
-                               (float)(-rw * q / 6), (float)(-rw * p / 3));
+        // constant reciprocals: float64 division is slow on this part and the
+        // results are rounded to fp32 anyway
+        const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
+        float4 v = make_float4((float)(rw * (s * third - d4 * q * 0.125)),
+                               (float)(rw * (t * third - d4 * p * 0.25)), (float)(-rw * q * sixth),
+                               (float)(-rw * p * third));
         abcc[r] = v;
         ma = fabsf(v.x);
         mb = fabsf(v.y);
@@ -724,10 +728,24 @@ __global__ void k_gsum(const float *__restrict__ gpart, int nsplit, int ldG, int
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         int a = (int)(e / M), b = (int)(e % M);
         const float *g = gpart + (long)a * ldG + b;
-        // compensated fp32 sum (float64 adds are slow on this part)
+        // compensated fp32 sum (float64 adds are slow on this part); the
+        // partials are loaded four at a time so the loads overlap
         float sum = 0.f, comp = 0.f;
-        for (int s = 0; s < nsplit; ++s) {
-            float y = g[s * stride] - comp;
+        int s = 0;
+        for (; s + 4 <= nsplit; s += 4) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = g[(long)(s + u) * stride];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                float y = v[u] - comp;
+                float t = sum + y;
+                comp = (t - sum) - y;
+                sum = t;
+            }
+        }
+        for (; s < nsplit; ++s) {
+            float y = g[(long)s * stride] - comp;
             float t = sum + y;
             comp = (t - sum) - y;
             sum = t;
@@ -737,17 +755,38 @@ __global__ void k_gsum(const float *__restrict__ gpart, int nsplit, int ldG, int
 }
 
 // ... then d2v = -(G + G^T) / norm and f = sum of the W-build partials / norm.
+// One 32 x 32 tile of d2v per block (256 threads), the transposed tile read
+// through shared memory so both reads are coalesced.
 __global__ void k_finalize_mixed(const double *__restrict__ gs, const float *__restrict__ fpart,
                                  int nfchunk, int M, double norm, double *__restrict__ f,
                                  double *__restrict__ d2v) {
-    long n = (long)M * M;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        int a = (int)(e / M), b = (int)(e % M);
-        d2v[e] = -(gs[e] + gs[(long)b * M + a]) / norm;
-        if (e < M) {
-            double acc = 0;
-            for (int ch = 0; ch < nfchunk; ++ch) acc += (double)fpart[(long)ch * M + e];
-            f[e] = acc / norm;
+    __shared__ double tr[32][33];
+    const double inv = 1.0 / norm;
+    const int a0 = blockIdx.y * 32, b0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 32
+    for (int k = ty; k < 32; k += 8) {
+        int a = b0 + k, b = a0 + tx;                            // gs[b0 + k][a0 + tx]
+        tr[k][tx] = (a < M && b < M) ? gs[(long)a * M + b] : 0.0;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        int a = a0 + k, b = b0 + tx;
+        if (a < M && b < M) d2v[(long)a * M + b] = -(gs[(long)a * M + b] + tr[tx][k]) * inv;
+    }
+    if (blockIdx.y == 0) {
+        // f for the block's 32 columns: 8 chunk-strided partials per column
+        __syncthreads();
+        double *red = &tr[0][0];
+        int e = b0 + tx;
+        double acc = 0;
+        if (e < M)
+            for (int ch = ty; ch < nfchunk; ch += 8) acc += (double)fpart[(long)ch * M + e];
+        red[ty * 33 + tx] = acc;
+        __syncthreads();
+        if (ty == 0 && e < M) {
+            double sum = 0;
+            for (int k = 0; k < 8; ++k) sum += red[k * 33 + tx];
+            f[e] = sum * inv;
         }
     }
 }
@@ -1025,7 +1064,7 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     }
     {
         ProfScope ps(c, 1, st);
-        k_rows_mixed<<<ceil_div(R, 256), 256, 0, st>>>(mx.qp, mx.nctile, R, c->S, c->rho, apply_d4,
+        k_rows_mixed<<<ceil_div(R, 128), 128, 0, st>>>(mx.qp, mx.nctile, R, c->S, c->rho, apply_d4,
                                                         x->abcc, x->absmax);
         TDS_CHECK_LAUNCH();
     }
@@ -1058,7 +1097,8 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
         ProfScope ps(c, 4, st);
         int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 2048));
         k_gsum<<<nb, 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, M, c->gpart);
-        k_finalize_mixed<<<nb, 256, 0, st>>>(c->gpart, x->fpart, x->nfchunk, M, c->sum_rho * c->S,
+        dim3 gt(ceil_div(M, 32), ceil_div(M, 32));
+        k_finalize_mixed<<<gt, 256, 0, st>>>(c->gpart, x->fpart, x->nfchunk, M, c->sum_rho * c->S,
                                              c->f, c->d2v);
         TDS_CHECK_LAUNCH();
     }
