@@ -385,6 +385,7 @@ def run_ours(args):
         rows["static"] = static
     if not args.no_rows:
         rows["qspace"] = qspace_leg(args.qworkload, K, W, dev, peaks, with_cpu=not args.no_cpu)
+        rows["batched"] = batch_leg(max(K, 20) * 3)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
@@ -524,6 +525,66 @@ def static_leg(lib, nat, ctx, M, R, dev):
                      "rows_timed": nvec, "matvec_s_at_M_rows": ms * M / 1e3,
                      "achieved_tflops": 4.0 * R * M * M / (ms / 1e3) / 1e12}
     return out
+
+
+def batch_leg(n_steps, seed=31):
+    """Independent runs of uneven size advanced together (tdscha_lanczos_run_batch)
+    against the same runs one after the other: mode counts log-uniform in
+    [48, 384], 2000-40000 configurations, mixed precision with re-orthogonalisation,
+    plus two q-space runs (2x2x2 grid, 6 bands)."""
+    import torch
+    from tdscha_gb300.batch import run_batch
+    from tdscha_gb300.DynamicalLanczos import Lanczos
+    from tdscha_gb300.QSpaceLanczos import QSpaceLanczos
+    from tdscha_gb300.synthetic import make_ensemble, make_qspace_ensemble, random_R1
+    rng = np.random.default_rng(seed)
+    specs = [(int(np.exp(rng.uniform(np.log(48), np.log(384)))), int(rng.uniform(2000, 40000)))
+             for _ in range(8)]
+    ens = [make_ensemble(M, N, seed=seed + i, rho_sigma=0.1) for i, (M, N) in enumerate(specs)]
+    qens = [make_qspace_ensemble((2, 2, 2), 6, 5000, seed=seed + 50 + i, dispersion=0.2)
+            for i in range(2)]
+
+    def build():
+        runs = []
+        for i, e in enumerate(ens):
+            lz = Lanczos.from_arrays(e["X"], e["Y"], e["w"], e["rho"], e["T"], use_wigner=False,
+                                     precision="mixed")
+            lz.init(use_symmetries=False)
+            lz.full_reorth = True
+            lz.prepare_perturbation(random_R1(specs[i][0], i), masses_exp=0)
+            runs.append(lz)
+        for e in qens:
+            ql = QSpaceLanczos.from_arrays(e["X_q"], e["Y_q"], e["w_q"], e["rho"], e["T"],
+                                           q_points=e["q"])
+            ql.init(use_symmetries=False)
+            ql.prepare_mode_q(0, 2)
+            runs.append(ql)
+        for r in runs:          # contexts, operands and first steps outside the timing
+            r.run_FT(2, verbose=False)
+        return runs
+
+    seq = build()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in seq:
+        r.run_FT(n_steps, verbose=False)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    for r in seq:
+        r._invalidate()
+    bat = build()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_batch(bat, n_steps)
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    for r in bat:
+        r._invalidate()
+    total = n_steps * len(bat)
+    return {"runs": [{"M": M, "N": N} for M, N in specs] + [{"qspace": "2x2x2, 6 bands, N=5000"}] * 2,
+            "steps_per_run": n_steps, "batched_steps_per_s": total / t_bat,
+            "sequential_steps_per_s": total / t_seq, "speedup": t_seq / t_bat,
+            "timer": "host wall clock, synchronised, contexts built beforehand"}
 
 
 def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):

@@ -137,6 +137,29 @@ int tdscha_lanczos_run_hostbuf(tdscha_ctx *ctx, double *basis_Q, double *basis_P
                                int full_reorth, double *hist, int *steps_done, int *converged);
 
 /*
+ * Independent Lanczos runs advanced together (the batched workload of
+ * independent perturbations, polarisations and q-points): one descriptor per
+ * run, real-space (kind 0, ctx a tdscha_ctx, the arguments of
+ * tdscha_lanczos_run) or q-space (kind 1, ctx a tdscha_qctx, those of
+ * tdscha_qlanczos_run; run_simm and precision ignored).  A context carries
+ * the recurrence state of one run, so runs need distinct contexts (several
+ * perturbations of one ensemble: one context each).  Every run gets its own
+ * stream; up to 16 steps of every active run are launched before any is read
+ * back, so the runs' kernels overlap on the GPU.  Fills steps_done, converged
+ * and status (0 or a TDSCHA_ERR_*) per run; returns the first error.
+ */
+typedef struct tdscha_run {
+    int kind;
+    void *ctx;
+    double *basis_Q, *basis_P;
+    int capacity, start_step, n_iter;
+    int run_simm, precision, reorth;
+    double *hist;
+    int steps_done, converged, status;
+} tdscha_run;
+int tdscha_lanczos_run_batch(tdscha_run *runs, int n_runs);
+
+/*
  * Continued-fraction Green function on the GPU, one thread per frequency
  * (get_green_function_continued_fraction, Modules/DynamicalLanczos.py:
  * 5032-5162).  a[n], b[n_b], c[n_c] host arrays; c is used when n_c == n_b,

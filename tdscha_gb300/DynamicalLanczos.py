@@ -646,6 +646,37 @@ class Lanczos(object):
         if run_simm and not self.use_wigner:
             raise NotImplementedError("The symmetric Lanczos works only with Wigner. Set "
                                       "use_wigner to True")
+        setup = self._ft_setup(n_iter, run_simm, 1 if (n_rep_orth > 0 or self.full_reorth) else 0)
+        torch = _torch()
+        steps_done = nat.ctypes.c_int(0)
+        conv = nat.ctypes.c_int(0)
+        st = torch.cuda.current_stream().cuda_stream
+        chunk = save_each if save_dir is not None else n_iter
+        done = 0
+        converged = False
+        i_step = setup["start"]
+        while done < n_iter and not converged:
+            todo = min(chunk, n_iter - done)
+            start = i_step + done
+            t0 = time.time()
+            nat.check(nat.load().tdscha_lanczos_run(
+                setup["ctx"], self._Qd.data_ptr(), self._Pd.data_ptr(), setup["cap"], start, todo,
+                setup["run_simm"], setup["precision"], setup["reorth"], nat.dp(setup["hist"]),
+                nat.ctypes.byref(steps_done), nat.ctypes.byref(conv), st))
+            n = steps_done.value
+            self._ft_collect(setup["hist"], start, n, bool(conv.value))
+            converged = bool(conv.value)
+            done += n
+            if verbose:
+                print("Lanczos steps %d-%d in %.3f s" % (start + 1, start + n, time.time() - t0))
+            if save_dir is not None and not converged and (start + n) % save_each == 0:
+                self.save_status("%s/%s_STEP%d" % (save_dir, prefix, start + n))
+        if converged and verbose:
+            print("   last a coeff = {}".format(self.a_coeffs[-1]))
+
+    def _ft_setup(self, n_iter, run_simm, reorth):
+        """Device basis with room for n_iter more steps and the coefficient
+        history in the C-ABI layout (rows of a, b, c, s_norm)."""
         torch = _torch()
         ctx = self._context()
         P = ctx.P
@@ -659,20 +690,17 @@ class Lanczos(object):
             else:
                 first = psi / np.sqrt(psi.dot(psi * mask))
             self.s_norm = [1]
-            rows_Q = [first]
-            rows_P = [first]
         else:
             if len(self.b_coeffs) != len(self.c_coeffs):
                 raise AssertionError("Something wrong when restoring the Lanczos. len b = {} len c = {}"
                                      .format(len(self.b_coeffs), len(self.c_coeffs)))
-            rows_Q = rows_P = None
         cap = i_step + n_iter + 2
         if i_step == 0 or self._Qd is None or self._Qd.shape[0] < cap:
             Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
             Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
             if i_step == 0:
-                Qd[0].copy_(torch.from_numpy(rows_Q[0]))
-                Pd[0].copy_(torch.from_numpy(rows_P[0]))
+                Qd[0].copy_(torch.from_numpy(first))
+                Pd[0].copy_(torch.from_numpy(first))
             elif self._Qd is not None:
                 Qd[: self._nbasis].copy_(self._Qd[: self._nbasis])
                 Pd[: self._nbasis].copy_(self._Pd[: self._nbasis])
@@ -685,46 +713,24 @@ class Lanczos(object):
         self._nbasis = i_step + 1
         self._basis_host = None
         hist = np.zeros(4 * cap, dtype=np.float64)
-        for k, a in enumerate(self.a_coeffs):
-            hist[4 * k] = a
-        for k, b in enumerate(self.b_coeffs):
-            hist[4 * k + 1] = b
-        for k, c in enumerate(self.c_coeffs):
-            hist[4 * k + 2] = c
-        for k, s in enumerate(list(self.s_norm)[: i_step + 1]):
-            hist[4 * k + 3] = s
-        steps_done = nat.ctypes.c_int(0)
-        conv = nat.ctypes.c_int(0)
-        st = torch.cuda.current_stream().cuda_stream
-        reorth = 1 if (n_rep_orth > 0 or self.full_reorth) else 0
-        chunk = save_each if save_dir is not None else n_iter
-        done = 0
-        converged = False
-        while done < n_iter and not converged:
-            todo = min(chunk, n_iter - done)
-            start = i_step + done
-            t0 = time.time()
-            nat.check(nat.load().tdscha_lanczos_run(
-                ctx.handle, self._Qd.data_ptr(), self._Pd.data_ptr(), cap, start, todo,
-                1 if run_simm else 0, self._prec(), reorth, nat.dp(hist),
-                nat.ctypes.byref(steps_done), nat.ctypes.byref(conv), st))
-            n = steps_done.value
-            for k in range(start, start + n):
-                self.a_coeffs.append(float(hist[4 * k]))
-                if conv.value and k == start + n - 1:
-                    break
-                self.b_coeffs.append(float(hist[4 * k + 1]))
-                self.c_coeffs.append(float(hist[4 * k + 2]))
-                self.s_norm.append(float(hist[4 * (k + 1) + 3]))
-                self._nbasis = k + 2
-            converged = bool(conv.value)
-            done += n
-            if verbose:
-                print("Lanczos steps %d-%d in %.3f s" % (start + 1, start + n, time.time() - t0))
-            if save_dir is not None and not converged and (start + n) % save_each == 0:
-                self.save_status("%s/%s_STEP%d" % (save_dir, prefix, start + n))
-        if converged and verbose:
-            print("   last a coeff = {}".format(self.a_coeffs[-1]))
+        hist[0:4 * len(self.a_coeffs):4] = self.a_coeffs
+        hist[1:4 * len(self.b_coeffs):4] = self.b_coeffs
+        hist[2:4 * len(self.c_coeffs):4] = self.c_coeffs
+        s_prev = list(self.s_norm)[: i_step + 1]
+        hist[3:4 * len(s_prev):4] = s_prev
+        return {"ctx": ctx.handle, "cap": cap, "start": i_step, "hist": hist, "kind": 0,
+                "run_simm": 1 if run_simm else 0, "precision": self._prec(), "reorth": reorth}
+
+    def _ft_collect(self, hist, start, n, converged):
+        """Append the coefficients of steps start .. start+n-1 from the history."""
+        for k in range(start, start + n):
+            self.a_coeffs.append(float(hist[4 * k]))
+            if converged and k == start + n - 1:
+                break
+            self.b_coeffs.append(float(hist[4 * k + 1]))
+            self.c_coeffs.append(float(hist[4 * k + 2]))
+            self.s_norm.append(float(hist[4 * (k + 1) + 3]))
+            self._nbasis = k + 2
 
     def get_green_function_continued_fraction(self, w_array, use_terminator=True, last_average=1,
                                               smearing=0, smooth_ramp=0):

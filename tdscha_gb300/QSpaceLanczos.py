@@ -522,6 +522,38 @@ class QSpaceLanczos(Lanczos):
             raise ValueError(err)
         if save_dir is not None and not os.path.exists(save_dir):
             os.makedirs(save_dir)
+        setup = self._ft_setup(n_iter, 1 if reorthogonalize else 0)
+        torch = _torch()
+        steps_done = nat.ctypes.c_int(0)
+        conv = nat.ctypes.c_int(0)
+        st = torch.cuda.current_stream().cuda_stream
+        chunk = save_each if save_dir is not None else n_iter
+        done = 0
+        converged = False
+        i_step = setup["start"]
+        while done < n_iter and not converged:
+            todo = min(chunk, n_iter - done)
+            start = i_step + done
+            t0 = time.time()
+            nat.check(nat.load().tdscha_qlanczos_run(
+                setup["ctx"], self._Qd.data_ptr(), self._Pd.data_ptr(), setup["cap"], start, todo,
+                setup["reorth"], nat.dp(setup["hist"]), nat.ctypes.byref(steps_done),
+                nat.ctypes.byref(conv), st))
+            n = steps_done.value
+            self._ft_collect(setup["hist"], start, n, bool(conv.value))
+            converged = bool(conv.value)
+            done += n
+            if verbose:
+                print("Q-space Lanczos steps %d-%d in %.3f s" % (start + 1, start + n,
+                                                                time.time() - t0))
+            if save_dir is not None and not converged and (start + n) % save_each == 0:
+                self.save_status("%s/%s_STEP%d" % (save_dir, prefix, start + n))
+        if converged and verbose:
+            print("   last a coeff = {}".format(self.a_coeffs[-1]))
+
+    def _ft_setup(self, n_iter, reorth):
+        """Device basis (interleaved complex rows) with room for n_iter more
+        steps and the coefficient history in the C-ABI layout."""
         torch = _torch()
         ctx = self._qcontext()
         n2 = 2 * ctx.P
@@ -529,7 +561,9 @@ class QSpaceLanczos(Lanczos):
         dev = torch.device("cuda")
         cap = i_step + n_iter + 2
         if i_step == 0:
-            first = psi / np.sqrt(psi_norm)
+            mask = self.mask_dot_wigner()
+            psi = np.asarray(self.psi, dtype=np.complex128)
+            first = psi / np.sqrt(np.real(np.conj(psi).dot(psi * mask)))
             self.s_norm = [1]
         if i_step == 0 or self._Qd is None or self._Qd.shape[0] < cap:
             Qd = torch.empty((cap, n2), dtype=torch.float64, device=dev)
@@ -555,38 +589,8 @@ class QSpaceLanczos(Lanczos):
         hist[2:4 * len(self.c_coeffs):4] = self.c_coeffs
         s_prev = list(self.s_norm)[: i_step + 1]
         hist[3:4 * len(s_prev):4] = s_prev
-        steps_done = nat.ctypes.c_int(0)
-        conv = nat.ctypes.c_int(0)
-        st = torch.cuda.current_stream().cuda_stream
-        chunk = save_each if save_dir is not None else n_iter
-        done = 0
-        converged = False
-        while done < n_iter and not converged:
-            todo = min(chunk, n_iter - done)
-            start = i_step + done
-            t0 = time.time()
-            nat.check(nat.load().tdscha_qlanczos_run(
-                ctx.handle, self._Qd.data_ptr(), self._Pd.data_ptr(), cap, start, todo,
-                1 if reorthogonalize else 0, nat.dp(hist), nat.ctypes.byref(steps_done),
-                nat.ctypes.byref(conv), st))
-            n = steps_done.value
-            for k in range(start, start + n):
-                self.a_coeffs.append(float(hist[4 * k]))
-                if conv.value and k == start + n - 1:
-                    break
-                self.b_coeffs.append(float(hist[4 * k + 1]))
-                self.c_coeffs.append(float(hist[4 * k + 2]))
-                self.s_norm.append(float(hist[4 * (k + 1) + 3]))
-                self._nbasis = k + 2
-            converged = bool(conv.value)
-            done += n
-            if verbose:
-                print("Q-space Lanczos steps %d-%d in %.3f s" % (start + 1, start + n,
-                                                                time.time() - t0))
-            if save_dir is not None and not converged and (start + n) % save_each == 0:
-                self.save_status("%s/%s_STEP%d" % (save_dir, prefix, start + n))
-        if converged and verbose:
-            print("   last a coeff = {}".format(self.a_coeffs[-1]))
+        return {"ctx": ctx.handle, "cap": cap, "start": i_step, "hist": hist, "kind": 1,
+                "run_simm": 0, "precision": 0, "reorth": reorth}
 
     # ------------------------------------------------------------------ I/O
     def save_status(self, file):

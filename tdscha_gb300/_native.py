@@ -27,6 +27,7 @@ EXPORTS = [
     "tdscha_static_L", "tdscha_ctx_sync", "tdscha_static_hessian_expand",
     "tdscha_static_hessian_collect", "tdscha_qkpm_run", "tdscha_lanczos_run_hostbuf",
     "tdscha_project_modes", "tdscha_project_bloch", "tdscha_ctx_set_translations",
+    "tdscha_lanczos_run_batch",
 ]
 
 
@@ -94,6 +95,7 @@ def load():
     lib.tdscha_project_bloch.argtypes = [_c_int, _c_int, _c_int, _c_int, _d, _d, _d, _d, _d,
                                          _c_double, _c_double, _d, _d]
     lib.tdscha_ctx_set_translations.argtypes = [_vp, _c_int, _d, _c_int, _i]
+    lib.tdscha_lanczos_run_batch.argtypes = [_vp, _c_int]
     lib.tdscha_qkpm_run.argtypes = [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_double, _c_double, _vp,
                                     _i, _vp]
     lib.tdscha_static_hessian_collect.argtypes = [_vp, _vp, _vp, _vp]

@@ -536,30 +536,15 @@ extern "C" int tdscha_apply_full_L(tdscha_ctx *ctx, const double *psi_in, double
     return apply_full_L_dev(ctx, psi_in, psi_out, transpose, precision, (cudaStream_t)stream);
 }
 
-extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
-                                  int start_step, int n_iter, int run_simm, int precision,
-                                  int full_reorth, double *hist, int *steps_done, int *converged,
-                                  void *stream) {
-    set_error("");
-    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
-        set_error("lanczos_run: null pointer");
-        return TDSCHA_ERR_ARG;
-    }
-    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
-        set_error("lanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
-        return TDSCHA_ERR_ARG;
-    }
-    if (run_simm && !ctx->use_wigner) {
-        set_error("lanczos_run: the symmetric Lanczos works only with Wigner");
-        return TDSCHA_ERR_ARG;
-    }
-    *steps_done = 0;
-    *converged = 0;
-    cudaStream_t st = (cudaStream_t)stream;
+namespace tdscha {
+
+// Buffers and start-of-run state of one real-space run (everything before the
+// first step of tdscha_lanczos_run); stream ordered.
+static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                    int start_step, int run_simm, int full_reorth, const double *hist,
+                    cudaStream_t st) {
     const long P = ctx->P;
-    const int nblk = ctx->nblk_dot;
     const double *mask = run_simm ? ctx->mask : nullptr;
-    // device copy of the history (capacity rows)
     if (ctx->hist_cap < capacity + 1) {
         if (ctx->hist_dev) cudaFree(ctx->hist_dev);
         ctx->hist_dev = nullptr;
@@ -584,10 +569,6 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
-    // the recurrence's stop conditions are evaluated on the device (per-step
-    // status + a halt flag that turns later steps into no-ops), so steps are
-    // launched back to back and read back every kSyncEvery steps
-    constexpr int kSyncEvery = 16;
     if (ctx->stat_cap < capacity + 1) {
         if (ctx->stat_dev) cudaFree(ctx->stat_dev);
         if (ctx->stat_host) cudaFreeHost(ctx->stat_host);
@@ -598,10 +579,83 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         ctx->stat_cap = capacity + 1;
     }
     TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
-    int rc = TDSCHA_OK;
-    int nb = std::max(1, std::min(ceil_div(P, kDotThreads), nblk));
+    return TDSCHA_OK;
+}
+
+// The launches of step k (run_FT :6145-6448): operator application(s), the
+// recurrence scalars on the device, the new pair and its re-biorthogonalisation.
+static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity, int k,
+                   int run_simm, int precision, int full_reorth, cudaStream_t st) {
+    const long P = ctx->P;
+    const double *mask = run_simm ? ctx->mask : nullptr;
+    const int nb = std::max(1, std::min(ceil_div(P, kDotThreads), ctx->nblk_dot));
     // elementwise passes over the vectors and the basis: eight blocks per SM
-    int nbw = std::max(1, std::min(ceil_div(P, kDotThreads), 1216));
+    const int nbw = std::max(1, std::min(ceil_div(P, kDotThreads), 1216));
+    double *q = basis_Q + (long)k * P, *p = basis_P + (long)k * P;
+    TDS_TRY(apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st));
+    const double *pL = ctx->Lq;
+    if (!run_simm) {
+        TDS_TRY(apply_full_L_dev(ctx, p, ctx->pL, 1, precision, st));
+        pL = ctx->pL;
+    }
+    k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
+    k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
+    const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
+    k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
+                                         ctx->rk, ctx->sk, ctx->dots, nb);
+    k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
+    k_normalize<<<nbw, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
+    if (full_reorth) {
+        int nvec = k + 1;
+        double *part = ctx->rcoef + 2 * (capacity + 1);
+        k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P,
+                                                            part);
+        k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
+        for (int j0 = 0; j0 < nvec; j0 += kProjMax) {
+            bool last = j0 + kProjMax >= nvec;
+            k_proj_apply<<<nbw, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
+                                              std::min(kProjMax, nvec - j0), P, qn, pn, mask,
+                                              last ? ctx->dots : nullptr);
+        }
+        // weight p_{k+1} . q_{k+1} of the new pair from the apply pass's partials
+        k_pq_reduce<<<1, 512, 0, st>>>(ctx->dots, nbw, ctx->pqn, k + 1);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
+    return TDSCHA_OK;
+}
+
+// the recurrence's stop conditions are evaluated on the device (per-step
+// status + a halt flag that turns later steps into no-ops), so steps are
+// launched back to back and read back every kSyncEvery steps
+constexpr int kSyncEvery = 16;
+
+}  // namespace tdscha
+
+extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                                  int start_step, int n_iter, int run_simm, int precision,
+                                  int full_reorth, double *hist, int *steps_done, int *converged,
+                                  void *stream) {
+    set_error("");
+    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
+        set_error("lanczos_run: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
+        set_error("lanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
+        return TDSCHA_ERR_ARG;
+    }
+    if (run_simm && !ctx->use_wigner) {
+        set_error("lanczos_run: the symmetric Lanczos works only with Wigner");
+        return TDSCHA_ERR_ARG;
+    }
+    *steps_done = 0;
+    *converged = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    TDS_TRY(lz_begin(ctx, basis_Q, basis_P, capacity, start_step, run_simm, full_reorth, hist, st));
+    int rc = TDSCHA_OK;
     int next = start_step;          // first step not yet read back
     bool stop = false;
     for (int it = 0; it < n_iter && !stop; ++it) {
@@ -611,41 +665,8 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             rc = TDSCHA_ERR_ARG;
             break;
         }
-        double *q = basis_Q + (long)k * P, *p = basis_P + (long)k * P;
-        if ((rc = apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st)) != TDSCHA_OK) break;
-        const double *pL = ctx->Lq;
-        if (!run_simm) {
-            if ((rc = apply_full_L_dev(ctx, p, ctx->pL, 1, precision, st)) != TDSCHA_OK) break;
-            pL = ctx->pL;
-        }
-        k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
-        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-        const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
-        const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
-        k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
-                                             ctx->rk, ctx->sk, ctx->dots, nb);
-        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-        double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
-        k_normalize<<<nbw, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
-        if (full_reorth) {
-            int nvec = k + 1;
-            double *part = ctx->rcoef + 2 * (capacity + 1);
-            k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P,
-                                                                part);
-            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
-            for (int j0 = 0; j0 < nvec; j0 += kProjMax) {
-                bool last = j0 + kProjMax >= nvec;
-                k_proj_apply<<<nbw, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
-                                                  std::min(kProjMax, nvec - j0), P, qn, pn, mask,
-                                                  last ? ctx->dots : nullptr);
-            }
-            // weight p_{k+1} . q_{k+1} of the new pair from the apply pass's partials
-            k_pq_reduce<<<1, 512, 0, st>>>(ctx->dots, nbw, ctx->pqn, k + 1);
-        }
-        {
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
-        }
+        if ((rc = lz_step(ctx, basis_Q, basis_P, capacity, k, run_simm, precision, full_reorth, st)) != TDSCHA_OK)
+            break;
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
         rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
                              hist, start_step, steps_done, converged, &stop);
@@ -763,25 +784,11 @@ extern "C" int tdscha_continued_fraction(const double *a, int n, const double *b
     return TDSCHA_OK;
 }
 
-extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capacity,
-                                   int start_step, int n_iter, int reorthogonalize, double *hist,
-                                   int *steps_done, int *converged, void *stream) {
-    set_error("");
-    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
-        set_error("qlanczos_run: null pointer");
-        return TDSCHA_ERR_ARG;
-    }
-    if (ctx->n_pairs == 0) { set_error("qlanczos_run: call tdscha_qctx_set_pert first"); return TDSCHA_ERR_STATE; }
-    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
-        set_error("qlanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
-        return TDSCHA_ERR_ARG;
-    }
-    if (basis_Q == basis_P) { set_error("qlanczos_run: basis_Q and basis_P must be distinct"); return TDSCHA_ERR_ARG; }
-    *steps_done = 0;
-    *converged = 0;
-    cudaStream_t st = (cudaStream_t)stream;
+namespace tdscha {
+
+static int qz_begin(tdscha_qctx *ctx, double *basis_Q, int capacity, int start_step,
+                    int reorthogonalize, const double *hist, cudaStream_t st) {
     const long n = 2 * ctx->P;           // interleaved (re, im) doubles
-    const double *mask = ctx->mask;
     if (ctx->hist_cap < capacity + 1) {
         if (ctx->hist_dev) cudaFree(ctx->hist_dev);
         if (ctx->stat_dev) cudaFree(ctx->stat_dev);
@@ -802,14 +809,75 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
     double *part = ctx->rcoef + 2 * (capacity + 1);
     if (reorthogonalize) {
         // Q is orthonormal in the mask product; the weights q_j . q_j are kept exact
-        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, 0, part);
+        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, ctx->mask, n, n, 0, part);
         k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
     TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
-    constexpr int kSyncEvery = 16;
-    int rc = TDSCHA_OK;
+    return TDSCHA_OK;
+}
+
+// Step k of the Hermitian q-space Lanczos (QSpaceLanczos.py:1050-1140).
+static int qz_step(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capacity, int k,
+                   int reorthogonalize, cudaStream_t st) {
+    const long n = 2 * ctx->P;
+    const double *mask = ctx->mask;
     const int nb = std::max(1, std::min(ceil_div(n, kDotThreads), 296));
+    double *part = ctx->rcoef + 2 * (capacity + 1);
+    double *q = basis_Q + (long)k * n, *p = basis_P + (long)k * n;
+    // Hermitian operator: p_L = L q (QSpaceLanczos.py:1055-1057)
+    TDS_TRY(q_apply_full_L_dev(ctx, q, ctx->Lq, st));
+    k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, n, ctx->dots);
+    k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * n : nullptr;
+    const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * n : nullptr;
+    k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, ctx->Lq, q, p, qprev, pprev, mask, ctx->scal, n,
+                                         ctx->rk, ctx->sk, ctx->dots, nb);
+    k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    double *qn = basis_Q + (long)(k + 1) * n, *pn = basis_P + (long)(k + 1) * n;
+    k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, n, qn, pn);
+    if (reorthogonalize) {
+        // one classical Gram-Schmidt pass of q_{k+1} against q_0..q_k with the
+        // real mask product (the p side of the shared kernels runs on the
+        // p_{k+1} slot, which the renormalisation then overwrites)
+        int nvec = k + 1;
+        k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, qn, pn, mask, n, n, part);
+        k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
+        for (int j0 = 0; j0 < nvec; j0 += kProjMax)
+            k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_Q, ctx->rcoef, n, j0,
+                                             std::min(kProjMax, nvec - j0), n, qn, pn, nullptr,
+                                             nullptr);
+        k_dot1<<<nb, kDotThreads, 0, st>>>(qn, qn, mask, n, ctx->dots);
+        k_qrenorm<<<nb, kDotThreads, 0, st>>>(ctx->dots, nb, ctx->scal, ctx->hist_dev, k, n, qn, pn);
+        k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);
+        k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error("qlanczos_run launch: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
+    return TDSCHA_OK;
+}
+
+}  // namespace tdscha
+
+extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                                   int start_step, int n_iter, int reorthogonalize, double *hist,
+                                   int *steps_done, int *converged, void *stream) {
+    set_error("");
+    if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
+        set_error("qlanczos_run: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    if (ctx->n_pairs == 0) { set_error("qlanczos_run: call tdscha_qctx_set_pert first"); return TDSCHA_ERR_STATE; }
+    if (capacity < 1 || start_step < 0 || n_iter < 0 || start_step + 1 > capacity) {
+        set_error("qlanczos_run: bad capacity %d / start %d / n_iter %d", capacity, start_step, n_iter);
+        return TDSCHA_ERR_ARG;
+    }
+    if (basis_Q == basis_P) { set_error("qlanczos_run: basis_Q and basis_P must be distinct"); return TDSCHA_ERR_ARG; }
+    *steps_done = 0;
+    *converged = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    TDS_TRY(qz_begin(ctx, basis_Q, capacity, start_step, reorthogonalize, hist, st));
+    int rc = TDSCHA_OK;
     int next = start_step;
     bool stop = false;
     for (int it = 0; it < n_iter && !stop; ++it) {
@@ -819,43 +887,110 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
             rc = TDSCHA_ERR_ARG;
             break;
         }
-        double *q = basis_Q + (long)k * n, *p = basis_P + (long)k * n;
-        // Hermitian operator: p_L = L q (QSpaceLanczos.py:1055-1057)
-        if ((rc = q_apply_full_L_dev(ctx, q, ctx->Lq, st)) != TDSCHA_OK) break;
-        k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, n, ctx->dots);
-        k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-        const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * n : nullptr;
-        const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * n : nullptr;
-        k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, ctx->Lq, q, p, qprev, pprev, mask, ctx->scal, n,
-                                             ctx->rk, ctx->sk, ctx->dots, nb);
-        k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-        double *qn = basis_Q + (long)(k + 1) * n, *pn = basis_P + (long)(k + 1) * n;
-        k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, n, qn, pn);
-        if (reorthogonalize) {
-            // one classical Gram-Schmidt pass of q_{k+1} against q_0..q_k with the
-            // real mask product (the p side of the shared kernels runs on the
-            // p_{k+1} slot, which the renormalisation then overwrites)
-            int nvec = k + 1;
-            k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, qn, pn, mask, n, n, part);
-            k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
-            for (int j0 = 0; j0 < nvec; j0 += kProjMax)
-                k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_Q, ctx->rcoef, n, j0,
-                                                 std::min(kProjMax, nvec - j0), n, qn, pn, nullptr,
-                                                 nullptr);
-            k_dot1<<<nb, kDotThreads, 0, st>>>(qn, qn, mask, n, ctx->dots);
-            k_qrenorm<<<nb, kDotThreads, 0, st>>>(ctx->dots, nb, ctx->scal, ctx->hist_dev, k, n, qn, pn);
-            k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);
-            k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
-        }
-        {
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) { set_error("qlanczos_run launch: %s", cudaGetErrorString(e)); rc = TDSCHA_ERR_CUDA; break; }
-        }
+        if ((rc = qz_step(ctx, basis_Q, basis_P, capacity, k, reorthogonalize, st)) != TDSCHA_OK) break;
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
         rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
                              hist, start_step, steps_done, converged, &stop);
         if (rc != TDSCHA_OK) break;
         next = k + 1;
+    }
+    return rc;
+}
+
+// Many independent runs together (real-space and q-space contexts mixed): each
+// run gets its own stream; the driver launches up to kSyncEvery steps of every
+// active run before it reads any of them back, so the runs' kernels overlap on
+// the device.  Per-run results and status in the descriptors.
+extern "C" int tdscha_lanczos_run_batch(tdscha_run *runs, int n_runs) {
+    set_error("");
+    if (!runs || n_runs < 0) { set_error("lanczos_run_batch: bad arguments"); return TDSCHA_ERR_ARG; }
+    for (int i = 0; i < n_runs; ++i) {
+        tdscha_run &r = runs[i];
+        r.steps_done = 0;
+        r.converged = 0;
+        r.status = TDSCHA_OK;
+        bool ok = r.ctx && r.basis_Q && r.basis_P && r.hist && r.capacity >= 1 && r.start_step >= 0 &&
+                  r.n_iter >= 0 && r.start_step + r.n_iter < r.capacity && (r.kind == 0 || r.kind == 1) &&
+                  r.basis_Q != r.basis_P;
+        if (ok && r.kind == 0) ok = !r.run_simm || ((tdscha_ctx *)r.ctx)->use_wigner;
+        if (ok && r.kind == 1) ok = ((tdscha_qctx *)r.ctx)->n_pairs > 0;
+        if (!ok) {
+            set_error("lanczos_run_batch: run %d has bad arguments", i);
+            return TDSCHA_ERR_ARG;
+        }
+    }
+    // a context holds the recurrence state of one run: one context per run
+    for (int i = 0; i < n_runs; ++i)
+        for (int j = 0; j < i; ++j)
+            if (runs[j].ctx == runs[i].ctx) {
+                set_error("lanczos_run_batch: runs %d and %d share a context", j, i);
+                return TDSCHA_ERR_ARG;
+            }
+    std::vector<cudaStream_t> own;
+    std::vector<cudaStream_t> streams(n_runs, nullptr);
+    std::vector<int> next(n_runs), done(n_runs, 0);
+    std::vector<bool> active(n_runs, true);
+    int rc = TDSCHA_OK;
+    auto fail = [&](int i, int code) {
+        runs[i].status = code;
+        active[i] = false;
+        if (rc == TDSCHA_OK) rc = code;
+    };
+    for (int i = 0; i < n_runs && rc == TDSCHA_OK; ++i) {
+        if (cudaStreamCreateWithFlags(&streams[i], cudaStreamNonBlocking) != cudaSuccess) {
+            set_error("lanczos_run_batch: cannot create a stream");
+            rc = TDSCHA_ERR_CUDA;
+            break;
+        }
+        own.push_back(streams[i]);
+        tdscha_run &r = runs[i];
+        int b = r.kind == 0
+                    ? lz_begin((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, r.start_step,
+                               r.run_simm, r.reorth, r.hist, streams[i])
+                    : qz_begin((tdscha_qctx *)r.ctx, r.basis_Q, r.capacity, r.start_step, r.reorth,
+                               r.hist, streams[i]);
+        if (b != TDSCHA_OK) fail(i, b);
+        next[i] = r.start_step;
+        if (r.n_iter == 0) active[i] = false;
+    }
+    while (rc == TDSCHA_OK) {
+        bool any = false;
+        for (int i = 0; i < n_runs; ++i) {
+            if (!active[i]) continue;
+            any = true;
+            tdscha_run &r = runs[i];
+            int todo = std::min(kSyncEvery, r.n_iter - done[i]);
+            for (int t = 0; t < todo; ++t) {
+                int k = r.start_step + done[i] + t;
+                int e = r.kind == 0
+                            ? lz_step((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, k,
+                                      r.run_simm, r.precision, r.reorth, streams[i])
+                            : qz_step((tdscha_qctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, k,
+                                      r.reorth, streams[i]);
+                if (e != TDSCHA_OK) { fail(i, e); break; }
+            }
+            if (active[i]) done[i] += todo;
+        }
+        if (!any || rc != TDSCHA_OK) break;
+        for (int i = 0; i < n_runs; ++i) {
+            if (!active[i]) continue;
+            tdscha_run &r = runs[i];
+            int k = r.start_step + done[i] - 1;
+            bool stop = false;
+            double *hd = r.kind == 0 ? ((tdscha_ctx *)r.ctx)->hist_dev : ((tdscha_qctx *)r.ctx)->hist_dev;
+            double *sd = r.kind == 0 ? ((tdscha_ctx *)r.ctx)->stat_dev : ((tdscha_qctx *)r.ctx)->stat_dev;
+            double *sh = r.kind == 0 ? ((tdscha_ctx *)r.ctx)->stat_host : ((tdscha_qctx *)r.ctx)->stat_host;
+            int e = read_back_steps(hd, sd, sh, r.capacity, next[i], k, streams[i], r.hist,
+                                    r.start_step, &r.steps_done, &r.converged, &stop);
+            if (e == TDSCHA_OK && r.kind == 0) e = mixed_check_error((tdscha_ctx *)r.ctx);
+            if (e != TDSCHA_OK) { fail(i, e); continue; }
+            next[i] = k + 1;
+            if (stop || done[i] >= r.n_iter) active[i] = false;
+        }
+    }
+    for (cudaStream_t s : own) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
     }
     return rc;
 }
