@@ -386,6 +386,7 @@ def run_ours(args):
     if not args.no_rows:
         rows["qspace"] = qspace_leg(args.qworkload, K, W, dev, peaks, with_cpu=not args.no_cpu)
         rows["batched"] = batch_leg(max(K, 20) * 3)
+        rows["learned_terminator"] = terminator_leg()
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
@@ -585,6 +586,19 @@ def batch_leg(n_steps, seed=31):
             "steps_per_run": n_steps, "batched_steps_per_s": total / t_bat,
             "sequential_steps_per_s": total / t_seq, "speedup": t_seq / t_bat,
             "timer": "host wall clock, synchronised, contexts built beforehand"}
+
+
+def terminator_leg():
+    """The learned terminator (committed weights) on ten fresh runs it was not
+    trained on: 100 measured steps extended to 320 against the 320-step run."""
+    from tdscha_gb300.terminator import LearnedTerminator, evaluate, generate_runs
+    runs = generate_runs(10, 320, seed=7)
+    term = LearnedTerminator()
+    t0 = time.perf_counter()
+    rep = evaluate(term, runs, 100, 320)
+    rep["evaluate_s"] = time.perf_counter() - t0
+    rep["network"] = "3 layers, width 256, tanh; window 48, horizon 64; trained on 400 runs"
+    return rep
 
 
 def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):

@@ -342,6 +342,29 @@ int tdscha_qkpm_run(tdscha_qctx *ctx, double *vm, double *v, double *work, int n
                     int n_moments, double rescale_a, double rescale_b, double *moments,
                     int *swapped, void *stream);
 
+/*
+ * Learned continued-fraction terminator (no counterpart in the reference): a
+ * 3-layer perceptron h1 = tanh(x W1 + b1), h2 = tanh(h1 W2 + b2), y = h2 W3 + b3,
+ * trained on the GPU (float32 forward / backward, mean-squared error, Adam).
+ * Parameters flat: W1 (n_in x n_hidden), b1, W2 (n_hidden x n_hidden), b2,
+ * W3 (n_hidden x n_out), b3, weights row-major.  forward / loss_grad take host
+ * buffers; train_step takes device buffers (x: rows x n_in, t: rows x n_out).
+ * bf16 != 0 in forward rounds weights and layer inputs to bfloat16 (float32
+ * accumulation).
+ */
+typedef struct tdscha_mlp tdscha_mlp;
+int tdscha_mlp_create(tdscha_mlp **mlp, int n_in, int n_hidden, int n_out);
+int tdscha_mlp_destroy(tdscha_mlp *mlp);
+long tdscha_mlp_num_params(const tdscha_mlp *mlp);
+int tdscha_mlp_set_params(tdscha_mlp *mlp, const float *params);
+int tdscha_mlp_get_params(tdscha_mlp *mlp, float *params);
+int tdscha_mlp_forward(tdscha_mlp *mlp, const float *x, int rows, int bf16, float *y);
+int tdscha_mlp_loss_grad(tdscha_mlp *mlp, const float *x, const float *t, int rows, float *loss,
+                         float *grad);
+int tdscha_mlp_train_step(tdscha_mlp *mlp, const float *x, const float *t, int rows, float lr,
+                          float beta1, float beta2, float eps, int step, float *loss,
+                          void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,9 @@ EXPORTS = [
     "tdscha_static_L", "tdscha_ctx_sync", "tdscha_static_hessian_expand",
     "tdscha_static_hessian_collect", "tdscha_qkpm_run", "tdscha_lanczos_run_hostbuf",
     "tdscha_project_modes", "tdscha_project_bloch", "tdscha_ctx_set_translations",
-    "tdscha_lanczos_run_batch",
+    "tdscha_lanczos_run_batch", "tdscha_mlp_create", "tdscha_mlp_destroy",
+    "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
+    "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
 ]
 
 
@@ -96,6 +98,16 @@ def load():
                                          _c_double, _c_double, _d, _d]
     lib.tdscha_ctx_set_translations.argtypes = [_vp, _c_int, _d, _c_int, _i]
     lib.tdscha_lanczos_run_batch.argtypes = [_vp, _c_int]
+    _f = ctypes.POINTER(ctypes.c_float)
+    lib.tdscha_mlp_create.argtypes = [ctypes.POINTER(_vp), _c_int, _c_int, _c_int]
+    lib.tdscha_mlp_destroy.argtypes = [_vp]
+    lib.tdscha_mlp_num_params.argtypes = [_vp]
+    lib.tdscha_mlp_set_params.argtypes = [_vp, _f]
+    lib.tdscha_mlp_get_params.argtypes = [_vp, _f]
+    lib.tdscha_mlp_forward.argtypes = [_vp, _f, _c_int, _c_int, _f]
+    lib.tdscha_mlp_loss_grad.argtypes = [_vp, _f, _f, _c_int, _f, _f]
+    lib.tdscha_mlp_train_step.argtypes = [_vp, _vp, _vp, _c_int, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_float, _c_int, _f, _vp]
     lib.tdscha_qkpm_run.argtypes = [_vp, _vp, _vp, _vp, _c_int, _c_int, _c_double, _c_double, _vp,
                                     _i, _vp]
     lib.tdscha_static_hessian_collect.argtypes = [_vp, _vp, _vp, _vp]
@@ -103,6 +115,7 @@ def load():
         fn = getattr(lib, name)
         if name not in ("tdscha_last_error", "tdscha_version"):
             fn.restype = ctypes.c_int
+    lib.tdscha_mlp_num_params.restype = ctypes.c_long
     _lib = lib
     return lib
 
