@@ -349,9 +349,10 @@ def run_ours(args):
                 Mp = ((M + 63) // 64) * 64
                 roof["tensor_work_incl_split_tflops"] = 3 * 2.0 * R * Mp * Mp / per_launch_s / 1e12
                 roof["frac_incl_split"] = roof["tensor_work_incl_split_tflops"] / peak
-                # DRAM bytes per launch from the ncu capture of the same kernel at
-                # N=20 000 (profiles/k_gemm_tc_m573_n20k.md), scaled by image rows
-                per_row = {0: 143.8e6 / 20000, 3: 95.9e6 / 20000}[kid]
+                # DRAM bytes per launch from the ncu captures of the same kernels
+                # at N=20 000 (profiles/k_stageA_tc_m573_n20k.md for stage A,
+                # profiles/k_gemm_tc_m573_n20k.md for stage B), scaled by image rows
+                per_row = {0: 144.9e6 / 20000, 3: 95.9e6 / 20000}[kid]
                 if M == 573:
                     roof["traffic"] = per_row * R
                     roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"

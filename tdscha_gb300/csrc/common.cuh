@@ -59,7 +59,7 @@ struct MixedStore {
     float *ut32 = nullptr;                               // U^T (fp32)
     __half *wt_hi = nullptr, *wt_lo = nullptr;          // W^T, rebuilt per call
     __half *y1_hi = nullptr, *y1_lo = nullptr;          // Y1 (Mp x Mp), per call
-    float *qp = nullptr;          // per-column-tile partial q, p  (ntile x 2 x R)
+    float *qp = nullptr;          // per-column-tile partial q, p, s, t  (ntile x 4 x R)
     float *gpart = nullptr;       // split-K partial G            (nsplit x Mp x Mp)
     int nsplit = 0;
     int nctile = 0;

@@ -18,14 +18,17 @@
 // and W^T row b by 1/sw_b, an upper bound of max_r |W[r][b]| from the maxima
 // of alpha, beta, F and U.
 //
-// Kernel anatomy (k_gemm_tc): one CTA = one 128 x BN output tile, 128 threads.
+// Stage B kernel (k_gemm_tc): one CTA = one 128 x BN split-K output tile,
+// 128 threads.
 //   warp 0 lane 0  TMA producer: cp.async.bulk.tensor 2D loads of the four
 //                  operand tiles (A hi/lo 128x64, B hi/lo BNx64, 128B swizzle)
 //                  into a STAGES-deep ring, completion on mbarrier full[s]
 //   warp 1 lane 0  MMA issuer: 4 K-slices x 3 products per stage, then
 //                  tcgen05.commit -> empty[s]; a final commit -> done
 //   all 4 warps    epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
-//                  32w..32w+31), fused row dots (stage A) or tile store (B)
+//                  32w..32w+31), scaled tile store
+// Stage A kernel (k_stageA_tc): persistent, warp-specialised, accumulators
+// double-buffered in TMEM (described at the kernel).
 // Every mbarrier wait is bounded (clock64 budget); on expiry the kernel sets
 // the context's error flag, drains its own copies and MMAs (bounded again),
 // frees its TMEM and returns.
@@ -43,7 +46,6 @@ constexpr int kBM = 128;          // tile rows (TMEM lanes)
 constexpr int kBK = 64;           // K block: 64 fp16 = one 128-byte swizzle row
 constexpr uint32_t kABytes = kBM * kBK * 2;
 constexpr int kBNB = 128;         // stage B tile width
-constexpr int kStagesA = 2;
 constexpr int kStagesB = 3;
 constexpr int kSplitRows = 2048;  // stage B rows per split (fp32 accumulation length)
 constexpr float kLoScale = 2048.f;
@@ -59,20 +61,16 @@ struct TmaEpi {
     CUtensorMap d, g;
 };
 
+// stage B
 struct GemmArgs {
     // geometry
-    int nkb;            // k-blocks per CTA (stage A); k-blocks per split (stage B)
-    int nkb_total;      // stage B: total k-blocks
+    int nkb;            // k-blocks per split
+    int nkb_total;      // total k-blocks
     long R;             // image rows
     int Mp;             // padded mode count
-    int ldG;            // stage B: leading dimension of the partial tiles
-    int ntile;          // stage B: tiles per dimension
-    // stage A epilogue
-    const float *d32, *g32;       // d and g = f_psi * f rows (R x Mp)
-    const float *vec_s, *vec_t;   // f_Y*R1 and R1/f_psi (Mp)
-    const float *tcol;            // Y1 row scales t_n (Mp)
-    float *qpst;                  // [nct][4][R]
-    // stage B epilogue
+    int ldG;            // leading dimension of the partial tiles
+    int ntile;          // tiles per dimension
+    // epilogue
     const float *su, *sw;         // row scales of U^T and W^T (Mp)
     float *gpart;
     // bounded waits
@@ -214,10 +212,9 @@ __device__ __forceinline__ void tmem_combined(uint32_t lane_base, int col, int b
 }
 
 // ------------------------------------------------------------ the GEMM
-// MODE 0: stage A (row dots epilogue).  MODE 1: stage B (split-K tile store).
-template <int BN, int STAGES, int MODE>
+// Stage B: G = U^T W, split-K partial tiles.
+template <int BN, int STAGES>
 __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQuad tm,
-                                                     const __grid_constant__ TmaEpi te,
                                                      const GemmArgs args) {
     constexpr uint32_t kBBytes = BN * kBK * 2;
     constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
@@ -228,26 +225,15 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * kStageBytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 3);
-    // stage A: per-column factors of this tile (t_n, f_Y R1, R1 / f_psi)
-    float *colv = reinterpret_cast<float *>(tmem_slot + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES),
                    done = smem_u32(bars + 2 * STAGES);
 
     // tile coordinates and K range
-    int arow, brow, kb0, nkb;
-    if (MODE == 0) {
-        arow = blockIdx.y * kBM;
-        brow = blockIdx.x * BN;
-        kb0 = 0;
-        nkb = args.nkb;
-    } else {
-        int ta = blockIdx.x / args.ntile, tb = blockIdx.x % args.ntile;
-        arow = ta * kBM;
-        brow = tb * BN;
-        kb0 = blockIdx.y * args.nkb;
-        nkb = min(args.nkb, args.nkb_total - kb0);
-    }
+    const int ta = blockIdx.x / args.ntile, tb = blockIdx.x % args.ntile;
+    const int arow = ta * kBM, brow = tb * BN;
+    const int kb0 = blockIdx.y * args.nkb;
+    const int nkb = min(args.nkb, args.nkb_total - kb0);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -255,18 +241,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
             mbar_init(empty0 + 8 * s, 1);
         }
         mbar_init(done, 1);
-        mbar_init(done + 8, 1);
-        mbar_init(done + 16, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    if (MODE == 0) {
-        for (int c = threadIdx.x; c < BN; c += blockDim.x) {
-            int n = brow + c;
-            colv[c] = args.tcol[n];
-            colv[BN + c] = args.vec_s[n];
-            colv[2 * BN + c] = args.vec_t[n];
-        }
     }
     if (warp == 0) tmem_alloc<kCols>(smem_u32(tmem_slot));
     tc_fence_before();
@@ -337,75 +313,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
     tc_fence_after();
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     const bool have_acc = nkb > 0 && ready;
-    if (MODE == 0) {
-        // The pipeline buffers are free once `done` completed: the d and g row
-        // tiles of this CTA come in through TMA, 64 columns (two 32-column
-        // boxes per tensor, 128-byte swizzle) per part, double buffered.
-        constexpr int kParts = BN / 64;
-        constexpr uint32_t kBox = kBM * 32 * 4;          // one 128 x 32 fp32 box
-        constexpr uint32_t kPartBytes = 4 * kBox;        // d0 d1 g0 g1
-        const uint32_t epi0 = done + 8;
-        const int row_in = warp * 32 + lane;
-        const long row = (long)arow + row_in;
-        auto issue = [&](int part) {
-            uint32_t buf = smem_u32(smem + (part & 1) * kPartBytes);
-            uint32_t bar = epi0 + 8 * (part & 1);
-            int x = brow + part * 64;
-            mbar_expect_tx(bar, kPartBytes);
-            tma_load_2d(buf, &te.d, bar, x, arow);
-            tma_load_2d(buf + kBox, &te.d, bar, x + 32, arow);
-            tma_load_2d(buf + 2 * kBox, &te.g, bar, x, arow);
-            tma_load_2d(buf + 3 * kBox, &te.g, bar, x + 32, arow);
-        };
-        if (threadIdx.x == 0 && have_acc) {
-            issue(0);
-            if (kParts > 1) issue(1);
-        }
-        float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
-#pragma unroll 1
-        for (int part = 0; part < kParts; ++part) {
-            bool landed = have_acc && mbar_wait(epi0 + 8 * (part & 1), (part >> 1) & 1, budget);
-            if (have_acc && !landed && lane == 0) *(volatile int *)args.err = 3;
-            const uint8_t *buf = smem + (part & 1) * kPartBytes;
-#pragma unroll 1
-            for (int half = 0; half < 2; ++half) {
-                float v[32];
-                tmem_combined(lane_base, part * 64 + half * 32, BN, v);
-                if (landed) {
-                    const uint8_t *bd = buf + half * kBox + row_in * 128;
-                    const uint8_t *bg = buf + (2 + half) * kBox + row_in * 128;
-                    const int sw = row_in & 7;
-#pragma unroll
-                    for (int ch = 0; ch < 8; ++ch) {
-                        float4 d4 = *reinterpret_cast<const float4 *>(bd + ((ch ^ sw) << 4));
-                        float4 g4 = *reinterpret_cast<const float4 *>(bg + ((ch ^ sw) << 4));
-                        float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            int j = 4 * ch + e, c = part * 64 + half * 32 + j;
-                            float vv = v[j] * colv[c];
-                            q = fmaf(dd[e], vv, q);
-                            p = fmaf(gg[e], vv, p);
-                            sacc = fmaf(colv[BN + c], dd[e], sacc);
-                            tacc = fmaf(colv[2 * BN + c], gg[e], tacc);
-                        }
-                    }
-                }
-            }
-            if (part + 2 < kParts) {
-                __syncthreads();                       // everyone is done with this buffer
-                if (threadIdx.x == 0 && have_acc) issue(part + 2);
-            }
-        }
-        if (row < args.R) {
-            long R = args.R;
-            float *o = args.qpst + (long)blockIdx.x * 4 * R;
-            o[row] = q;
-            o[R + row] = p;
-            o[2 * R + row] = sacc;
-            o[3 * R + row] = tacc;
-        }
-    } else {
+    {
         long a = arow + warp * 32 + lane;
         float sa = a < args.Mp ? args.su[a] : 0.f;
         float *dst = args.gpart + (long)blockIdx.y * args.ldG * args.ldG + a * args.ldG + brow;
@@ -436,6 +344,334 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQ
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc<kCols>(tmem);
+}
+
+// ------------------------------------------------- persistent stage A
+// One CTA per SM walks a contiguous range of the 128 x 128 tiles of V = D Y1
+// (row tile major, column tile minor): the first column tile of a row block
+// pulls its A rows from HBM and the others re-read them from L2, while the
+// SMs work on row blocks far apart (no two SMs waiting on the same misses).
+// Warp roles:
+//   warps 0-3  epilogue: warp w owns TMEM lanes (tile rows) 32w..32w+31
+//   warp 4     TMA producer of the operand ring
+//   warp 5     MMA issuer (and TMEM owner)
+// D0 / D1 of a tile take 2 x 128 TMEM columns; two tiles' accumulators are
+// resident (512 columns), so the epilogue of tile i (TMEM reads and the
+// q, p, s, t row dots) runs while the MMAs of tile i+1 fill the other half.
+// The epilogue's d and g rows come in by TMA in 16-column parts (64-byte
+// swizzle) through a two-part ring that its leader thread keeps two parts
+// ahead, across tiles; that keeps the operand ring at three 64 KB stages.
+// Every wait is bounded; a failed wait sets the error flag and a shared
+// abort flag that ends the other roles' loops, in-flight copies and MMAs are
+// drained (bounded again) and the TMEM is freed before the CTA exits.
+constexpr int kPBN = 128;                                   // tile columns
+constexpr int kPBK = kBK;                                   // K block: one 128-byte swizzle row
+constexpr int kPStages = 3;
+constexpr uint32_t kPLimbA = kBM * kPBK * 2;                // 16 KB
+constexpr uint32_t kPLimbB = kPBN * kPBK * 2;               // 16 KB
+constexpr uint32_t kPStageBytes = 2 * kPLimbA + 2 * kPLimbB;   // 64 KB
+constexpr int kPEpiCols = 16;                               // columns per epilogue part
+constexpr uint32_t kPEpiBox = kBM * kPEpiCols * 4;          // 128 rows x 16 fp32
+constexpr uint32_t kPEpiBytes = 2 * kPEpiBox;               // d and g of one part
+constexpr int kPBars = 2 * kPStages + 7;                    // full, empty, tfull[2], tempty[2], efull[2], done
+constexpr size_t kPSmem = 1024 + kPStages * (size_t)kPStageBytes + 2 * (size_t)kPEpiBytes +
+                          3 * kPBN * sizeof(float) + 8 * kPBars + 16;
+static_assert(kPSmem <= 232448, "stage A shared memory above the per-block limit");
+
+struct StageAArgs {
+    long R;
+    int Mp;
+    int nkb;              // k-blocks per tile (Mp / 64)
+    int nct;              // column tiles (ceil(Mp / 128))
+    int b_box;            // rows of one B (Y1) box: min(128, Mp)
+    long ntiles;
+    const float *tcol, *vec_s, *vec_t;
+    float *qpst;          // [nct][4][R]
+    int *err;
+    long long budget;
+};
+
+// Bounded wait that also gives up once another role has raised `abort`.
+__device__ __forceinline__ bool mbar_wait_ab(uint32_t bar, uint32_t parity, long long budget,
+                                             volatile int *abort) {
+    long long t0 = clock64();
+    uint32_t spins = 0;
+    while (!mbar_try(bar, parity)) {
+        if ((++spins & 31u) == 0 && *abort) return false;
+        if (clock64() - t0 > budget) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Named barrier 1 over the 128 epilogue threads; returns true if `pred` was
+// set in any of them.
+__device__ __forceinline__ bool epi_sync_or(bool pred) {
+    uint32_t out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(out)
+        : "r"((uint32_t)pred)
+        : "memory");
+    return out != 0;
+}
+
+__global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ TmaQuad tm,
+                                                       const __grid_constant__ TmaEpi te,
+                                                       const StageAArgs args) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *epi = smem + kPStages * kPStageBytes;
+    float *colv = reinterpret_cast<float *>(epi + 2 * kPEpiBytes);   // [3][kPBN]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(colv + 3 * kPBN);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kPBars);
+    volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * kPStages,
+                   tfull0 = empty0 + 8 * kPStages, tempty0 = tfull0 + 16, efull0 = tempty0 + 16,
+                   done = efull0 + 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long budget = args.budget;
+    const long G = gridDim.x;
+    // this CTA's tiles: [t0, t0 + nloc), an even split of the tile sequence
+    const long t0 = args.ntiles * blockIdx.x / G;
+    const long nloc = args.ntiles * (blockIdx.x + 1) / G - t0;
+    const int nct = args.nct, Mp = args.Mp;
+    const uint32_t b_bytes = (uint32_t)args.b_box * kPBK * 2;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kPStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int j = 0; j < 2; ++j) {
+            mbar_init(tfull0 + 8 * j, 1);
+            mbar_init(tempty0 + 8 * j, 128);
+            mbar_init(efull0 + 8 * j, 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 5) tmem_alloc<512>(smem_u32(tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    int fail_code = 0;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            // ---- TMA producer: the operand ring, continuous across tiles
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long t = t0 + i;
+                int arow = (int)(t / nct) * kBM, brow = (int)(t % nct) * kPBN;
+                for (int kb = 0; kb < args.nkb; ++kb, ++g) {
+                    int s = (int)(g % kPStages);
+                    uint32_t n = (uint32_t)(g / kPStages);
+                    if (g >= kPStages && !mbar_wait_ab(empty0 + 8 * s, (n & 1) ^ 1, budget, abort)) {
+                        fail_code = 1;
+                        break;
+                    }
+                    uint32_t base = smem_u32(smem + s * kPStageBytes);
+                    uint32_t bar = full0 + 8 * s;
+                    int kx = kb * kPBK;
+                    mbar_expect_tx(bar, 2 * kPLimbA + 2 * b_bytes);
+                    tma_load_2d(base, &tm.a_hi, bar, kx, arow);
+                    tma_load_2d(base + kPLimbA, &tm.a_lo, bar, kx, arow);
+                    tma_load_2d(base + 2 * kPLimbA, &tm.b_hi, bar, kx, brow);
+                    tma_load_2d(base + 2 * kPLimbA + kPLimbB, &tm.b_lo, bar, kx, brow);
+                }
+            }
+            if (fail_code) {
+                *abort = 1;
+                // every issued stage must land before the CTA exits
+                for (long gg = g > kPStages ? g - kPStages : 0; gg < g; ++gg)
+                    mbar_wait(full0 + 8 * (int)(gg % kPStages), (uint32_t)(gg / kPStages) & 1,
+                              kDefaultBudget);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // ---- MMA issuer: D0 += hi*hi, D1 += hi*lo + lo*hi, tile i into
+            // TMEM half (i & 1)
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long t = t0 + i;
+                int brow = (int)(t % nct) * kPBN;
+                int ncols = min(kPBN, Mp - brow);
+                const uint32_t idesc = idesc_f16(kBM, ncols);
+                int j = (int)(i & 1);
+                uint32_t u = (uint32_t)(i >> 1);
+                if (i >= 2 && !mbar_wait_ab(tempty0 + 8 * j, (u - 1) & 1, budget, abort)) {
+                    fail_code = 2;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d0 = tmem + 256 * j, d1 = d0 + 128;
+                for (int kb = 0; kb < args.nkb; ++kb, ++g) {
+                    int s = (int)(g % kPStages);
+                    uint32_t n = (uint32_t)(g / kPStages);
+                    if (!mbar_wait_ab(full0 + 8 * s, n & 1, budget, abort)) {
+                        fail_code = 2;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint32_t base = smem_u32(smem + s * kPStageBytes);
+#pragma unroll
+                    for (int kk = 0; kk < kPBK / 16; ++kk) {
+                        uint64_t ah = sdesc_sw128(base + kk * 32);
+                        uint64_t al = sdesc_sw128(base + kPLimbA + kk * 32);
+                        uint64_t bh = sdesc_sw128(base + 2 * kPLimbA + kk * 32);
+                        uint64_t bl = sdesc_sw128(base + 2 * kPLimbA + kPLimbB + kk * 32);
+                        uint32_t acc = (kb | kk) != 0;
+                        mma_f16(d0, ah, bh, idesc, acc);
+                        mma_f16(d1, ah, bl, idesc, acc);
+                        mma_f16(d1, al, bh, idesc, 1);
+                    }
+                    mma_commit(empty0 + 8 * s);
+                }
+                if (fail_code) break;
+                mma_commit(tfull0 + 8 * j);
+            }
+            if (fail_code) *abort = 1;
+            mma_commit(done);   // tracks every MMA issued, also after a failure
+        }
+    } else {
+        // ---- epilogue (warps 0-3): thread = tile row = TMEM lane
+        const int row_in = warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        const bool leader = threadIdx.x == 0;
+        // leader's cursor over the (tile, part) sequence of epilogue loads
+        long iss_i = 0, issued = 0;
+        int iss_p = 0;
+        auto issue_next = [&]() {
+            if (iss_i >= nloc) return;
+            long t = t0 + iss_i;
+            int arow = (int)(t / nct) * kBM, brow = (int)(t % nct) * kPBN;
+            int e = (int)(issued & 1);
+            uint32_t buf = smem_u32(epi + e * kPEpiBytes), bar = efull0 + 8 * e;
+            int x = brow + iss_p * kPEpiCols;
+            mbar_expect_tx(bar, kPEpiBytes);
+            tma_load_2d(buf, &te.d, bar, x, arow);
+            tma_load_2d(buf + kPEpiBox, &te.g, bar, x, arow);
+            ++issued;
+            if (++iss_p == min(kPBN, Mp - brow) / kPEpiCols) {
+                iss_p = 0;
+                ++iss_i;
+            }
+        };
+        if (leader) {
+            issue_next();
+            issue_next();
+        }
+        long consumed = 0;
+        for (long i = 0; i < nloc; ++i) {
+            long t = t0 + i;
+            const int ct = (int)(t % nct);
+            const int brow = ct * kPBN;
+            const long row = (long)(t / nct) * kBM + row_in;
+            const int np = min(kPBN, Mp - brow) / 32;   // 32-column TMEM chunks
+            const int j = (int)(i & 1);
+            const uint32_t u = (uint32_t)(i >> 1);
+            // column factors of this tile; the previous tile's last reads of
+            // them came before its last part barrier
+            float *cv = colv;
+            {
+                int c = brow + row_in;
+                bool in = c < Mp;
+                cv[row_in] = in ? args.tcol[c] : 0.f;
+                cv[kPBN + row_in] = in ? args.vec_s[c] : 0.f;
+                cv[2 * kPBN + row_in] = in ? args.vec_t[c] : 0.f;
+            }
+            bool ok = mbar_wait_ab(tfull0 + 8 * j, u & 1, budget, abort);
+            __syncwarp();
+            if (epi_sync_or(!ok)) {   // also publishes cv to the other warps
+                fail_code = 3;
+                break;
+            }
+            tc_fence_after();
+            float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
+            for (int chunk = 0; chunk < np; ++chunk) {
+                float v[32];
+                tmem_combined(lane_base + 256 * j, chunk * 32, 128, v);
+                if (chunk == np - 1) {
+                    // this tile's accumulators are read: release the TMEM half
+                    tc_fence_before();
+                    mbar_arrive(tempty0 + 8 * j);
+                }
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    const int e = (int)(consumed & 1);
+                    bool landed = mbar_wait_ab(efull0 + 8 * e, (uint32_t)(consumed >> 1) & 1,
+                                               budget, abort);
+                    __syncwarp();
+                    if (epi_sync_or(!landed)) {
+                        fail_code = 3;
+                        break;
+                    }
+                    // 64-byte rows, 16-byte granule c stored at c ^ ((row >> 1) & 3)
+                    const uint8_t *bd = epi + e * kPEpiBytes + row_in * 64;
+                    const uint8_t *bg = bd + kPEpiBox;
+                    const int sw = (row_in >> 1) & 3;
+                    const float *cp = cv + chunk * 32 + half * 16;
+#pragma unroll
+                    for (int ch = 0; ch < 4; ++ch) {
+                        float4 d4 = *reinterpret_cast<const float4 *>(bd + ((ch ^ sw) << 4));
+                        float4 g4 = *reinterpret_cast<const float4 *>(bg + ((ch ^ sw) << 4));
+                        float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            int c = 4 * ch + k;
+                            float vv = v[half * 16 + c] * cp[c];
+                            q = fmaf(dd[k], vv, q);
+                            p = fmaf(gg[k], vv, p);
+                            sacc = fmaf(cp[kPBN + c], dd[k], sacc);
+                            tacc = fmaf(cp[2 * kPBN + c], gg[k], tacc);
+                        }
+                    }
+                    ++consumed;
+                    // every epilogue thread is done with buffer e: refill it
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    if (leader) issue_next();
+                }
+                if (fail_code) break;
+            }
+            if (fail_code) break;
+            if (row < args.R) {
+                const long R = args.R;
+                float *o = args.qpst + (long)ct * 4 * R;
+                o[row] = q;
+                o[R + row] = p;
+                o[2 * R + row] = sacc;
+                o[3 * R + row] = tacc;
+            }
+        }
+        if (fail_code) {
+            *abort = 1;
+            if (leader)
+                for (long k = consumed; k < issued; ++k)
+                    mbar_wait(efull0 + 8 * (int)(k & 1), (uint32_t)(k >> 1) & 1, kDefaultBudget);
+        }
+    }
+    if (fail_code && lane == 0) *(volatile int *)args.err = fail_code;
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 5) {
+        // every MMA has completed before the TMEM is freed
+        mbar_wait(done, 0, kDefaultBudget);
+        __syncwarp();
+        tc_fence_after();
+        tmem_dealloc<512>(tmem);
+    }
 }
 
 // --------------------------------------------------------- data movers
@@ -827,7 +1063,7 @@ static int make_map(CUtensorMap *m, const void *base, uint64_t inner, uint64_t o
     return TDSCHA_OK;
 }
 
-// 2D fp32 tensor (inner x outer), box 32 x 128, 128-byte swizzle.
+// 2D fp32 tensor (inner x outer), box 16 x 128, 64-byte swizzle.
 static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer) {
     auto fn = encode_fn();
     if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return TDSCHA_ERR_CUDA; }
@@ -837,10 +1073,10 @@ static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64
     }
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * 4};
-    cuuint32_t box[2] = {32, (cuuint32_t)kBM};
+    cuuint32_t box[2] = {(cuuint32_t)kPEpiCols, (cuuint32_t)kBM};
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides,
-                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled (fp32) failed (%d)", (int)r); return TDSCHA_ERR_CUDA; }
     return TDSCHA_OK;
@@ -849,15 +1085,7 @@ static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64
 template <int BN, int STAGES>
 static constexpr size_t gemm_smem() {
     return 1024 + STAGES * (2 * (size_t)kABytes + 2 * (size_t)BN * kBK * 2) + 8 * (2 * STAGES + 3) +
-           16 + 3 * 4 * (size_t)BN;
-}
-
-// Stage A column tile: the widest multiple of 64 (<= 192) dividing Mp.
-static int choose_bn(int Mp) {
-    int k = Mp / 64;
-    for (int c = 3; c >= 1; --c)
-        if (k % c == 0) return 64 * c;
-    return 64;
+           16;
 }
 
 struct MixedExtra {
@@ -871,6 +1099,7 @@ struct MixedExtra {
     float *fpart = nullptr;
     int nfchunk = 0;
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
+    int nsm = 1;
     long long budget = kDefaultBudget;
 };
 
@@ -887,8 +1116,14 @@ int mixed_prepare(tdscha_ctx *c) {
     MixedExtra *x = new MixedExtra();
     mx.tmaps = x;
     if (const char *b = getenv("TDSCHA_WAIT_BUDGET_CYCLES")) x->budget = atoll(b);
-    x->bnA = choose_bn(Mp);
-    mx.nctile = Mp / x->bnA;
+    x->bnA = std::min(kPBN, Mp);
+    mx.nctile = ceil_div(Mp, kPBN);
+    {
+        int dev = 0, nsm = 0;
+        TDS_CUDA(cudaGetDevice(&dev));
+        TDS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        x->nsm = std::max(1, nsm);
+    }
     x->ldG = ((Mp + kBM - 1) / kBM) * kBM;
     x->ntB = x->ldG / kBM;
     x->nkbB = (int)(Rp / kBK);
@@ -974,16 +1209,9 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_TRY(make_map_f32(&x->te.g, mx.g32, Mp, R));
     static bool attr_done = false;
     if (!attr_done) {
-        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<192, kStagesA, 0>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)gemm_smem<192, kStagesA>()));
-        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<128, kStagesA, 0>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)gemm_smem<128, kStagesA>()));
-        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<64, kStagesA, 0>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)gemm_smem<64, kStagesA>()));
-        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<kBNB, kStagesB, 1>,
+        TDS_CUDA(cudaFuncSetAttribute(k_stageA_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kPSmem));
+        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<kBNB, kStagesB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)gemm_smem<kBNB, kStagesB>()));
         attr_done = true;
@@ -1034,32 +1262,23 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
                                       mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax);
         TDS_CHECK_LAUNCH();
     }
-    GemmArgs ga{};
-    ga.nkb = Mp / kBK;
+    StageAArgs ga{};
     ga.R = R;
     ga.Mp = Mp;
-    ga.d32 = x->d32;
-    ga.g32 = mx.g32;
+    ga.nkb = Mp / kPBK;
+    ga.nct = mx.nctile;
+    ga.b_box = x->bnA;
+    ga.ntiles = (long)ceil_div(R, kBM) * mx.nctile;
+    ga.tcol = x->tcol;
     ga.vec_s = x->vs;
     ga.vec_t = x->vt;
-    ga.tcol = x->tcol;
     ga.qpst = mx.qp;
     ga.err = err_dev;
     ga.budget = x->budget;
     {
         ProfScope ps(c, 0, st);
-        dim3 grid(mx.nctile, ceil_div(R, kBM));
-        switch (x->bnA) {
-            case 192:
-                k_gemm_tc<192, kStagesA, 0><<<grid, 128, gemm_smem<192, kStagesA>(), st>>>(x->tmA, x->te, ga);
-                break;
-            case 128:
-                k_gemm_tc<128, kStagesA, 0><<<grid, 128, gemm_smem<128, kStagesA>(), st>>>(x->tmA, x->te, ga);
-                break;
-            default:
-                k_gemm_tc<64, kStagesA, 0><<<grid, 128, gemm_smem<64, kStagesA>(), st>>>(x->tmA, x->te, ga);
-                break;
-        }
+        int grid = (int)std::min<long>(ga.ntiles, x->nsm);
+        k_stageA_tc<<<grid, 192, kPSmem, st>>>(x->tmA, x->te, ga);
         TDS_CHECK_LAUNCH();
     }
     {
@@ -1090,7 +1309,7 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 3, st);
         dim3 grid(x->ntB * x->ntB, mx.nsplit);
-        k_gemm_tc<kBNB, kStagesB, 1><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, x->te, gb);
+        k_gemm_tc<kBNB, kStagesB><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, gb);
         TDS_CHECK_LAUNCH();
     }
     {
