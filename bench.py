@@ -351,8 +351,8 @@ def run_ours(args):
                 roof["frac_incl_split"] = roof["tensor_work_incl_split_tflops"] / peak
                 # DRAM bytes per launch from the ncu captures of the same kernels
                 # at N=20 000 (profiles/k_stageA_tc_m573_n20k.md for stage A,
-                # profiles/k_gemm_tc_m573_n20k.md for stage B), scaled by image rows
-                per_row = {0: 144.9e6 / 20000, 3: 95.9e6 / 20000}[kid]
+                # profiles/k_stageB_tc_m573_n20k.md for stage B), scaled by image rows
+                per_row = {0: 144.9e6 / 20000, 3: 96.0e6 / 20000}[kid]
                 if M == 573:
                     roof["traffic"] = per_row * R
                     roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"

@@ -18,20 +18,20 @@
 // and W^T row b by 1/sw_b, an upper bound of max_r |W[r][b]| from the maxima
 // of alpha, beta, F and U.
 //
-// Stage B kernel (k_gemm_tc): one CTA = one 128 x BN split-K output tile,
-// 128 threads.
-//   warp 0 lane 0  TMA producer: cp.async.bulk.tensor 2D loads of the four
-//                  operand tiles (A hi/lo 128x64, B hi/lo BNx64, 128B swizzle)
-//                  into a STAGES-deep ring, completion on mbarrier full[s]
-//   warp 1 lane 0  MMA issuer: 4 K-slices x 3 products per stage, then
-//                  tcgen05.commit -> empty[s]; a final commit -> done
-//   all 4 warps    epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
-//                  32w..32w+31), scaled tile store
-// Stage A kernel (k_stageA_tc): persistent, warp-specialised, accumulators
-// double-buffered in TMEM (described at the kernel).
+// Kernel anatomy (k_stageA_tc, k_stageB_tc): persistent, one CTA per SM,
+// 192 threads, accumulators double-buffered in TMEM.
+//   warp 4 lane 0  TMA producer: cp.async.bulk.tensor 2D loads of the four
+//                  operand tiles (A hi/lo 128x64, B hi/lo 128x64, 128B swizzle)
+//                  into a 3-stage ring, completion on mbarrier full[s]
+//   warp 5 lane 0  MMA issuer: 4 K-slices x 3 products per stage, then
+//                  tcgen05.commit -> empty[s]; per tile a commit -> tfull[j]
+//   warps 0-3      epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
+//                  32w..32w+31) from TMEM half j while the next tile's MMAs
+//                  fill the other half; fused row dots (A) or tile store (B)
 // Every mbarrier wait is bounded (clock64 budget); on expiry the kernel sets
-// the context's error flag, drains its own copies and MMAs (bounded again),
-// frees its TMEM and returns.
+// the context's error flag and a shared abort flag that ends the other roles'
+// loops, drains its own copies and MMAs (bounded again), frees its TMEM and
+// returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
@@ -46,7 +46,6 @@ constexpr int kBM = 128;          // tile rows (TMEM lanes)
 constexpr int kBK = 64;           // K block: 64 fp16 = one 128-byte swizzle row
 constexpr uint32_t kABytes = kBM * kBK * 2;
 constexpr int kBNB = 128;         // stage B tile width
-constexpr int kStagesB = 3;
 constexpr int kSplitRows = 2048;  // stage B rows per split (fp32 accumulation length)
 constexpr float kLoScale = 2048.f;
 constexpr float kLoInv = 1.f / 2048.f;
@@ -61,22 +60,6 @@ struct TmaEpi {
     CUtensorMap d, g;
 };
 
-// stage B
-struct GemmArgs {
-    // geometry
-    int nkb;            // k-blocks per split
-    int nkb_total;      // total k-blocks
-    long R;             // image rows
-    int Mp;             // padded mode count
-    int ldG;            // leading dimension of the partial tiles
-    int ntile;          // tiles per dimension
-    // epilogue
-    const float *su, *sw;         // row scales of U^T and W^T (Mp)
-    float *gpart;
-    // bounded waits
-    int *err;
-    long long budget;
-};
 
 // ------------------------------------------------------------------ PTX
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -196,11 +179,6 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
                  : "memory");
 }
 
-template <int N>
-struct TmemCols {
-    static constexpr int value = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : N <= 256 ? 256 : 512;
-};
-
 // D0 + 2^-11 D1 for 32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_combined(uint32_t lane_base, int col, int bn, float (&o)[32]) {
     uint32_t v0[32], v1[32];
@@ -209,141 +187,6 @@ __device__ __forceinline__ void tmem_combined(uint32_t lane_base, int col, int b
     tmem_wait_ld();
 #pragma unroll
     for (int j = 0; j < 32; ++j) o[j] = fmaf(__uint_as_float(v1[j]), kLoInv, __uint_as_float(v0[j]));
-}
-
-// ------------------------------------------------------------ the GEMM
-// Stage B: G = U^T W, split-K partial tiles.
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ TmaQuad tm,
-                                                     const GemmArgs args) {
-    constexpr uint32_t kBBytes = BN * kBK * 2;
-    constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
-    constexpr int kCols = TmemCols<2 * BN>::value;
-    constexpr uint32_t kIdesc = idesc_f16(kBM, BN);
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = reinterpret_cast<uint8_t *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * kStageBytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 3);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES),
-                   done = smem_u32(bars + 2 * STAGES);
-
-    // tile coordinates and K range
-    const int ta = blockIdx.x / args.ntile, tb = blockIdx.x % args.ntile;
-    const int arow = ta * kBM, brow = tb * BN;
-    const int kb0 = blockIdx.y * args.nkb;
-    const int nkb = min(args.nkb, args.nkb_total - kb0);
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
-        }
-        mbar_init(done, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    if (warp == 0) tmem_alloc<kCols>(smem_u32(tmem_slot));
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    const long long budget = args.budget;
-    bool failed = false;
-    if (warp == 0 && lane == 0) {
-        // ---- TMA producer
-        int issued = 0;
-        for (int i = 0; i < nkb; ++i) {
-            int s = i % STAGES;
-            if (i >= STAGES && !mbar_wait(empty0 + 8 * s, ((i / STAGES) & 1) ^ 1, budget)) {
-                failed = true;
-                break;
-            }
-            uint32_t base = smem_u32(smem + s * kStageBytes);
-            uint32_t bar = full0 + 8 * s;
-            int kx = (kb0 + i) * kBK;
-            mbar_expect_tx(bar, kStageBytes);
-            tma_load_2d(base, &tm.a_hi, bar, kx, arow);
-            tma_load_2d(base + kABytes, &tm.a_lo, bar, kx, arow);
-            tma_load_2d(base + 2 * kABytes, &tm.b_hi, bar, kx, brow);
-            tma_load_2d(base + 2 * kABytes + kBBytes, &tm.b_lo, bar, kx, brow);
-            issued = i + 1;
-        }
-        if (failed) {
-            // drain: every issued stage must land before the CTA exits
-            for (int i = max(0, issued - STAGES); i < issued; ++i)
-                mbar_wait(full0 + 8 * (i % STAGES), (i / STAGES) & 1, kDefaultBudget);
-        }
-    } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer: D0 += hi*hi, D1 += hi*lo + lo*hi
-        const uint32_t d0 = tmem, d1 = tmem + BN;
-        for (int i = 0; i < nkb; ++i) {
-            int s = i % STAGES;
-            if (!mbar_wait(full0 + 8 * s, (i / STAGES) & 1, budget)) {
-                failed = true;
-                break;
-            }
-            tc_fence_after();
-            uint32_t base = smem_u32(smem + s * kStageBytes);
-#pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
-                uint64_t ah = sdesc_sw128(base + kk * 32);
-                uint64_t al = sdesc_sw128(base + kABytes + kk * 32);
-                uint64_t bh = sdesc_sw128(base + 2 * kABytes + kk * 32);
-                uint64_t bl = sdesc_sw128(base + 2 * kABytes + kBBytes + kk * 32);
-                uint32_t acc = (i | kk) != 0;
-                mma_f16(d0, ah, bh, kIdesc, acc);
-                mma_f16(d1, ah, bl, kIdesc, acc);
-                mma_f16(d1, al, bh, kIdesc, 1);
-            }
-            mma_commit(empty0 + 8 * s);
-        }
-        mma_commit(done);   // also after a failure: tracks the MMAs already issued
-    }
-    if (failed) *(volatile int *)args.err = 1;
-    __syncwarp();
-
-    // ---- epilogue
-    bool ready = mbar_wait(done, 0, budget);
-    if (!ready) {
-        if (lane == 0) *(volatile int *)args.err = 2;
-        ready = mbar_wait(done, 0, kDefaultBudget);   // MMAs must finish before dealloc
-    }
-    tc_fence_after();
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    const bool have_acc = nkb > 0 && ready;
-    {
-        long a = arow + warp * 32 + lane;
-        float sa = a < args.Mp ? args.su[a] : 0.f;
-        float *dst = args.gpart + (long)blockIdx.y * args.ldG * args.ldG + a * args.ldG + brow;
-#pragma unroll 1
-        for (int ch = 0; ch < BN / 32; ++ch) {
-            float v[32];
-            tmem_combined(lane_base, ch * 32, BN, v);
-            float4 *d4 = reinterpret_cast<float4 *>(dst + ch * 32);
-            int c0 = brow + ch * 32;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (have_acc) {
-                    int c = c0 + 4 * j;
-                    float s0 = c < args.Mp ? args.sw[c] : 0.f;
-                    float s1 = c + 1 < args.Mp ? args.sw[c + 1] : 0.f;
-                    float s2 = c + 2 < args.Mp ? args.sw[c + 2] : 0.f;
-                    float s3 = c + 3 < args.Mp ? args.sw[c + 3] : 0.f;
-                    o.x = v[4 * j] * sa * s0;
-                    o.y = v[4 * j + 1] * sa * s1;
-                    o.z = v[4 * j + 2] * sa * s2;
-                    o.w = v[4 * j + 3] * sa * s3;
-                }
-                d4[j] = o;
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc<kCols>(tmem);
 }
 
 // ------------------------------------------------- persistent stage A
@@ -667,6 +510,208 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
     __syncthreads();
     if (warp == 5) {
         // every MMA has completed before the TMEM is freed
+        mbar_wait(done, 0, kDefaultBudget);
+        __syncwarp();
+        tc_fence_after();
+        tmem_dealloc<512>(tmem);
+    }
+}
+
+// ------------------------------------------------- persistent stage B
+// G = U^T W as split-K partial tiles: work item w = (split, tile), tile a
+// 128 x 128 block of the ldG x ldG output, split a range of kbps K blocks.
+// One CTA per SM takes items blockIdx.x, blockIdx.x + G, ... (round robin, so
+// the SMs work on neighbouring items of the same split at the same time and
+// share its U^T and W^T rows in L2).  Same roles as stage A: warps 0-3 write
+// the scaled partial tile of item i from one TMEM half while warp 5 runs the
+// MMAs of item i+1 into the other; warp 4 keeps the 3-stage operand ring
+// full across items.  Bounded waits and the abort flag as in stage A.
+constexpr int kQStages = 3;
+constexpr uint32_t kQStageBytes = 2 * kABytes + 2 * kBNB * kBK * 2;   // 64 KB
+constexpr int kQBars = 2 * kQStages + 5;   // full, empty, tfull[2], tempty[2], done
+constexpr size_t kQSmem = 1024 + kQStages * (size_t)kQStageBytes + 2 * kBNB * sizeof(float) +
+                          8 * kQBars + 16;
+static_assert(kQSmem <= 232448, "stage B shared memory above the per-block limit");
+
+struct StageBArgs {
+    int nkb;              // K blocks per split
+    int nkb_total;        // K blocks in all
+    int Mp;
+    int ldG;              // leading dimension of the partial tiles
+    int ntile;            // tiles per dimension (ldG / 128)
+    long nitems;          // ntile^2 x nsplit
+    const float *su, *sw; // row scales of U^T and W^T (Mp)
+    float *gpart;         // [nsplit][ldG][ldG]
+    int *err;
+    long long budget;
+};
+
+__global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ TmaQuad tm,
+                                                       const StageBArgs args) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    float *colv = reinterpret_cast<float *>(smem + kQStages * kQStageBytes);   // [2][kBNB]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(colv + 2 * kBNB);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kQBars);
+    volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * kQStages,
+                   tfull0 = empty0 + 8 * kQStages, tempty0 = tfull0 + 16, done = tempty0 + 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long budget = args.budget;
+    const long G = gridDim.x;
+    const long nloc = args.nitems > (long)blockIdx.x ? (args.nitems - 1 - blockIdx.x) / G + 1 : 0;
+    const int tiles = args.ntile * args.ntile;
+    constexpr uint32_t kIdesc = idesc_f16(kBM, kBNB);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kQStages; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int j = 0; j < 2; ++j) {
+            mbar_init(tfull0 + 8 * j, 1);
+            mbar_init(tempty0 + 8 * j, 128);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 5) tmem_alloc<512>(smem_u32(tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    int fail_code = 0;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            // ---- TMA producer
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long w = blockIdx.x + i * G;
+                int split = (int)(w / tiles), tile = (int)(w % tiles);
+                int arow = (tile / args.ntile) * kBM, brow = (tile % args.ntile) * kBNB;
+                int kb0 = split * args.nkb, nkb = min(args.nkb, args.nkb_total - kb0);
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    int s = (int)(g % kQStages);
+                    uint32_t n = (uint32_t)(g / kQStages);
+                    if (g >= kQStages && !mbar_wait_ab(empty0 + 8 * s, (n & 1) ^ 1, budget, abort)) {
+                        fail_code = 1;
+                        break;
+                    }
+                    uint32_t base = smem_u32(smem + s * kQStageBytes);
+                    uint32_t bar = full0 + 8 * s;
+                    int kx = (kb0 + kb) * kBK;
+                    mbar_expect_tx(bar, kQStageBytes);
+                    tma_load_2d(base, &tm.a_hi, bar, kx, arow);
+                    tma_load_2d(base + kABytes, &tm.a_lo, bar, kx, arow);
+                    tma_load_2d(base + 2 * kABytes, &tm.b_hi, bar, kx, brow);
+                    tma_load_2d(base + 2 * kABytes + kBNB * kBK * 2, &tm.b_lo, bar, kx, brow);
+                }
+            }
+            if (fail_code) {
+                *abort = 1;
+                for (long gg = g > kQStages ? g - kQStages : 0; gg < g; ++gg)
+                    mbar_wait(full0 + 8 * (int)(gg % kQStages), (uint32_t)(gg / kQStages) & 1,
+                              kDefaultBudget);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // ---- MMA issuer: item i into TMEM half (i & 1)
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long w = blockIdx.x + i * G;
+                int split = (int)(w / tiles);
+                int kb0 = split * args.nkb, nkb = min(args.nkb, args.nkb_total - kb0);
+                int j = (int)(i & 1);
+                uint32_t u = (uint32_t)(i >> 1);
+                if (i >= 2 && !mbar_wait_ab(tempty0 + 8 * j, (u - 1) & 1, budget, abort)) {
+                    fail_code = 2;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d0 = tmem + 256 * j, d1 = d0 + 128;
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    int s = (int)(g % kQStages);
+                    uint32_t n = (uint32_t)(g / kQStages);
+                    if (!mbar_wait_ab(full0 + 8 * s, n & 1, budget, abort)) {
+                        fail_code = 2;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint32_t base = smem_u32(smem + s * kQStageBytes);
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; ++kk) {
+                        uint64_t ah = sdesc_sw128(base + kk * 32);
+                        uint64_t al = sdesc_sw128(base + kABytes + kk * 32);
+                        uint64_t bh = sdesc_sw128(base + 2 * kABytes + kk * 32);
+                        uint64_t bl = sdesc_sw128(base + 2 * kABytes + kBNB * kBK * 2 + kk * 32);
+                        uint32_t acc = (kb | kk) != 0;
+                        mma_f16(d0, ah, bh, kIdesc, acc);
+                        mma_f16(d1, ah, bl, kIdesc, acc);
+                        mma_f16(d1, al, bh, kIdesc, 1);
+                    }
+                    mma_commit(empty0 + 8 * s);
+                }
+                if (fail_code) break;
+                mma_commit(tfull0 + 8 * j);
+            }
+            if (fail_code) *abort = 1;
+            mma_commit(done);   // tracks every MMA issued, also after a failure
+        }
+    } else {
+        // ---- epilogue (warps 0-3): thread = tile row = TMEM lane
+        const int row_in = warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (long i = 0; i < nloc; ++i) {
+            long w = blockIdx.x + i * G;
+            int split = (int)(w / tiles), tile = (int)(w % tiles);
+            int arow = (tile / args.ntile) * kBM, brow = (tile % args.ntile) * kBNB;
+            const int j = (int)(i & 1);
+            const uint32_t u = (uint32_t)(i >> 1);
+            // W^T row scales of this tile's columns (two buffers: a thread is at
+            // most one item ahead of the slowest, see the barrier below)
+            float *cv = colv + j * kBNB;
+            {
+                int c = brow + row_in;
+                cv[row_in] = c < args.Mp ? args.sw[c] : 0.f;
+            }
+            const int a = arow + row_in;
+            const float sa = a < args.Mp ? args.su[a] : 0.f;
+            bool ok = mbar_wait_ab(tfull0 + 8 * j, u & 1, budget, abort);
+            __syncwarp();
+            if (epi_sync_or(!ok)) {   // also publishes cv
+                fail_code = 3;
+                break;
+            }
+            tc_fence_after();
+            float *dst = args.gpart + (long)split * args.ldG * args.ldG + (long)a * args.ldG + brow;
+#pragma unroll 1
+            for (int ch = 0; ch < kBNB / 32; ++ch) {
+                float v[32];
+                tmem_combined(lane_base + 256 * j, ch * 32, 128, v);
+                if (ch == kBNB / 32 - 1) {
+                    tc_fence_before();
+                    mbar_arrive(tempty0 + 8 * j);
+                }
+                float4 *d4 = reinterpret_cast<float4 *>(dst + ch * 32);
+                const float *cp = cv + ch * 32;
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    d4[q] = make_float4(v[4 * q] * sa * cp[4 * q], v[4 * q + 1] * sa * cp[4 * q + 1],
+                                        v[4 * q + 2] * sa * cp[4 * q + 2],
+                                        v[4 * q + 3] * sa * cp[4 * q + 3]);
+            }
+        }
+        if (fail_code) *abort = 1;
+    }
+    if (fail_code && lane == 0) *(volatile int *)args.err = fail_code;
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 5) {
         mbar_wait(done, 0, kDefaultBudget);
         __syncwarp();
         tc_fence_after();
@@ -1082,11 +1127,6 @@ static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64
     return TDSCHA_OK;
 }
 
-template <int BN, int STAGES>
-static constexpr size_t gemm_smem() {
-    return 1024 + STAGES * (2 * (size_t)kABytes + 2 * (size_t)BN * kBK * 2) + 8 * (2 * STAGES + 3) +
-           16;
-}
 
 struct MixedExtra {
     TmaQuad tmA, tmB;
@@ -1211,9 +1251,8 @@ int mixed_prepare(tdscha_ctx *c) {
     if (!attr_done) {
         TDS_CUDA(cudaFuncSetAttribute(k_stageA_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)kPSmem));
-        TDS_CUDA(cudaFuncSetAttribute(k_gemm_tc<kBNB, kStagesB>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)gemm_smem<kBNB, kStagesB>()));
+        TDS_CUDA(cudaFuncSetAttribute(k_stageB_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kQSmem));
         attr_done = true;
     }
     TDS_CUDA(cudaDeviceSynchronize());
@@ -1294,13 +1333,13 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
                                     mx.wt_hi, mx.wt_lo, x->sw, x->fpart);
         TDS_CHECK_LAUNCH();
     }
-    GemmArgs gb{};
+    StageBArgs gb{};
     gb.nkb = x->kbps;
     gb.nkb_total = x->nkbB;
-    gb.R = R;
     gb.Mp = Mp;
     gb.ldG = x->ldG;
     gb.ntile = x->ntB;
+    gb.nitems = (long)x->ntB * x->ntB * mx.nsplit;
     gb.su = x->su;
     gb.sw = x->sw;
     gb.gpart = mx.gpart;
@@ -1308,8 +1347,8 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     gb.budget = x->budget;
     {
         ProfScope ps(c, 3, st);
-        dim3 grid(x->ntB * x->ntB, mx.nsplit);
-        k_gemm_tc<kBNB, kStagesB><<<grid, 128, gemm_smem<kBNB, kStagesB>(), st>>>(x->tmB, gb);
+        int grid = (int)std::min<long>(gb.nitems, x->nsm);
+        k_stageB_tc<<<grid, 192, kQSmem, st>>>(x->tmB, gb);
         TDS_CHECK_LAUNCH();
     }
     {
