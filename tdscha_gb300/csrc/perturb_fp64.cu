@@ -229,10 +229,25 @@ int alloc_fp64_scratch(tdscha_ctx *c) {
     c->nct64 = ceil_div(M, kT);
     int ntile = ceil_div(M, kT);
     int tiles = ntile * ntile;
-    // split-K so that tiles x nsplit fills the 152 SMs about twice, with at
-    // least 64 rows per split
-    int ns = std::max(1, ceil_div(2 * 152, tiles));
-    ns = std::min<long>(ns, std::max<long>(1, R / 64));
+    // split-K: the float64 pipe (about 2 FMA per cycle per SM) bounds stage B,
+    // so every SM should get the same share of tiles x splits.  At least two
+    // blocks per SM and 64 rows per split as before; above that minimum, up
+    // to 64 splits, the count whose blocks fill whole rounds of 152 SMs best
+    // (ties: fewer splits, less partial-tile traffic).
+    const long n_hi = std::max<long>(1, std::min<long>(64, R / 64));
+    const long n_lo = std::min<long>(n_hi, ceil_div(2 * 152, tiles));
+    int ns = (int)n_lo;
+    {
+        double best = -1;
+        for (long n = n_lo; n <= n_hi; ++n) {
+            long blocks = (long)tiles * n;
+            double fill = (double)blocks / (double)(ceil_div(blocks, 152) * 152L);
+            if (fill > best + 1e-9) {
+                best = fill;
+                ns = (int)n;
+            }
+        }
+    }
     c->nsplit64 = ns;
     c->nfchunk = (int)std::min<long>(std::max<long>(1, R / 256), 512);
     TDS_CUDA(cudaMalloc(&c->qp_part, sizeof(double) * 2 * c->nct64 * R));
