@@ -66,7 +66,8 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms; the samples
+    that arrive within the timed region (one interval either side) are kept."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -80,7 +81,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -89,9 +90,16 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
-    def stop(self):
+    def wait_first(self, timeout=3.0):
+        """Block until the first sample arrived: nvidia-smi's start-up (NVML
+        initialisation) then lies before the timed region, not inside it."""
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.01)
+
+    def stop(self, t0=None, t1=None):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -101,7 +109,11 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lines = self.lines
+        if t0 is not None and t1 is not None:
+            inside = [x for x in lines if t0 - 0.02 <= x[0] <= t1 + 0.02]
+            lines = inside if inside else lines
+        for _, line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -280,20 +292,24 @@ def run_ours(args):
         if conv.value or done.value != n:
             raise RuntimeError("Lanczos converged early (%d of %d steps)" % (done.value, n))
 
+    # the clock sampler starts before the warm-up steps, so that its own
+    # start-up cost is outside the timed region
+    clk = ClockSampler(local)
+    clk.start()
+    clk.wait_first()
     steps(0, W)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
-    clk = ClockSampler(local)
-    clk.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    t_start = time.time()
     e0.record(stream)
     steps(W, K)
     e1.record(stream)
     torch.cuda.synchronize()
-    clocks = clk.stop()
+    clocks = clk.stop(t_start, time.time())
     ms = e0.elapsed_time(e1)
     if ws > 1:
         t = torch.tensor([ms], device=dev)

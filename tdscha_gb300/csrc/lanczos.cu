@@ -490,6 +490,91 @@ __global__ void k_kpm_moment(const double *__restrict__ part, int nblk, double *
 
 // Copies hist rows / status of steps next..k back to the host and applies the
 // stop conditions; returns TDSCHA_OK or an error and sets *stop.
+// Lagged read-back for one run on one stream: at a batch boundary the
+// history rows and status words of the batch's steps are copied into one of
+// two pinned halves of stat_host with an event behind them, and the batch
+// before it (whose copies the GPU finished while it ran this batch) is
+// processed.  The host never drains the stream at a boundary, so the GPU keeps
+// up to one batch of steps queued.  Steps launched after the processed batch
+// reports convergence or a NaN are no-ops of the recurrence on the device
+// (halt flag) and are not reported.
+struct LaggedReadBack {
+    double *hist_dev, *stat_dev, *stat_host;
+    int capacity;
+    cudaStream_t st;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int buf = 0, pend_next = 0, pend_k = -1, pend_buf = 0;
+    bool pending = false;
+
+    LaggedReadBack(double *hd, double *sd, double *sh, int cap, cudaStream_t s)
+        : hist_dev(hd), stat_dev(sd), stat_host(sh), capacity(cap), st(s) {}
+    ~LaggedReadBack() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    double *half(int b) const { return stat_host + (size_t)b * 5 * (capacity + 1); }
+    int init() {
+        for (auto &e : ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                set_error("lanczos_run: cannot create an event");
+                return TDSCHA_ERR_CUDA;
+            }
+        return TDSCHA_OK;
+    }
+    // copies of steps next..k behind the launches so far, then the previous batch
+    int boundary(int next, int k, double *hist, int start_step, int *steps_done, int *converged,
+                 bool *stop) {
+        int cnt = k - next + 1;
+        double *hh = half(buf), *hs = hh + 4 * (capacity + 1);
+        if (cudaMemcpyAsync(hh, hist_dev + 4 * next, sizeof(double) * 4 * (cnt + 1),
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(hs, stat_dev + next, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess ||
+            cudaEventRecord(ev[buf], st) != cudaSuccess) {
+            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+            return TDSCHA_ERR_CUDA;
+        }
+        int rc = pending ? process(hist, start_step, steps_done, converged, stop) : TDSCHA_OK;
+        pending = true;
+        pend_next = next;
+        pend_k = k;
+        pend_buf = buf;
+        buf ^= 1;
+        return rc;
+    }
+    // the last batch enqueued (at the end of the run)
+    int finish(double *hist, int start_step, int *steps_done, int *converged, bool *stop) {
+        return pending ? process(hist, start_step, steps_done, converged, stop) : TDSCHA_OK;
+    }
+    int process(double *hist, int start_step, int *steps_done, int *converged, bool *stop) {
+        pending = false;
+        if (cudaEventSynchronize(ev[pend_buf]) != cudaSuccess) {
+            set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+            return TDSCHA_ERR_CUDA;
+        }
+        const double *hh = half(pend_buf), *hs = hh + 4 * (capacity + 1);
+        for (int j = 0; j < pend_k - pend_next + 1; ++j) {
+            int kj = pend_next + j;
+            if (hs[j] == ST_NAN) {
+                set_error("Invalid value encountered during the Lanczos (a is NaN at step %d)", kj);
+                *stop = true;
+                return TDSCHA_ERR_NAN;
+            }
+            hist[4 * kj + 0] = hh[4 * j + 0];
+            *steps_done = kj - start_step + 1;
+            if (hs[j] == ST_CONV) {
+                *converged = 1;
+                *stop = true;
+                return TDSCHA_OK;
+            }
+            hist[4 * kj + 1] = hh[4 * j + 1];
+            hist[4 * kj + 2] = hh[4 * j + 2];
+            hist[4 * (kj + 1) + 3] = hh[4 * (j + 1) + 3];
+        }
+        return TDSCHA_OK;
+    }
+};
+
 static int read_back_steps(double *hist_dev, double *stat_dev, double *stat_host, int capacity,
                            int next, int k, cudaStream_t st, double *hist, int start_step,
                            int *steps_done, int *converged, bool *stop) {
@@ -575,7 +660,8 @@ static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capac
         ctx->stat_dev = ctx->stat_host = nullptr;
         ctx->stat_cap = 0;
         TDS_CUDA(cudaMalloc(&ctx->stat_dev, sizeof(double) * (capacity + 1)));
-        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 5 * (capacity + 1)));
+        // two halves for the lagged read-back
+        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 10 * (capacity + 1)));
         ctx->stat_cap = capacity + 1;
     }
     TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
@@ -655,8 +741,10 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
     *converged = 0;
     cudaStream_t st = (cudaStream_t)stream;
     TDS_TRY(lz_begin(ctx, basis_Q, basis_P, capacity, start_step, run_simm, full_reorth, hist, st));
+    LaggedReadBack rb(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, st);
+    TDS_TRY(rb.init());
     int rc = TDSCHA_OK;
-    int next = start_step;          // first step not yet read back
+    int next = start_step;          // first step not yet copied back
     bool stop = false;
     for (int it = 0; it < n_iter && !stop; ++it) {
         int k = start_step + it;
@@ -668,14 +756,21 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
         if ((rc = lz_step(ctx, basis_Q, basis_P, capacity, k, run_simm, precision, full_reorth, st)) != TDSCHA_OK)
             break;
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
-        rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
-                             hist, start_step, steps_done, converged, &stop);
+        rc = rb.boundary(next, k, hist, start_step, steps_done, converged, &stop);
         // a timed-out tensor-core wait outranks whatever the read-back saw
         int mrc = mixed_check_error(ctx);
         if (mrc != TDSCHA_OK) { rc = mrc; break; }
         if (rc != TDSCHA_OK) break;
         next = k + 1;
     }
+    if (rc == TDSCHA_OK && !stop) rc = rb.finish(hist, start_step, steps_done, converged, &stop);
+    // every launched step completes before the call returns
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == TDSCHA_OK) {
+        set_error("lanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = TDSCHA_ERR_CUDA;
+    }
+    int mrc = mixed_check_error(ctx);
+    if (mrc != TDSCHA_OK) rc = mrc;
     return rc;
 }
 
@@ -799,7 +894,7 @@ static int qz_begin(tdscha_qctx *ctx, double *basis_Q, int capacity, int start_s
         ctx->hist_cap = 0;
         TDS_CUDA(cudaMalloc(&ctx->hist_dev, sizeof(double) * 4 * (capacity + 1)));
         TDS_CUDA(cudaMalloc(&ctx->stat_dev, sizeof(double) * (capacity + 1)));
-        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 5 * (capacity + 1)));
+        TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 10 * (capacity + 1)));
         TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
         TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kDotChunks + 1)));
         ctx->hist_cap = capacity + 1;
@@ -877,6 +972,8 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
     *converged = 0;
     cudaStream_t st = (cudaStream_t)stream;
     TDS_TRY(qz_begin(ctx, basis_Q, capacity, start_step, reorthogonalize, hist, st));
+    LaggedReadBack rb(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, st);
+    TDS_TRY(rb.init());
     int rc = TDSCHA_OK;
     int next = start_step;
     bool stop = false;
@@ -889,10 +986,14 @@ extern "C" int tdscha_qlanczos_run(tdscha_qctx *ctx, double *basis_Q, double *ba
         }
         if ((rc = qz_step(ctx, basis_Q, basis_P, capacity, k, reorthogonalize, st)) != TDSCHA_OK) break;
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
-        rc = read_back_steps(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, next, k, st,
-                             hist, start_step, steps_done, converged, &stop);
+        rc = rb.boundary(next, k, hist, start_step, steps_done, converged, &stop);
         if (rc != TDSCHA_OK) break;
         next = k + 1;
+    }
+    if (rc == TDSCHA_OK && !stop) rc = rb.finish(hist, start_step, steps_done, converged, &stop);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == TDSCHA_OK) {
+        set_error("qlanczos_run: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = TDSCHA_ERR_CUDA;
     }
     return rc;
 }
