@@ -39,13 +39,19 @@ __global__ void k_expand_images(const double *__restrict__ X, const double *__re
                                 const int *__restrict__ deg_space,
                                 const int *__restrict__ blocks_ids,
                                 const double *__restrict__ sym, double *__restrict__ D,
-                                double *__restrict__ F) {
+                                double *__restrict__ F,
+                                unsigned long long *__restrict__ first_bad) {
     long total = (long)N * S * M;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
          e += (long)gridDim.x * blockDim.x) {
         int mu = (int)(e % M);
         long r = e / M;
         int i = (int)(r / S), j = (int)(r % S);
+        // every input entry once (first image): the smallest non-finite index
+        if (j == 0) {
+            long x = (long)i * M + mu;
+            if (!isfinite(X[x]) || !isfinite(Y[x])) atomicMin(first_bad, (unsigned long long)x);
+        }
         int b = blocks_ids[mu];
         const int *space = deg_space + deg_off[b];
         int bd = n_deg[b];
@@ -144,8 +150,7 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     }
     for (long k = 0; k < acc_s; ++k)
         if (!std::isfinite(sym[k])) { set_error("ctx_create: non-finite symmetry entry"); return TDSCHA_ERR_NAN; }
-    for (long k = 0; k < (long)N * M; ++k)
-        if (!std::isfinite(X[k]) || !std::isfinite(Y[k])) { set_error("ctx_create: non-finite X/Y at %ld", k); return TDSCHA_ERR_NAN; }
+    // X and Y are checked for non-finite entries on the device (k_expand_images)
     for (int mu = 0; mu < M; ++mu)
         if (!(w[mu] > 0) || !std::isfinite(w[mu])) { set_error("ctx_create: frequency w[%d]=%g must be positive", mu, w[mu]); return TDSCHA_ERR_ARG; }
     double sum_rho = 0;
@@ -177,6 +182,7 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     int *d_ndeg = nullptr, *d_degoff = nullptr, *d_space = nullptr, *d_bid = nullptr;
     long *d_symoff = nullptr;
     double *d_sym = nullptr, *d_X = nullptr, *d_Y = nullptr;
+    unsigned long long *d_bad = nullptr, h_bad = ~0ULL;
 #define TRYC(x) do { rc = (x); if (rc != TDSCHA_OK) goto fail; } while (0)
 #define CUC(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { set_error("%s: %s", #x, cudaGetErrorString(_e)); rc = TDSCHA_ERR_CUDA; goto fail; } } while (0)
     TRYC(dev_alloc(&c->w, M)); TRYC(dev_alloc(&c->fY, M)); TRYC(dev_alloc(&c->fpsi, M));
@@ -193,6 +199,8 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     TRYC(dev_alloc(&d_ndeg, n_blocks)); TRYC(dev_alloc(&d_degoff, n_blocks));
     TRYC(dev_alloc(&d_symoff, n_blocks)); TRYC(dev_alloc(&d_space, M));
     TRYC(dev_alloc(&d_bid, M)); TRYC(dev_alloc(&d_sym, acc_s));
+    TRYC(dev_alloc(&d_bad, 1));
+    CUC(cudaMemcpy(d_bad, &h_bad, sizeof(h_bad), cudaMemcpyHostToDevice));
     CUC(cudaMemcpy(d_X, X, sizeof(double) * N * M, cudaMemcpyHostToDevice));
     CUC(cudaMemcpy(d_Y, Y, sizeof(double) * N * M, cudaMemcpyHostToDevice));
     CUC(cudaMemcpy(d_ndeg, n_deg, sizeof(int) * n_blocks, cudaMemcpyHostToDevice));
@@ -205,13 +213,19 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
         long total = c->R * M;
         int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
         k_expand_images<<<blocks, 256>>>(d_X, d_Y, N, M, N_syms, d_ndeg, d_degoff, d_symoff,
-                                         d_space, d_bid, d_sym, c->D, c->F);
+                                         d_space, d_bid, d_sym, c->D, c->F, d_bad);
         CUC(cudaGetLastError());
-        CUC(cudaDeviceSynchronize());
+        CUC(cudaMemcpy(&h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost));
+        if (h_bad != ~0ULL) {
+            set_error("ctx_create: non-finite X/Y at %ld", (long)h_bad);
+            rc = TDSCHA_ERR_NAN;
+            goto fail;
+        }
     }
     cudaFree(d_X); cudaFree(d_Y); cudaFree(d_ndeg); cudaFree(d_degoff); cudaFree(d_symoff);
-    cudaFree(d_space); cudaFree(d_bid); cudaFree(d_sym);
+    cudaFree(d_space); cudaFree(d_bid); cudaFree(d_sym); cudaFree(d_bad);
     d_X = d_Y = nullptr; d_ndeg = d_degoff = d_space = d_bid = nullptr; d_symoff = nullptr; d_sym = nullptr;
+    d_bad = nullptr;
 
     TRYC(dev_alloc(&c->R1, M)); TRYC(dev_alloc(&c->Y1, (size_t)M * M));
     TRYC(dev_alloc(&c->f, M)); TRYC(dev_alloc(&c->d2v, (size_t)M * M));
@@ -237,6 +251,7 @@ fail:
     if (d_space) cudaFree(d_space);
     if (d_bid) cudaFree(d_bid);
     if (d_sym) cudaFree(d_sym);
+    if (d_bad) cudaFree(d_bad);
     ctx_free(c);
     return rc;
 #undef TRYC

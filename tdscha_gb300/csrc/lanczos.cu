@@ -33,17 +33,20 @@ int build_pair_coeffs(tdscha_ctx *c) {
     auto nb_div = [&](double x) { return T > 0 ? 1 / (exp(x / (T / kRyToK)) - 1) : 0.0; };
     // and as get_chi_minus/plus write them (multiplication form, :2650-2652)
     auto nb_mul = [&](double x) { return T > kEps ? 1.0 / (exp(x * 157887.32400374097 / T) - 1.0) : 0.0; };
-    std::vector<double> yw(M), reaw(M);
+    std::vector<double> yw(M), reaw(M), bdiv(M), bmul(M);
     for (int m = 0; m < M; ++m) {
         double n_mu = T > kEps ? 1.0 / (exp(w[m] * 157887.32400374097 / T) - 1.0) : 0.0;
         yw[m] = 2 * w[m] / (2 * n_mu + 1);
         reaw[m] = 2 * w[m] * n_mu * (n_mu + 1) / (2 * n_mu + 1);
+        // per-mode Bose factors, looked up by the pair loop below
+        bdiv[m] = nb_div(w[m]);
+        bmul[m] = nb_mul(w[m]);
     }
     long k = 0;
     for (int i = 0; i < M; ++i) {
         for (int j = i; j < M; ++j, ++k) {
             double wa = w[j], wb = w[i];          // i_a = column, i_b = row (:2338-2346)
-            double na = nb_div(wa), nbb = nb_div(wb);
+            double na = bdiv[j], nbb = bdiv[i];
             double den = (2 * na + 1) * (2 * nbb + 1);
             if (!c->use_wigner) {
                 double X_ab = -wa * wa - wb * wb - (2 * wa * wb) / den;
@@ -66,7 +69,7 @@ int build_pair_coeffs(tdscha_ctx *c) {
             pc[PC_UA * H + k] = w2_on_X * sqrt(-0.5 * chi_m);
             pc[PC_UB * H + k] = w2_on_X * sqrt(+0.5 * chi_p);
             // repack factors from get_chi_minus / get_chi_plus (row i, column j)
-            double ni = nb_mul(w[i]), nj = nb_mul(w[j]);
+            double ni = bmul[i], nj = bmul[j];
             double cm = ((w[j] - w[i]) * (nj - ni)) / ((2. * w[j]) * w[i]);
             double cp = ((w[j] + w[i]) * (1 + nj + ni)) / ((2. * w[j]) * w[i]);
             pc[PC_RA * H + k] = sqrt(-0.5 * cm);

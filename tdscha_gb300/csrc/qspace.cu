@@ -49,6 +49,13 @@ __device__ __forceinline__ double2 cfma_conj(double2 a, double2 b, double2 acc) 
 }
 
 // x_rot = S_j x_i for every image row, S_j in CSR (identity when n_syms == 0).
+// bad = 1 if any of the n entries of a or b is not finite
+__global__ void k_q_finite(const double *__restrict__ a, const double *__restrict__ b, long n,
+                           int *__restrict__ bad) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        if (!isfinite(a[e]) || !isfinite(b[e])) *bad = 1;
+}
+
 __global__ void k_q_expand(const double2 *__restrict__ X, const double2 *__restrict__ Y, int N,
                            int n_q, int nb, int S, int has_syms, const int *__restrict__ rowptr,
                            const int *__restrict__ col, const double2 *__restrict__ val,
@@ -557,8 +564,7 @@ extern "C" int tdscha_qctx_create(tdscha_qctx **out, int n_q, int nb, int N, con
         for (long t = 0; t < nnz; ++t)
             if (sym_col[t] < 0 || sym_col[t] >= L) { set_error("qctx_create: symmetry column %ld out of range", t); return TDSCHA_ERR_ARG; }
     }
-    for (long k = 0; k < 2L * n_q * N * nb; ++k)
-        if (!std::isfinite(X_q[k]) || !std::isfinite(Y_q[k])) { set_error("qctx_create: non-finite X_q/Y_q"); return TDSCHA_ERR_NAN; }
+    // X_q and Y_q are checked for non-finite entries on the device after the upload
     double sum_rho = 0;
     for (int i = 0; i < N; ++i) sum_rho += rho[i];
     if (!(sum_rho != 0) || !std::isfinite(sum_rho)) { set_error("qctx_create: bad weights"); return TDSCHA_ERR_ARG; }
@@ -581,15 +587,27 @@ extern "C" int tdscha_qctx_create(tdscha_qctx **out, int n_q, int nb, int N, con
             fp[q * nb + nu] = (1.0 + 2.0 * nw) / (2.0 * w);
         }
     double2 *dX = nullptr, *dY = nullptr, *dval = nullptr;
-    int *drp = nullptr, *dcol = nullptr;
-    int rc = TDSCHA_OK;
-    auto fail = [&](int code) { if (dX) cudaFree(dX); if (dY) cudaFree(dY); if (dval) cudaFree(dval); if (drp) cudaFree(drp); if (dcol) cudaFree(dcol); q_free(c); return code; };
+    int *drp = nullptr, *dcol = nullptr, *dbad = nullptr;
+    auto fail = [&](int code) { if (dX) cudaFree(dX); if (dY) cudaFree(dY); if (dval) cudaFree(dval); if (drp) cudaFree(drp); if (dcol) cudaFree(dcol); if (dbad) cudaFree(dbad); q_free(c); return code; };
 #define QCU(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { set_error("%s: %s", #x, cudaGetErrorString(_e)); return fail(TDSCHA_ERR_CUDA); } } while (0)
     size_t nX = (size_t)n_q * N * nb;
     QCU(cudaMalloc(&dX, sizeof(double2) * nX));
     QCU(cudaMalloc(&dY, sizeof(double2) * nX));
     QCU(cudaMemcpy(dX, X_q, sizeof(double2) * nX, cudaMemcpyHostToDevice));
     QCU(cudaMemcpy(dY, Y_q, sizeof(double2) * nX, cudaMemcpyHostToDevice));
+    {
+        int hbad = 0;
+        QCU(cudaMalloc(&dbad, sizeof(int)));
+        QCU(cudaMemset(dbad, 0, sizeof(int)));
+        long n = 2 * (long)nX;
+        k_q_finite<<<(int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 16)), 256>>>(
+            reinterpret_cast<const double *>(dX), reinterpret_cast<const double *>(dY), n, dbad);
+        QCU(cudaGetLastError());
+        QCU(cudaMemcpy(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost));
+        cudaFree(dbad);
+        dbad = nullptr;
+        if (hbad) { set_error("qctx_create: non-finite X_q/Y_q"); return fail(TDSCHA_ERR_NAN); }
+    }
     if (n_syms > 0) {
         QCU(cudaMalloc(&drp, sizeof(int) * (size_t)n_syms * (L + 1)));
         QCU(cudaMalloc(&dcol, sizeof(int) * std::max<long>(1, nnz)));
@@ -626,7 +644,6 @@ extern "C" int tdscha_qctx_create(tdscha_qctx **out, int n_q, int nb, int N, con
     QCU(cudaMalloc(&c->dots, sizeof(double) * 4 * 296));
     QCU(cudaMalloc(&c->scal, sizeof(double) * 64));
 #undef QCU
-    (void)rc;
     *out = c;
     return TDSCHA_OK;
 }

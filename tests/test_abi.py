@@ -65,10 +65,17 @@ def test_create_rejects_bad_sizes(lib):
     assert b"bad sizes" in lib.tdscha_last_error()
 
 
-def test_create_rejects_nan_input(lib):
+@pytest.mark.gpu
+def test_create_rejects_nan_input(gpu_lib):
+    # the ensemble is checked for non-finite entries on the device, while its
+    # images are formed
     X = np.zeros((3, 4)); X[1, 2] = np.nan
-    rc, _ = _create(lib, X=X)
-    assert rc == nat.ERR_NAN
+    rc, h = _create(gpu_lib, X=X)
+    assert rc == nat.ERR_NAN and not h.value
+    assert b"non-finite X/Y at 6" in gpu_lib.tdscha_last_error()
+    Y = np.zeros((3, 4)); Y[2, 0] = np.inf
+    rc, h = _create(gpu_lib, Y=Y)
+    assert rc == nat.ERR_NAN and b"at 8" in gpu_lib.tdscha_last_error()
 
 
 def test_create_rejects_bad_blocks(lib):

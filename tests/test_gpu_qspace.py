@@ -158,6 +158,14 @@ def test_qspace_errors(gpu_lib):
                                 nat.dp(X.view(np.float64)), nat.dp(np.ones(40)), None,
                                 nat.dp(np.ones(4)), 300.0, 0, None, None, None)
     assert rc == nat.ERR_ARG   # more than 32 bands
+    # non-finite ensemble entries are found on the device after the upload
+    Xn = np.zeros((2, 10, 3), dtype=np.complex128)
+    Xn[1, 4, 2] = complex(0.0, np.nan)
+    Yn = np.zeros_like(Xn)
+    rc = lib.tdscha_qctx_create(ctypes.byref(h), 2, 3, 10, nat.dp(Xn.view(np.float64)),
+                                nat.dp(Yn.view(np.float64)), nat.dp(np.ones(6)), None,
+                                nat.dp(np.ones(10)), 300.0, 0, None, None, None)
+    assert rc == nat.ERR_NAN and b"non-finite" in lib.tdscha_last_error()
     e, lz, o = _setup((3, 1, 1), 2, 50, "sum")
     ctx = lz._qcontext()
     with pytest.raises(nat.TdschaError):
