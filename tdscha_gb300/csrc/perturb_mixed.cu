@@ -1001,72 +1001,86 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
     }
 }
 
-// Sum of the split-K partial tiles (coalesced, float64 out) ...
-__global__ void k_gsum(const float *__restrict__ gpart, int nsplit, int ldG, int M,
-                       double *__restrict__ gs) {
-    long n = (long)M * M;
-    long stride = (long)ldG * ldG;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        int a = (int)(e / M), b = (int)(e % M);
-        const float *g = gpart + (long)a * ldG + b;
-        // compensated fp32 sum (float64 adds are slow on this part); the
-        // partials are loaded four at a time so the loads overlap
-        float sum = 0.f, comp = 0.f;
-        int s = 0;
-        for (; s + 4 <= nsplit; s += 4) {
-            float v[4];
+// Split-K sum and finalisation in one pass: one block per 8-row slab of a
+// 32 x 32 tile pair (A, B), A <= B.  G over the partial tiles is formed for the
+// slab's transposed part of tile (B, A) first (kept in shared memory) and then
+// for its part of (A, B), each element as a
+// compensated fp32 sum over the splits in split order, and
+// d2v[a][b] = d2v[b][a] = -(G[a][b] + G[b][a]) / norm is written without a
+// float64 G round trip.  Blocks with A = 0 also finish f for the columns of
+// tile B.
+__device__ __forceinline__ double gsum_one(const float *__restrict__ g, int nsplit, long stride) {
+    float sum = 0.f, comp = 0.f;
+    int s = 0;
+    // eight loads in flight per thread (the sum is latency-bound)
+    for (; s + 8 <= nsplit; s += 8) {
+        float v[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = g[(long)(s + u) * stride];
+        for (int u = 0; u < 8; ++u) v[u] = g[(long)(s + u) * stride];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                float y = v[u] - comp;
-                float t = sum + y;
-                comp = (t - sum) - y;
-                sum = t;
-            }
-        }
-        for (; s < nsplit; ++s) {
-            float y = g[(long)s * stride] - comp;
+        for (int u = 0; u < 8; ++u) {
+            float y = v[u] - comp;
             float t = sum + y;
             comp = (t - sum) - y;
             sum = t;
         }
-        gs[e] = (double)sum - (double)comp;
     }
+    for (; s < nsplit; ++s) {
+        float y = g[(long)s * stride] - comp;
+        float t = sum + y;
+        comp = (t - sum) - y;
+        sum = t;
+    }
+    return (double)sum - (double)comp;
 }
 
-// ... then d2v = -(G + G^T) / norm and f = sum of the W-build partials / norm.
-// One 32 x 32 tile of d2v per block (256 threads), the transposed tile read
-// through shared memory so both reads are coalesced.
-__global__ void k_finalize_mixed(const double *__restrict__ gs, const float *__restrict__ fpart,
-                                 int nfchunk, int M, double norm, double *__restrict__ f,
-                                 double *__restrict__ d2v) {
-    __shared__ double tr[32][33];
+__global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart, int nsplit,
+                                                int ldG, int M, const float *__restrict__ fpart,
+                                                int nfchunk, double norm, double *__restrict__ f,
+                                                double *__restrict__ d2v) {
+    __shared__ double tr[32][9];    // G over rows b of tile B, the slab's 8 columns a: [b][a]
+    __shared__ double red[8][33];
+    // (pair, slab): pair index -> (A, B), A <= B, row-major over the upper
+    // triangle of tiles; slab = 8 rows a of tile A
+    const int nt = (M + 31) / 32;
+    const int slab = blockIdx.x & 3;
+    int A = 0, rem = blockIdx.x >> 2;
+    while (rem >= nt - A) {
+        rem -= nt - A;
+        ++A;
+    }
+    const int B = A + rem;
     const double inv = 1.0 / norm;
-    const int a0 = blockIdx.y * 32, b0 = blockIdx.x * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 32
-    for (int k = ty; k < 32; k += 8) {
-        int a = b0 + k, b = a0 + tx;                            // gs[b0 + k][a0 + tx]
-        tr[k][tx] = (a < M && b < M) ? gs[(long)a * M + b] : 0.0;
+    const long stride = (long)ldG * ldG;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 x 32
+    const int a0 = A * 32 + slab * 8, b0 = B * 32;
+    {
+        // G[b][a] for the 32 rows b of tile B and the slab's 8 columns a; lanes
+        // along a, so that a warp reads 4 rows x 8 consecutive floats (4 sectors)
+        int ao = threadIdx.x & 7, bo = threadIdx.x >> 3;
+        int b = b0 + bo, a = a0 + ao;
+        tr[bo][ao] = (a < M && b < M) ? gsum_one(gpart + (long)b * ldG + a, nsplit, stride) : 0.0;
     }
     __syncthreads();
-    for (int k = ty; k < 32; k += 8) {
-        int a = a0 + k, b = b0 + tx;
-        if (a < M && b < M) d2v[(long)a * M + b] = -(gs[(long)a * M + b] + tr[tx][k]) * inv;
+    {
+        int a = a0 + ty, b = b0 + tx;                         // G[a][b], coalesced in b
+        if (a < M && b < M) {
+            double v = -(gsum_one(gpart + (long)a * ldG + b, nsplit, stride) + tr[tx][ty]) * inv;
+            d2v[(long)a * M + b] = v;
+            if (A != B) d2v[(long)b * M + a] = v;
+        }
     }
-    if (blockIdx.y == 0) {
-        // f for the block's 32 columns: 8 chunk-strided partials per column
-        __syncthreads();
-        double *red = &tr[0][0];
+    if (A == 0 && slab == 0) {
+        // f for the block's 32 columns of tile B: 8 chunk-strided partials per column
         int e = b0 + tx;
         double acc = 0;
         if (e < M)
             for (int ch = ty; ch < nfchunk; ch += 8) acc += (double)fpart[(long)ch * M + e];
-        red[ty * 33 + tx] = acc;
+        red[ty][tx] = acc;
         __syncthreads();
         if (ty == 0 && e < M) {
             double sum = 0;
-            for (int k = 0; k < 8; ++k) sum += red[k * 33 + tx];
+            for (int k = 0; k < 8; ++k) sum += red[k][tx];
             f[e] = sum * inv;
         }
     }
@@ -1353,11 +1367,9 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     }
     {
         ProfScope ps(c, 4, st);
-        int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 2048));
-        k_gsum<<<nb, 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, M, c->gpart);
-        dim3 gt(ceil_div(M, 32), ceil_div(M, 32));
-        k_finalize_mixed<<<gt, 256, 0, st>>>(c->gpart, x->fpart, x->nfchunk, M, c->sum_rho * c->S,
-                                             c->f, c->d2v);
+        const int nt = ceil_div(M, 32);
+        k_gfinal<<<4 * (nt * (nt + 1) / 2), 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, M, x->fpart,
+                                                    x->nfchunk, c->sum_rho * c->S, c->f, c->d2v);
         TDS_CHECK_LAUNCH();
     }
     return TDSCHA_OK;
