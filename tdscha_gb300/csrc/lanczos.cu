@@ -361,7 +361,29 @@ __global__ void k_proj_dots(const double *__restrict__ Qb, const double *__restr
     long e0 = n * blockIdx.y / kDotChunks, e1 = n * (blockIdx.y + 1) / kDotChunks;
     const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
     double a = 0, b = 0;
-    for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    // four strides' loads issued before their FMAs (the pass streams the whole
+    // basis and is bound by loads in flight); the accumulation order is the
+    // plain strided one
+    const long bd = blockDim.x;
+    long e = e0 + threadIdx.x;
+    for (; e + 3 * bd < e1; e += 4 * bd) {
+        double vp[4], vq[4], vqn[4], vpn[4], m[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            long x = e + u * bd;
+            vp[u] = pj[x];
+            vq[u] = qj[x];
+            vqn[u] = qn[x];
+            vpn[u] = pn[x];
+            m[u] = mask ? mask[x] : 1.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a = fma(vp[u], vqn[u] * m[u], a);
+            b = fma(vq[u], vpn[u] * m[u], b);
+        }
+    }
+    for (; e < e1; e += bd) {
         double m = mask ? mask[e] : 1.0;
         a = fma(pj[e], qn[e] * m, a);
         b = fma(qj[e], pn[e] * m, b);
@@ -401,7 +423,22 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
     double pq = 0;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         double q = qn[e], p = pn[e];
-        for (int j = 0; j < nvec; ++j) {
+        // eight basis vectors' loads issued before their FMAs (in j order)
+        int j = 0;
+        for (; j + 8 <= nvec; j += 8) {
+            double vq[8], vp[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                vq[u] = Qb[(long)(j0 + j + u) * ld + e];
+                vp[u] = Pb[(long)(j0 + j + u) * ld + e];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                q = fma(-cs[2 * (j + u)], vq[u], q);
+                p = fma(-cs[2 * (j + u) + 1], vp[u], p);
+            }
+        }
+        for (; j < nvec; ++j) {
             q = fma(-cs[2 * j], Qb[(long)(j0 + j) * ld + e], q);
             p = fma(-cs[2 * j + 1], Pb[(long)(j0 + j) * ld + e], p);
         }
