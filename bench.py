@@ -382,9 +382,15 @@ def run_ours(args):
                     "avg_launch_ms": tot_ms / cnt}
     kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1]}
                for k, v in kern.items()}
-    # kernels launched per step: per application (precision dependent) + recurrence
-    per_app = (len(kern) + 3) if prec_name == "fp64" else (len(kern) + 3)
-    gpu_launches = K * (2 * per_app + 5)
+    # kernels launched per step.  One application: psi unpack + assemble and
+    # the averages (mixed: Y1 limbs, stage A, row scalars, W build, stage B,
+    # finalisation; float64: stage A, row scalars, force average, stage B,
+    # finalisation).  Recurrence: dot + a, residuals, b/c, normalisation, and
+    # with re-biorthogonalisation the dots, coefficients, apply and weight
+    # (one apply pass per 2048 stored vectors, here always one).
+    per_app = 2 + (6 if prec_name == "mixed" else 5)
+    per_step_rec = 5 + (4 if not args.no_reorth else 0)
+    gpu_launches = K * (2 * per_app + per_step_rec)
 
     # float64 arm of the metric (same GPU) and the spectral-error check
     fp64 = None
