@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/tdscha_gb300.h"
@@ -181,6 +182,34 @@ void free_translations(tdscha_ctx *c);
 int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t st);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Programmatic dependent launch.  A kernel started by launch_pdl is scheduled
+// as the blocks of the kernel before it in the stream exit, so its launch and
+// block set-up (and the barrier / TMEM set-up of the persistent kernels) hide
+// behind that kernel's tail.  Its threads call pdl_enter() before touching
+// global memory: it returns once the earlier kernels have completed and their
+// writes are visible.  No kernel triggers its dependents early: blocks of the
+// next kernel resident during a whole kernel took SM slots from its last wave
+// and made the Lanczos step slower (1365 steps/s against 1413 without
+// dependent launch and about 1500 with the launch at block exit, M=573,
+// N=50 000).  Launched the usual way, pdl_enter() is a no-op.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args &&...args) {
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Bracket a launch with CUDA events when profiling is on.
 struct ProfScope {

@@ -77,8 +77,11 @@ int build_pair_coeffs(tdscha_ctx *c) {
             // transpose rescaling coefficients (:3036-3050), [a=i][b=j]
             double cY = yw[i] * yw[j] * yw[j] + yw[i] * yw[i] * yw[j];
             double cRA = yw[i] * reaw[j] * yw[j] + yw[i] * reaw[i] * yw[j];
-            pc[PC_TY * H + k] = cY * 2;
-            pc[PC_TRA * H + k] = cRA * 2;
+            // times the half weight of an off-diagonal pair (exact: a power of
+            // two), so the unpack multiplies each entry once
+            double h = (i != j) ? 0.5 : 1.0;
+            pc[PC_TY * H + k] = (cY * 2) * h;
+            pc[PC_TRA * H + k] = (cRA * 2) * h;
             pc[PC_I * H + k] = i;
             pc[PC_J * H + k] = j;
         }
@@ -111,9 +114,12 @@ __device__ __forceinline__ long tri_index(int i, int j, int M) {
 __global__ void k_unpack(const double *__restrict__ psi, const double *__restrict__ pc, int M,
                          long H, int wigner, int transpose, int ignore_v3,
                          double *__restrict__ R1, double *__restrict__ Y1) {
-    long n = (long)M * M;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        int a = (int)(e / M), b = (int)(e % M);
+    pdl_enter();
+    // rows a over blockIdx.y, columns b over the x dimension: no 64-bit
+    // division per element
+    for (int a = blockIdx.y; a < M; a += gridDim.y)
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < M; b += gridDim.x * blockDim.x) {
+        const long e = (long)a * M + b;
         int i = min(a, b), j = max(a, b);
         long k = tri_index(i, j, M);
         double y = psi[M + k], ra = psi[M + H + k], v;
@@ -122,70 +128,103 @@ __global__ void k_unpack(const double *__restrict__ psi, const double *__restric
         } else if (!transpose) {
             v = y;
         } else {
-            double h = (i != j) ? 0.5 : 1.0;
-            v = (y * h) * pc[PC_TY * H + k] + (ra * h) * pc[PC_TRA * H + k];
+            v = y * pc[PC_TY * H + k] + ra * pc[PC_TRA * H + k];
         }
         Y1[e] = v;
-        if (e < M) R1[e] = ignore_v3 ? 0.0 : psi[e];
+        if (a == 0) R1[b] = ignore_v3 ? 0.0 : psi[b];
     }
 }
 
-// out = L1 psi (+ anharmonic repack of f, d2v) then reverse / shift.
+// out = L1 psi (+ anharmonic repack of f, d2v) then reverse / shift.  One
+// thread per mode (the first M entries) or per pair k, which writes both its
+// Y entry M + k and its A entry M + H + k: the two share the psi, tri and d2v
+// loads, and with the layout (plain, transposed, Wigner) and the reversal as
+// template arguments the float64 pipe sees only the products and sums (this
+// part runs float64 at two FMA per cycle per SM).  Sign flips are folded into
+// the operand order of the final sum.
+enum { ASM_PLAIN = 0, ASM_TRANSPOSE = 1, ASM_WIGNER = 2 };
+
+template <bool kRev>
+__device__ __forceinline__ double asm_out(double l1, double an_pos, bool minus_an) {
+    // o = l1 + (minus_an ? -an_pos : an_pos), negated when reversing
+    if (!minus_an) return kRev ? (-l1) - an_pos : l1 + an_pos;
+    return kRev ? an_pos - l1 : l1 - an_pos;
+}
+
+template <int kMode, bool kRev>
 __global__ void k_assemble(const double *__restrict__ psi, const double *__restrict__ f,
                            const double *__restrict__ d2v, const double *__restrict__ pc,
                            const int *__restrict__ tri, const double *__restrict__ w,
                            const double *__restrict__ Yw, const double *__restrict__ Ywinv,
-                           const double *__restrict__ ReAw, int M, long H, int wigner,
-                           int transpose, int ignore_harmonic, int with_anh, int reverse,
-                           double shift, double *__restrict__ out) {
-    long P = M + 2 * H;
-    double sg = wigner ? 1.0 : -1.0;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < P; e += (long)gridDim.x * blockDim.x) {
-        double l1 = 0.0, an = 0.0;
-        if (e < M) {
-            if (!ignore_harmonic) {
-                double t = (psi[e] * w[e]) * w[e];
-                l1 = wigner ? -t : t;
-            }
-            if (with_anh) an = sg * f[e];
-        } else {
-            bool ysec = e < M + H;
-            long k = ysec ? e - M : e - M - H;
-            double pY = psi[M + k], pA = psi[M + H + k];
-            if (!ignore_harmonic) {
-                if (wigner) {
-                    l1 = ysec ? pc[PC_X * H + k] * pY : pc[PC_Y1 * H + k] * pA;
-                } else if (!transpose) {
-                    l1 = ysec ? pc[PC_X * H + k] * pY + pc[PC_Y * H + k] * pA
-                              : pc[PC_X1 * H + k] * pY + pc[PC_Y1 * H + k] * pA;
-                } else {
-                    l1 = ysec ? pc[PC_X * H + k] * pY + pc[PC_X1 * H + k] * pA
-                              : pc[PC_Y * H + k] * pY + pc[PC_Y1 * H + k] * pA;
-                }
-            }
-            if (with_anh) {
-                int i = tri[2 * k], j = tri[2 * k + 1];
-                double dv = d2v[(long)i * M + j];
-                double v;
-                if (wigner) {
-                    v = (ysec ? pc[PC_RA * H + k] : pc[PC_RB * H + k]) * dv;
-                } else if (!transpose) {
-                    const double *ew = ysec ? Yw : ReAw;
-                    v = dv * ew[i] + dv * ew[j];
-                } else if (ysec) {
-                    v = 0.5 * (Ywinv[i] * dv * Ywinv[j]);
-                    if (i != j) v *= 2;
-                } else {
-                    v = 0.0;
-                }
-                an = sg * v;
+                           const double *__restrict__ ReAw, int M, long H, int ignore_harmonic,
+                           int with_anh, double shift, double *__restrict__ out) {
+    pdl_enter();
+    constexpr bool kW = kMode == ASM_WIGNER;
+    const bool harm = !ignore_harmonic, anh = with_anh != 0, sh = shift != 0.0;
+    const long n = M + H;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        if (t < M) {
+            const double p = psi[t];
+            const double hm = harm ? (p * w[t]) * w[t] : 0.0;
+            const double fa = anh ? f[t] : 0.0;
+            // plain / transposed: o = hm - f; Wigner: o = -hm + f
+            double o = kW ? asm_out<kRev>(fa, hm, true) : asm_out<kRev>(hm, fa, true);
+            if (sh) o += shift * p;
+            out[t] = o;
+            continue;
+        }
+        const long k = t - M;
+        const double pY = psi[M + k], pA = psi[M + H + k];
+        double lY = 0.0, lA = 0.0;
+        if (harm) {
+            if (kMode == ASM_WIGNER) {
+                lY = pc[PC_X * H + k] * pY;
+                lA = pc[PC_Y1 * H + k] * pA;
+            } else if (kMode == ASM_PLAIN) {
+                lY = pc[PC_X * H + k] * pY + pc[PC_Y * H + k] * pA;
+                lA = pc[PC_X1 * H + k] * pY + pc[PC_Y1 * H + k] * pA;
+            } else {
+                lY = pc[PC_X * H + k] * pY + pc[PC_X1 * H + k] * pA;
+                lA = pc[PC_Y * H + k] * pY + pc[PC_Y1 * H + k] * pA;
             }
         }
-        double o = l1 + an;
-        if (reverse) o *= -1;
-        o += shift * psi[e];
-        out[e] = o;
+        double vY = 0.0, vA = 0.0;
+        if (anh) {
+            const int i = tri[2 * k], j = tri[2 * k + 1];
+            const double dv = d2v[(long)i * M + j];
+            if (kMode == ASM_WIGNER) {
+                vY = pc[PC_RA * H + k] * dv;
+                vA = pc[PC_RB * H + k] * dv;
+            } else if (kMode == ASM_PLAIN) {
+                vY = dv * Yw[i] + dv * Yw[j];
+                vA = dv * ReAw[i] + dv * ReAw[j];
+            } else {
+                vY = 0.5 * (Ywinv[i] * dv * Ywinv[j]);
+                if (i != j) vY *= 2;
+            }
+        }
+        double oY = asm_out<kRev>(lY, vY, !kW);
+        double oA = asm_out<kRev>(lA, vA, !kW);
+        if (sh) {
+            oY += shift * pY;
+            oA += shift * pA;
+        }
+        out[M + k] = oY;
+        out[M + H + k] = oA;
     }
+}
+
+template <int kMode>
+static cudaError_t launch_assemble(int nb, cudaStream_t st, int reverse, const double *psi,
+                            const double *f, const double *d2v, const double *pc, const int *tri,
+                            const double *w, const double *Yw, const double *Ywinv,
+                            const double *ReAw, int M, long H, int ignore_harmonic, int with_anh,
+                            double shift, double *out) {
+    if (reverse)
+        return launch_pdl(k_assemble<kMode, true>, nb, 256, 0, st, psi, f, d2v, pc, tri, w, Yw,
+                          Ywinv, ReAw, M, H, ignore_harmonic, with_anh, shift, out);
+    return launch_pdl(k_assemble<kMode, false>, nb, 256, 0, st, psi, f, d2v, pc, tri, w, Yw, Ywinv,
+                      ReAw, M, H, ignore_harmonic, with_anh, shift, out);
 }
 
 int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,
@@ -194,28 +233,35 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
     long H = c->H;
     int with_anh = !c->ignore_v3;
     if (with_anh) {
-        int nb = std::max(1, std::min(ceil_div((long)M * M, 256), 4096));
-        k_unpack<<<nb, 256, 0, st>>>(psi_in, c->pc, M, H, c->use_wigner, transpose, c->ignore_v3,
-                                     c->R1, c->Y1);
-        TDS_CHECK_LAUNCH();
+        dim3 gu(ceil_div(M, 256), std::min(M, 65535));
+        TDS_CUDA(launch_pdl(k_unpack, gu, 256, 0, st, psi_in, c->pc, M, H, c->use_wigner, transpose,
+                            c->ignore_v3, c->R1, c->Y1));
         // Y1 from the unpack is symmetric by construction: no symmetrise pass
         TDS_TRY(run_perturb_sym(c, c->ignore_v4 ? 0 : 1, precision, st));
         // gamma_only: translation projection of f and d2v (DynamicalLanczos.py:3173-3191)
         if (c->tr_ntrans > 0) TDS_TRY(apply_translation_projection(c, st));
     }
-    int nb = std::max(1, std::min(ceil_div(c->P, 256), 4096));
-    k_assemble<<<nb, 256, 0, st>>>(psi_in, c->f, c->d2v, c->pc, c->tri, c->w, c->Yw, c->Ywinv,
-                                   c->ReAw, M, H,
-                                   c->use_wigner, transpose, c->ignore_harmonic, with_anh,
-                                   c->reverse_L, c->shift, psi_out);
-    TDS_CHECK_LAUNCH();
+    int nb = std::max(1, std::min(ceil_div(M + H, 256), 4096));
+    if (c->use_wigner)
+        TDS_CUDA(launch_assemble<ASM_WIGNER>(nb, st, c->reverse_L, psi_in, c->f, c->d2v, c->pc, c->tri, c->w,
+                                    c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic, with_anh,
+                                    c->shift, psi_out));
+    else if (transpose)
+        TDS_CUDA(launch_assemble<ASM_TRANSPOSE>(nb, st, c->reverse_L, psi_in, c->f, c->d2v, c->pc, c->tri,
+                                       c->w, c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic,
+                                       with_anh, c->shift, psi_out));
+    else
+        TDS_CUDA(launch_assemble<ASM_PLAIN>(nb, st, c->reverse_L, psi_in, c->f, c->d2v, c->pc, c->tri, c->w,
+                                   c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic, with_anh,
+                                   c->shift, psi_out));
     return TDSCHA_OK;
 }
 
 // ---------------------------------------------------------------------------
 // Lanczos recurrence.  Device scalars (ctx->scal):
 enum { SC_A = 0, SC_PNORM, SC_CQ, SC_CP, SC_B, SC_C, SC_SNORM, SC_SRAW, SC_CONV, SC_NAN, SC_HALT,
-       SC_NEXT };   // SC_NEXT: the last re-orthogonalised vector had zero norm
+       SC_NEXT,     // SC_NEXT: the last re-orthogonalised vector had zero norm
+       SC_IB, SC_IS };   // 1 / b and 1 / s_raw for the normalisation
 // per-step status written on the device: 0 running, 1 NaN in a, 2 converged
 enum { ST_OK = 0, ST_NAN = 1, ST_CONV = 2 };
 // hist_dev rows of 4: a_k, b_k, c_k, s_norm_k.
@@ -235,13 +281,31 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return s;   // valid in thread 0
 }
 
+// y * mask[e], or y where there is no mask.  The kernels below take the mask
+// test out of their loops (kMasked a compile-time flag): float64 runs at two
+// FMA per cycle per SM on this part and a multiplication by 1.0 costs as much
+// as the FMA it feeds.  y * 1.0 == y, so both forms give the same bits.
+template <bool kMasked>
+__device__ __forceinline__ double masked(double y, const double *__restrict__ mask, long e) {
+    return kMasked ? y * mask[e] : y;
+}
+
+template <bool kMasked>
+__device__ __forceinline__ double dot1_range(const double *__restrict__ x,
+                                             const double *__restrict__ y,
+                                             const double *__restrict__ mask, long n) {
+    double acc = 0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        acc += x[e] * masked<kMasked>(y[e], mask, e);
+    return acc;
+}
+
 // partial of sum x*y*mask (mask may be null) per block
 __global__ void k_dot1(const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ mask, long n, double *__restrict__ part) {
+    pdl_enter();
     __shared__ double sh[32];
-    double acc = 0;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
-        acc += x[e] * (mask ? y[e] * mask[e] : y[e]);
+    double acc = mask ? dot1_range<true>(x, y, mask, n) : dot1_range<false>(x, y, mask, n);
     double s = block_sum(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
@@ -257,6 +321,7 @@ __device__ __forceinline__ double reduce_parts(const double *__restrict__ part, 
 // a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232)
 __global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
                          int k, double *__restrict__ scal, double *__restrict__ status) {
+    pdl_enter();
     __shared__ double sh[32];
     double d = reduce_parts(part, nblk, sh);
     if (threadIdx.x != 0 || scal[SC_HALT] != 0.0) return;
@@ -278,16 +343,16 @@ __global__ void k_scal_a(const double *__restrict__ part, int nblk, const double
     scal[SC_CP] = cp;
 }
 
-// rk = Lq - a q - cq q_prev ; sk = pL - a p - cp p_prev ; partial dots ss, rr, sr
-__global__ void k_resid(const double *__restrict__ Lq, const double *__restrict__ pL,
-                        const double *__restrict__ q, const double *__restrict__ p,
-                        const double *__restrict__ qprev, const double *__restrict__ pprev,
-                        const double *__restrict__ mask, const double *__restrict__ scal, long n,
-                        double *__restrict__ rk, double *__restrict__ sk, double *__restrict__ part,
-                        int nblk) {
-    __shared__ double sh[32];
-    double a = scal[SC_A], cq = scal[SC_CQ], cp = scal[SC_CP];
-    double ss = 0, rr = 0, sr = 0;
+template <bool kMasked>
+__device__ __forceinline__ void resid_range(const double *__restrict__ Lq, const double *__restrict__ pL,
+                                            const double *__restrict__ q, const double *__restrict__ p,
+                                            const double *__restrict__ qprev,
+                                            const double *__restrict__ pprev,
+                                            const double *__restrict__ mask,
+                                            const double *__restrict__ scal, long n,
+                                            double *__restrict__ rk, double *__restrict__ sk,
+                                            double &ss, double &rr, double &sr) {
+    const double a = scal[SC_A], cq = scal[SC_CQ], cp = scal[SC_CP];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         double r = Lq[e] - a * q[e];
         double s = pL[e] - a * p[e];
@@ -295,11 +360,26 @@ __global__ void k_resid(const double *__restrict__ Lq, const double *__restrict_
         if (pprev) s -= cp * pprev[e];
         rk[e] = r;
         sk[e] = s;
-        double m = mask ? mask[e] : 1.0;
-        ss += s * (s * m);
-        rr += r * (r * m);
-        sr += s * (r * m);
+        ss += s * masked<kMasked>(s, mask, e);
+        rr += r * masked<kMasked>(r, mask, e);
+        sr += s * masked<kMasked>(r, mask, e);
     }
+}
+
+// rk = Lq - a q - cq q_prev ; sk = pL - a p - cp p_prev ; partial dots ss, rr, sr
+__global__ void k_resid(const double *__restrict__ Lq, const double *__restrict__ pL,
+                        const double *__restrict__ q, const double *__restrict__ p,
+                        const double *__restrict__ qprev, const double *__restrict__ pprev,
+                        const double *__restrict__ mask, const double *__restrict__ scal, long n,
+                        double *__restrict__ rk, double *__restrict__ sk, double *__restrict__ part,
+                        int nblk) {
+    pdl_enter();
+    __shared__ double sh[32];
+    double ss = 0, rr = 0, sr = 0;
+    if (mask)
+        resid_range<true>(Lq, pL, q, p, qprev, pprev, mask, scal, n, rk, sk, ss, rr, sr);
+    else
+        resid_range<false>(Lq, pL, q, p, qprev, pprev, mask, scal, n, rk, sk, ss, rr, sr);
     double t;
     t = block_sum(ss, sh); if (threadIdx.x == 0) part[blockIdx.x] = t;
     t = block_sum(rr, sh); if (threadIdx.x == 0) part[nblk + blockIdx.x] = t;
@@ -308,6 +388,7 @@ __global__ void k_resid(const double *__restrict__ Lq, const double *__restrict_
 
 __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
                           int k, double *__restrict__ scal, double *__restrict__ status) {
+    pdl_enter();
     __shared__ double sh[32];
     double ss = reduce_parts(part, nblk, sh);
     double rr = reduce_parts(part + nblk, nblk, sh);
@@ -321,6 +402,8 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
     scal[SC_C] = c;
     scal[SC_SNORM] = s_norm;
     scal[SC_SRAW] = s_raw;
+    scal[SC_IB] = 1.0 / b;
+    scal[SC_IS] = 1.0 / s_raw;
     bool conv = fabs(b) < kEps || fabs(c) < kEps || scal[SC_NEXT] != 0.0;
     scal[SC_CONV] = conv ? 1.0 : 0.0;
     if (conv) {
@@ -338,9 +421,11 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
 __global__ void k_normalize(const double *__restrict__ rk, const double *__restrict__ sk,
                             const double *__restrict__ scal, long n, double *__restrict__ qn,
                             double *__restrict__ pn) {
+    pdl_enter();
     if (scal[SC_HALT] != 0.0) return;
-    // one reciprocal per vector: float64 division is slow on this part
-    const double ib = 1.0 / scal[SC_B], is = 1.0 / scal[SC_SRAW];
+    // the reciprocals come from k_scal_bc: a float64 division per thread here
+    // cost more than the whole pass
+    const double ib = scal[SC_IB], is = scal[SC_IS];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         qn[e] = rk[e] * ib;
         pn[e] = sk[e] * is;
@@ -350,63 +435,96 @@ __global__ void k_normalize(const double *__restrict__ rk, const double *__restr
 // Full re-biorthogonalisation of the new pair (q_{k+1}, p_{k+1}) against the
 // stored basis: q -= sum_j (p_j.q / p_j.q_j) q_j and p -= sum_j (q_j.p / p_j.q_j) p_j
 // (one classical Gram-Schmidt pass; the recurrence scalars are not changed).
-// The dot products run on a (vectors x kDotChunks) grid of block partials.
-constexpr int kDotChunks = 24;
-__global__ void k_proj_dots(const double *__restrict__ Qb, const double *__restrict__ Pb,
-                            const double *__restrict__ qn, const double *__restrict__ pn,
-                            const double *__restrict__ mask, long n, long ld,
-                            double *__restrict__ part) {
-    __shared__ double sh[32];
-    int j = blockIdx.x;
-    long e0 = n * blockIdx.y / kDotChunks, e1 = n * (blockIdx.y + 1) / kDotChunks;
-    const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
-    double a = 0, b = 0;
-    // four strides' loads issued before their FMAs (the pass streams the whole
-    // basis and is bound by loads in flight); the accumulation order is the
-    // plain strided one
+// The dot products run on a (vectors x chunks) grid of block partials: about
+// four blocks per SM over all vectors (a single vector in 24 chunks was
+// latency-bound at 14 us), but at least 24 chunks of at least eight elements
+// per thread, since every block also pays its float64 tree reductions.
+constexpr int kMaxChunks = 256;
+inline int dot_chunks(long n, int nvec) {
+    int want = ceil_div(4L * 152, std::max(nvec, 1));
+    int cap = std::min(kMaxChunks, ceil_div(n, 256L * 8));
+    return std::max(std::min(24, cap), std::min(want, cap));
+}
+// four strides' loads issued before their FMAs (the pass streams the whole
+// basis and is bound by loads in flight and the float64 pipe); the
+// accumulation order is the plain strided one
+template <bool kMasked>
+__device__ __forceinline__ void proj_dots_range(const double *__restrict__ pj,
+                                                const double *__restrict__ qj,
+                                                const double *__restrict__ qn,
+                                                const double *__restrict__ pn,
+                                                const double *__restrict__ mask, long e0, long e1,
+                                                double &a, double &b) {
     const long bd = blockDim.x;
     long e = e0 + threadIdx.x;
     for (; e + 3 * bd < e1; e += 4 * bd) {
-        double vp[4], vq[4], vqn[4], vpn[4], m[4];
+        double vp[4], vq[4], vqn[4], vpn[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             long x = e + u * bd;
             vp[u] = pj[x];
             vq[u] = qj[x];
-            vqn[u] = qn[x];
-            vpn[u] = pn[x];
-            m[u] = mask ? mask[x] : 1.0;
+            vqn[u] = masked<kMasked>(qn[x], mask, x);
+            vpn[u] = masked<kMasked>(pn[x], mask, x);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            a = fma(vp[u], vqn[u] * m[u], a);
-            b = fma(vq[u], vpn[u] * m[u], b);
+            a = fma(vp[u], vqn[u], a);
+            b = fma(vq[u], vpn[u], b);
         }
     }
     for (; e < e1; e += bd) {
-        double m = mask ? mask[e] : 1.0;
-        a = fma(pj[e], qn[e] * m, a);
-        b = fma(qj[e], pn[e] * m, b);
+        a = fma(pj[e], masked<kMasked>(qn[e], mask, e), a);
+        b = fma(qj[e], masked<kMasked>(pn[e], mask, e), b);
     }
-    double t = block_sum(a, sh);
-    if (threadIdx.x == 0) part[((long)j * kDotChunks + blockIdx.y) * 2] = t;
-    t = block_sum(b, sh);
-    if (threadIdx.x == 0) part[((long)j * kDotChunks + blockIdx.y) * 2 + 1] = t;
 }
 
-// coef[2j], coef[2j+1] = chunk sums / (p_j . q_j)
-__global__ void k_proj_scale(const double *__restrict__ part, const double *__restrict__ pqn,
-                             int nvec, double *__restrict__ coef) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nvec) return;
+__global__ void k_proj_dots(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                            const double *__restrict__ qn, const double *__restrict__ pn,
+                            const double *__restrict__ mask, long n, long ld,
+                            double *__restrict__ part) {
+    pdl_enter();
+    __shared__ double sh[32];
+    int j = blockIdx.x;
+    const long nch = gridDim.y;
+    long e0 = n * blockIdx.y / nch, e1 = n * (blockIdx.y + 1) / nch;
+    const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
     double a = 0, b = 0;
-    for (int c = 0; c < kDotChunks; ++c) {
-        a += part[((long)j * kDotChunks + c) * 2];
-        b += part[((long)j * kDotChunks + c) * 2 + 1];
+    if (mask)
+        proj_dots_range<true>(pj, qj, qn, pn, mask, e0, e1, a, b);
+    else
+        proj_dots_range<false>(pj, qj, qn, pn, mask, e0, e1, a, b);
+    double t = block_sum(a, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2] = t;
+    t = block_sum(b, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2 + 1] = t;
+}
+
+// Sum of the nch chunk partials part[(j * nch + c) * stride + off] by one warp
+// (lane-strided, then a fixed shuffle tree): the same order on every run.
+__device__ __forceinline__ double warp_chunk_sum(const double *__restrict__ part, long j, int nch,
+                                                 int stride, int off) {
+    const int lane = threadIdx.x & 31;
+    double a = 0;
+    for (int c = lane; c < nch; c += 32) a += part[(j * nch + c) * stride + off];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+}
+
+// coef[2j], coef[2j+1] = chunk sums / (p_j . q_j); one warp per j
+__global__ void k_proj_scale(const double *__restrict__ part, const double *__restrict__ pqn,
+                             int nvec, int nch, double *__restrict__ coef) {
+    pdl_enter();
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (j >= nvec) return;   // whole warps
+    double a = warp_chunk_sum(part, j, nch, 2, 0);
+    double b = warp_chunk_sum(part, j, nch, 2, 1);
+    if ((threadIdx.x & 31) == 0) {
+        double inv = 1.0 / pqn[j];
+        coef[2 * j] = a * inv;
+        coef[2 * j + 1] = b * inv;
     }
-    double inv = 1.0 / pqn[j];
-    coef[2 * j] = a * inv;
-    coef[2 * j + 1] = b * inv;
 }
 
 constexpr int kProjMax = 2048;   // coefficients cached in shared memory per pass
@@ -416,6 +534,7 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
                              const double *__restrict__ coef, long n, int j0, int nvec, long ld,
                              double *__restrict__ qn, double *__restrict__ pn,
                              const double *__restrict__ mask, double *__restrict__ pq_part) {
+    pdl_enter();
     __shared__ double cs[2 * kProjMax];
     __shared__ double sh[32];
     for (int t = threadIdx.x; t < 2 * nvec; t += blockDim.x) cs[t] = coef[2 * j0 + t];
@@ -444,7 +563,7 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
         }
         qn[e] = q;
         pn[e] = p;
-        pq = fma(p, q * (mask ? mask[e] : 1.0), pq);
+        if (pq_part) pq = fma(p, mask ? q * mask[e] : q, pq);
     }
     if (pq_part) {
         double t = block_sum(pq, sh);
@@ -455,6 +574,7 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
 // pqn[k] = sum of nblk block partials (one block)
 __global__ void k_pq_reduce(const double *__restrict__ part, int nblk, double *__restrict__ pqn,
                             int k) {
+    pdl_enter();
     __shared__ double sh[32];
     double s = reduce_parts(part, nblk, sh);
     if (threadIdx.x == 0) pqn[k] = s;
@@ -466,23 +586,23 @@ __global__ void k_pq_part(const double *__restrict__ Qb, const double *__restric
                           double *__restrict__ part) {
     __shared__ double sh[32];
     int j = j0 + blockIdx.x;
-    long e0 = n * blockIdx.y / kDotChunks, e1 = n * (blockIdx.y + 1) / kDotChunks;
+    const long nch = gridDim.y;
+    long e0 = n * blockIdx.y / nch, e1 = n * (blockIdx.y + 1) / nch;
     double a = 0;
     for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         double m = mask ? mask[e] : 1.0;
         a = fma(Pb[(long)j * ld + e], Qb[(long)j * ld + e] * m, a);
     }
     double t = block_sum(a, sh);
-    if (threadIdx.x == 0) part[(long)blockIdx.x * kDotChunks + blockIdx.y] = t;
+    if (threadIdx.x == 0) part[(long)blockIdx.x * nch + blockIdx.y] = t;
 }
 
-__global__ void k_pq_finish(const double *__restrict__ part, int cnt, int j0,
+__global__ void k_pq_finish(const double *__restrict__ part, int cnt, int j0, int nch,
                             double *__restrict__ out) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= cnt) return;
-    double a = 0;
-    for (int c = 0; c < kDotChunks; ++c) a += part[(long)j * kDotChunks + c];
-    out[j0 + j] = a;
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (j >= cnt) return;   // whole warps
+    double a = warp_chunk_sum(part, j, nch, 1, 0);
+    if ((threadIdx.x & 31) == 0) out[j0 + j] = a;
 }
 
 // q-space Hermitian re-orthogonalisation tail: q_{k+1} /= |q_{k+1}|, p_{k+1} = q_{k+1}
@@ -684,14 +804,15 @@ static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capac
             if (ctx->rcoef) cudaFree(ctx->rcoef);
             ctx->pqn = ctx->rcoef = nullptr;
             TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
-            TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kDotChunks + 1)));
+            TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kMaxChunks + 1)));
             ctx->pqn_cap = capacity + 1;
         }
         // weights of the vectors already stored
         double *part = ctx->rcoef + 2 * (capacity + 1);
-        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0,
-                                                                    part);
-        k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
+        const int nch = dot_chunks(P, start_step + 1);
+        k_pq_part<<<dim3(start_step + 1, nch), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0, part);
+        k_pq_finish<<<ceil_div(start_step + 1, 8), 256, 0, st>>>(part, start_step + 1, 0, nch,
+                                                                 ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
     if (ctx->stat_cap < capacity + 1) {
@@ -724,29 +845,31 @@ static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capaci
         TDS_TRY(apply_full_L_dev(ctx, p, ctx->pL, 1, precision, st));
         pL = ctx->pL;
     }
-    k_dot1<<<nb, kDotThreads, 0, st>>>(p, ctx->Lq, mask, P, ctx->dots);
-    k_scal_a<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    launch_pdl(k_dot1, nb, kDotThreads, 0, st, p, ctx->Lq, mask, P, ctx->dots);
+    launch_pdl(k_scal_a, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
     const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
     const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
-    k_resid<<<nb, kDotThreads, 0, st>>>(ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
-                                         ctx->rk, ctx->sk, ctx->dots, nb);
-    k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    launch_pdl(k_resid, nb, kDotThreads, 0, st, ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
+               ctx->rk, ctx->sk, ctx->dots, nb);
+    launch_pdl(k_scal_bc, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
     double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
-    k_normalize<<<nbw, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
+    launch_pdl(k_normalize, nbw, kDotThreads, 0, st, ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
     if (full_reorth) {
         int nvec = k + 1;
         double *part = ctx->rcoef + 2 * (capacity + 1);
-        k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_P, qn, pn, mask, P, P,
-                                                            part);
-        k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
+        const int nch = dot_chunks(P, nvec);
+        launch_pdl(k_proj_dots, dim3(nvec, nch), 256, 0, st, basis_Q, basis_P, qn, pn, mask, P, P,
+                   part);
+        launch_pdl(k_proj_scale, ceil_div(nvec, 8), 256, 0, st, part, ctx->pqn, nvec, nch,
+                   ctx->rcoef);
         for (int j0 = 0; j0 < nvec; j0 += kProjMax) {
             bool last = j0 + kProjMax >= nvec;
-            k_proj_apply<<<nbw, 256, 0, st>>>(basis_Q, basis_P, ctx->rcoef, P, j0,
-                                              std::min(kProjMax, nvec - j0), P, qn, pn, mask,
-                                              last ? ctx->dots : nullptr);
+            launch_pdl(k_proj_apply, nbw, 256, 0, st, basis_Q, basis_P, ctx->rcoef, P, j0,
+                       std::min(kProjMax, nvec - j0), P, qn, pn, mask,
+                       last ? ctx->dots : nullptr);
         }
         // weight p_{k+1} . q_{k+1} of the new pair from the apply pass's partials
-        k_pq_reduce<<<1, 512, 0, st>>>(ctx->dots, nbw, ctx->pqn, k + 1);
+        launch_pdl(k_pq_reduce, 1, 512, 0, st, ctx->dots, nbw, ctx->pqn, k + 1);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
@@ -936,7 +1059,7 @@ static int qz_begin(tdscha_qctx *ctx, double *basis_Q, int capacity, int start_s
         TDS_CUDA(cudaMalloc(&ctx->stat_dev, sizeof(double) * (capacity + 1)));
         TDS_CUDA(cudaMallocHost((void **)&ctx->stat_host, sizeof(double) * 10 * (capacity + 1)));
         TDS_CUDA(cudaMalloc(&ctx->pqn, sizeof(double) * (capacity + 1)));
-        TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kDotChunks + 1)));
+        TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kMaxChunks + 1)));
         ctx->hist_cap = capacity + 1;
     }
     TDS_CUDA(cudaMemcpyAsync(ctx->hist_dev, hist, sizeof(double) * 4 * (start_step + 1),
@@ -944,8 +1067,10 @@ static int qz_begin(tdscha_qctx *ctx, double *basis_Q, int capacity, int start_s
     double *part = ctx->rcoef + 2 * (capacity + 1);
     if (reorthogonalize) {
         // Q is orthonormal in the mask product; the weights q_j . q_j are kept exact
-        k_pq_part<<<dim3(start_step + 1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, ctx->mask, n, n, 0, part);
-        k_pq_finish<<<ceil_div(start_step + 1, 128), 128, 0, st>>>(part, start_step + 1, 0, ctx->pqn);
+        const int nch = dot_chunks(n, start_step + 1);
+        k_pq_part<<<dim3(start_step + 1, nch), 256, 0, st>>>(basis_Q, basis_Q, ctx->mask, n, n, 0, part);
+        k_pq_finish<<<ceil_div(start_step + 1, 8), 256, 0, st>>>(part, start_step + 1, 0, nch,
+                                                                 ctx->pqn);
         TDS_CHECK_LAUNCH();
     }
     TDS_CUDA(cudaMemsetAsync(ctx->scal, 0, sizeof(double) * 64, st));
@@ -976,16 +1101,17 @@ static int qz_step(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capac
         // real mask product (the p side of the shared kernels runs on the
         // p_{k+1} slot, which the renormalisation then overwrites)
         int nvec = k + 1;
-        k_proj_dots<<<dim3(nvec, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, qn, pn, mask, n, n, part);
-        k_proj_scale<<<ceil_div(nvec, 128), 128, 0, st>>>(part, ctx->pqn, nvec, ctx->rcoef);
+        const int nch = dot_chunks(n, nvec);
+        k_proj_dots<<<dim3(nvec, nch), 256, 0, st>>>(basis_Q, basis_Q, qn, pn, mask, n, n, part);
+        k_proj_scale<<<ceil_div(nvec, 8), 256, 0, st>>>(part, ctx->pqn, nvec, nch, ctx->rcoef);
         for (int j0 = 0; j0 < nvec; j0 += kProjMax)
             k_proj_apply<<<nb, 256, 0, st>>>(basis_Q, basis_Q, ctx->rcoef, n, j0,
                                              std::min(kProjMax, nvec - j0), n, qn, pn, nullptr,
                                              nullptr);
         k_dot1<<<nb, kDotThreads, 0, st>>>(qn, qn, mask, n, ctx->dots);
         k_qrenorm<<<nb, kDotThreads, 0, st>>>(ctx->dots, nb, ctx->scal, ctx->hist_dev, k, n, qn, pn);
-        k_pq_part<<<dim3(1, kDotChunks), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);
-        k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, ctx->pqn);
+        k_pq_part<<<dim3(1, nch), 256, 0, st>>>(basis_Q, basis_Q, mask, n, n, k + 1, part);
+        k_pq_finish<<<1, 32, 0, st>>>(part, 1, k + 1, nch, ctx->pqn);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { set_error("qlanczos_run launch: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }

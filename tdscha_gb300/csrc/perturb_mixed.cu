@@ -308,6 +308,9 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // barriers and TMEM are set up; global memory only after the kernels
+    // before this one in the stream have completed
+    pdl_enter();
     int fail_code = 0;
 
     if (warp == 4) {
@@ -482,7 +485,13 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
                         }
                     }
                     ++consumed;
-                    // every epilogue thread is done with buffer e: refill it
+                    // every epilogue thread is done with buffer e: refill it.
+                    // The reads above are generic-proxy and the refill is a TMA
+                    // write (async proxy); the barrier alone does not order the
+                    // two, and a refill that landed before a slow warp's loads
+                    // had read the part gave wrong d values in a few rows of one
+                    // tile in about one call in 1500 (M=573, N=20 000)
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     asm volatile("bar.sync 1, 128;" ::: "memory");
                     if (leader) issue_next();
                 }
@@ -583,6 +592,9 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // barriers and TMEM are set up; global memory only after the kernels
+    // before this one in the stream have completed
+    pdl_enter();
     int fail_code = 0;
 
     if (warp == 4) {
@@ -843,6 +855,7 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
                           __half *__restrict__ y_lo, float *__restrict__ tcol,
                           float *__restrict__ vs, float *__restrict__ vt,
                           float *__restrict__ absmax) {
+    pdl_enter();
     __shared__ float red[32];
     int n = blockIdx.x;
     float mx = 0.f;
@@ -881,6 +894,7 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
 __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, int S,
                              const double *__restrict__ rho, int apply_d4,
                              float4 *__restrict__ abcc, float *__restrict__ absmax) {
+    pdl_enter();
     long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
     float ma = 0.f, mb = 0.f;
     if (r < R) {
@@ -941,6 +955,7 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
                                                 __half *__restrict__ wt_lo,
                                                 float *__restrict__ sw_out,
                                                 float *__restrict__ fpart) {
+    pdl_enter();
     __shared__ float red[kWRows][8];
     int b0 = blockIdx.x * kWRows;
     long r0 = (long)blockIdx.y * kWChunk;
@@ -1038,6 +1053,7 @@ __global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart,
                                                 int ldG, int M, const float *__restrict__ fpart,
                                                 int nfchunk, double norm, double *__restrict__ f,
                                                 double *__restrict__ d2v) {
+    pdl_enter();
     __shared__ double tr[32][9];    // G over rows b of tile B, the slab's 8 columns a: [b][a]
     __shared__ double red[8][33];
     // (pair, slab): pair index -> (A, B), A <= B, row-major over the upper
@@ -1311,9 +1327,8 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
     {
         ProfScope ps(c, 5, st);
-        k_prep_y1<<<Mp, 256, 0, st>>>(c->Y1, c->R1, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi,
-                                      mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_prep_y1, Mp, 256, 0, st, c->Y1, c->R1, c->fY, c->fpsi, x->sd, M, Mp,
+                            mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
     }
     StageAArgs ga{};
     ga.R = R;
@@ -1331,21 +1346,18 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 0, st);
         int grid = (int)std::min<long>(ga.ntiles, x->nsm);
-        k_stageA_tc<<<grid, 192, kPSmem, st>>>(x->tmA, x->te, ga);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_stageA_tc, grid, 192, kPSmem, st, x->tmA, x->te, ga));
     }
     {
         ProfScope ps(c, 1, st);
-        k_rows_mixed<<<ceil_div(R, 128), 128, 0, st>>>(mx.qp, mx.nctile, R, c->S, c->rho, apply_d4,
-                                                        x->abcc, x->absmax);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_rows_mixed, ceil_div(R, 128), 128, 0, st, mx.qp, mx.nctile, R, c->S,
+                            c->rho, apply_d4, x->abcc, x->absmax));
     }
     {
         ProfScope ps(c, 2, st);
         dim3 g(ceil_div(M, kWRows), x->nfchunk);
-        k_wbuild<<<g, 256, 0, st>>>(mx.ft32, mx.ut32, x->abcc, x->absmax, x->fmx, x->su, R, Rp, M,
-                                    mx.wt_hi, mx.wt_lo, x->sw, x->fpart);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_wbuild, g, 256, 0, st, mx.ft32, mx.ut32, x->abcc, x->absmax, x->fmx,
+                            x->su, R, Rp, M, mx.wt_hi, mx.wt_lo, x->sw, x->fpart));
     }
     StageBArgs gb{};
     gb.nkb = x->kbps;
@@ -1362,15 +1374,13 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     {
         ProfScope ps(c, 3, st);
         int grid = (int)std::min<long>(gb.nitems, x->nsm);
-        k_stageB_tc<<<grid, 192, kQSmem, st>>>(x->tmB, gb);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_stageB_tc, grid, 192, kQSmem, st, x->tmB, gb));
     }
     {
         ProfScope ps(c, 4, st);
         const int nt = ceil_div(M, 32);
-        k_gfinal<<<4 * (nt * (nt + 1) / 2), 256, 0, st>>>(mx.gpart, mx.nsplit, x->ldG, M, x->fpart,
-                                                    x->nfchunk, c->sum_rho * c->S, c->f, c->d2v);
-        TDS_CHECK_LAUNCH();
+        TDS_CUDA(launch_pdl(k_gfinal, 4 * (nt * (nt + 1) / 2), 256, 0, st, mx.gpart, mx.nsplit,
+                            x->ldG, M, x->fpart, x->nfchunk, c->sum_rho * c->S, c->f, c->d2v));
     }
     return TDSCHA_OK;
 }

@@ -109,3 +109,26 @@ def test_bounded_wait_reports_timeout_and_context_survives(gpu_lib, monkeypatch)
                                            ens["T"], 1, syms, spaces, bid)
     assert rel(d2v, d_ref) <= TOL_CALL
     ctx.close()
+
+
+def test_mixed_repeat_bitwise_identical(gpu_lib):
+    """Thousands of back-to-back calls on the same inputs give the same bits.
+    The stage A epilogue refills its d / g part buffers by TMA right after the
+    warps' shared-memory reads; without a proxy fence before the refill about
+    one call in 1500 read part of a refilled buffer (wrong q / s row dots in a
+    few rows of one tile, errors near 4e-4). 4000 calls catch that rate with
+    probability about 0.94."""
+    M, N = 573, 20000
+    ens = make_ensemble(M, N, seed=2024, rho_sigma=0.1)
+    syms, spaces, bid = oracle.identity_symmetries(M)
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    R1, Y1 = random_R1(M, 5), random_sym(M, 6, scale=1e-3)
+    f0, d0 = _mixed_call(ctx, R1, Y1)
+    bad = []
+    for i in range(4000):
+        f, d2v = _mixed_call(ctx, R1, Y1)
+        if not (np.array_equal(f, f0) and np.array_equal(d2v, d0)):
+            bad.append((i, rel(f, f0), rel(d2v, d0)))
+    ctx.close()
+    assert not bad, "calls with different results (index, rel f, rel d2v): %s" % bad[:5]
