@@ -92,11 +92,12 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append((time.time(), line.strip()))
 
-    def wait_first(self, timeout=3.0):
-        """Block until the first sample arrived: nvidia-smi's start-up (NVML
-        initialisation) then lies before the timed region, not inside it."""
+    def wait_first(self, n=3, timeout=3.0):
+        """Block until n samples arrived: nvidia-smi's start-up (NVML
+        initialisation, and whatever it still does right after its first
+        sample) then lies before the timed region, not inside it."""
         t0 = time.time()
-        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+        while self.proc is not None and len(self.lines) < n and time.time() - t0 < timeout:
             time.sleep(0.01)
 
     def stop(self, t0=None, t1=None):
