@@ -81,6 +81,7 @@ struct tdscha_ctx {
     int with_mixed = 0;
     // operator options
     int use_wigner = 1, ignore_harmonic = 0, ignore_v3 = 0, ignore_v4 = 0, reverse_L = 0;
+    int pc_wigner = -1;          // representation the pair coefficients were built for
     double shift = 0;
     // per-mode (device)
     double *w = nullptr, *fY = nullptr, *fpsi = nullptr, *rho = nullptr;

@@ -232,7 +232,7 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     TRYC(alloc_fp64_scratch(c));
     TRYC(dev_alloc(&c->Lq, c->P)); TRYC(dev_alloc(&c->pL, c->P));
     TRYC(dev_alloc(&c->rk, c->P)); TRYC(dev_alloc(&c->sk, c->P));
-    TRYC(dev_alloc(&c->mask, c->P)); TRYC(dev_alloc(&c->pc, 12 * c->H + 2 * (size_t)M * M));
+    TRYC(dev_alloc(&c->mask, c->P)); TRYC(dev_alloc(&c->pc, 12 * c->H + 4 * (size_t)M));
     c->nblk_dot = 296;    // block partials of the fused dot kernels (two blocks per SM)
     TRYC(dev_alloc(&c->dots, 4 * (size_t)std::max(c->nblk_dot, 1216))); TRYC(dev_alloc(&c->scal, 64));
     CUC(cudaMemset(c->scal, 0, sizeof(double) * 64));
@@ -277,7 +277,9 @@ extern "C" int tdscha_ctx_set_options(tdscha_ctx *ctx, int use_wigner, int ignor
     ctx->ignore_v4 = ignore_v4 != 0;
     ctx->reverse_L = reverse_L != 0;
     ctx->shift = shift_value;
-    return build_pair_coeffs(ctx);
+    // the pair coefficients depend only on the representation (and the
+    // context's frequencies and temperature)
+    return ctx->pc_wigner == ctx->use_wigner ? TDSCHA_OK : build_pair_coeffs(ctx);
 }
 
 namespace tdscha {

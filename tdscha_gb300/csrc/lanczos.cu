@@ -22,94 +22,108 @@ enum { PC_X = 0, PC_Y, PC_X1, PC_Y1, PC_UA, PC_UB, PC_RA, PC_RB, PC_TY, PC_TRA, 
 int run_perturb(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st);
 int run_perturb_sym(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st);
 
+__device__ __forceinline__ long tri_index(int i, int j, int M) {
+    return (long)i * M - (long)i * (i - 1) / 2 + (j - i);
+}
+
+// Per-pair coefficient arrays, the ψ-layout index tables and the Wigner mask,
+// one thread per mode pair (i <= j, row i over blockIdx.y).  Per-mode inputs
+// (w, the two Bose-factor forms, f_Y and the ReA weight) come from the host.
+__global__ void k_pair_coeffs(const double *__restrict__ w, const double *__restrict__ bdiv,
+                              const double *__restrict__ bmul, const double *__restrict__ yw,
+                              const double *__restrict__ reaw, int M, long H, int wigner,
+                              double *__restrict__ pc, int *__restrict__ tri,
+                              double *__restrict__ mask) {
+    for (int i = blockIdx.y; i < M; i += gridDim.y)
+    for (int j = i + blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+        const long k = tri_index(i, j, M);
+        const double wa = w[j], wb = w[i];          // i_a = column, i_b = row (:2338-2346)
+        const double na = bdiv[j], nbb = bdiv[i];
+        const double den = (2 * na + 1) * (2 * nbb + 1);
+        if (!wigner) {
+            double X_ab = -wa * wa - wb * wb - (2 * wa * wb) / den;
+            double Y_ab = -(8 * wa * wb) / den;
+            double X1_ab = -(2 * na * nbb + na + nbb) * (2 * na * nbb + na + nbb + 1) * (2 * wa * wb) / den;
+            double Y1_ab = -wa * wa - wb * wb + (2 * wa * wb) / den;
+            pc[PC_X * H + k] = -X_ab;
+            pc[PC_Y * H + k] = -Y_ab;
+            pc[PC_X1 * H + k] = -X1_ab;
+            pc[PC_Y1 * H + k] = -Y1_ab;
+        } else {
+            pc[PC_X * H + k] = -(wa * wa + wb * wb - 2. * wa * wb);
+            pc[PC_Y * H + k] = 0.0;
+            pc[PC_X1 * H + k] = 0.0;
+            pc[PC_Y1 * H + k] = -(wa * wa + wb * wb + 2. * wa * wb);
+        }
+        // Wigner change of variables a', b' -> alpha (:2818-2839)
+        const double Xf = ((1 + 2 * na) * (1 + 2 * nbb) / 8);
+        const double w2_on_X = (wa * wb) / Xf;
+        const double chi_m = ((wa - wb) * (na - nbb)) / (2 * wa * wb);
+        const double chi_p = ((wa + wb) * (1 + na + nbb)) / (2 * wa * wb);
+        pc[PC_UA * H + k] = w2_on_X * sqrt(-0.5 * chi_m);
+        pc[PC_UB * H + k] = w2_on_X * sqrt(+0.5 * chi_p);
+        // repack factors from get_chi_minus / get_chi_plus (row i, column j)
+        const double ni = bmul[i], nj = bmul[j];
+        const double cm = ((w[j] - w[i]) * (nj - ni)) / ((2. * w[j]) * w[i]);
+        const double cp = ((w[j] + w[i]) * (1 + nj + ni)) / ((2. * w[j]) * w[i]);
+        pc[PC_RA * H + k] = sqrt(-0.5 * cm);
+        pc[PC_RB * H + k] = -sqrt(+0.5 * cp);
+        // transpose rescaling coefficients (:3036-3050), [a=i][b=j], times the
+        // half weight of an off-diagonal pair (exact: a power of two), so the
+        // unpack multiplies each entry once
+        const double cY = yw[i] * yw[j] * yw[j] + yw[i] * yw[i] * yw[j];
+        const double cRA = yw[i] * reaw[j] * yw[j] + yw[i] * reaw[i] * yw[j];
+        const double h = (i != j) ? 0.5 : 1.0;
+        pc[PC_TY * H + k] = (cY * 2) * h;
+        pc[PC_TRA * H + k] = (cRA * 2) * h;
+        pc[PC_I * H + k] = i;
+        pc[PC_J * H + k] = j;
+        tri[2 * k] = i;
+        tri[2 * k + 1] = j;
+        // Wigner double-counting mask (mask_dot_wigner, :5905-5954)
+        const double m = (i < j) ? 2.0 : 1.0;
+        mask[M + k] = m;
+        mask[M + H + k] = m;
+        if (i == 0) mask[j] = 1.0;
+    }
+}
+
 int build_pair_coeffs(tdscha_ctx *c) {
     const int M = c->M;
     const long H = c->H;
     std::vector<double> w(M);
     TDS_CUDA(cudaMemcpy(w.data(), c->w, sizeof(double) * M, cudaMemcpyDeviceToHost));
-    std::vector<double> pc(12 * H);
     const double T = c->T;
     // Bose factors as apply_L1_FT writes them (division form, :2363-2366)
     auto nb_div = [&](double x) { return T > 0 ? 1 / (exp(x / (T / kRyToK)) - 1) : 0.0; };
     // and as get_chi_minus/plus write them (multiplication form, :2650-2652)
     auto nb_mul = [&](double x) { return T > kEps ? 1.0 / (exp(x * 157887.32400374097 / T) - 1.0) : 0.0; };
-    std::vector<double> yw(M), reaw(M), bdiv(M), bmul(M);
+    // per-mode inputs of the pair kernel: [bdiv | bmul | yw | reaw], and 1 / yw
+    std::vector<double> pm(4 * (size_t)M), ywinv(M);
     for (int m = 0; m < M; ++m) {
         double n_mu = T > kEps ? 1.0 / (exp(w[m] * 157887.32400374097 / T) - 1.0) : 0.0;
-        yw[m] = 2 * w[m] / (2 * n_mu + 1);
-        reaw[m] = 2 * w[m] * n_mu * (n_mu + 1) / (2 * n_mu + 1);
-        // per-mode Bose factors, looked up by the pair loop below
-        bdiv[m] = nb_div(w[m]);
-        bmul[m] = nb_mul(w[m]);
+        double yw = 2 * w[m] / (2 * n_mu + 1);
+        pm[m] = nb_div(w[m]);
+        pm[M + m] = nb_mul(w[m]);
+        pm[2 * M + m] = yw;
+        pm[3 * M + m] = 2 * w[m] * n_mu * (n_mu + 1) / (2 * n_mu + 1);
+        ywinv[m] = 1.0 / yw;
     }
-    long k = 0;
-    for (int i = 0; i < M; ++i) {
-        for (int j = i; j < M; ++j, ++k) {
-            double wa = w[j], wb = w[i];          // i_a = column, i_b = row (:2338-2346)
-            double na = bdiv[j], nbb = bdiv[i];
-            double den = (2 * na + 1) * (2 * nbb + 1);
-            if (!c->use_wigner) {
-                double X_ab = -wa * wa - wb * wb - (2 * wa * wb) / den;
-                double Y_ab = -(8 * wa * wb) / den;
-                double X1_ab = -(2 * na * nbb + na + nbb) * (2 * na * nbb + na + nbb + 1) * (2 * wa * wb) / den;
-                double Y1_ab = -wa * wa - wb * wb + (2 * wa * wb) / den;
-                pc[PC_X * H + k] = -X_ab;
-                pc[PC_Y * H + k] = -Y_ab;
-                pc[PC_X1 * H + k] = -X1_ab;
-                pc[PC_Y1 * H + k] = -Y1_ab;
-            } else {
-                pc[PC_X * H + k] = -(wa * wa + wb * wb - 2. * wa * wb);
-                pc[PC_Y1 * H + k] = -(wa * wa + wb * wb + 2. * wa * wb);
-            }
-            // Wigner change of variables a', b' -> alpha (:2818-2839)
-            double Xf = ((1 + 2 * na) * (1 + 2 * nbb) / 8);
-            double w2_on_X = (wa * wb) / Xf;
-            double chi_m = ((wa - wb) * (na - nbb)) / (2 * wa * wb);
-            double chi_p = ((wa + wb) * (1 + na + nbb)) / (2 * wa * wb);
-            pc[PC_UA * H + k] = w2_on_X * sqrt(-0.5 * chi_m);
-            pc[PC_UB * H + k] = w2_on_X * sqrt(+0.5 * chi_p);
-            // repack factors from get_chi_minus / get_chi_plus (row i, column j)
-            double ni = bmul[i], nj = bmul[j];
-            double cm = ((w[j] - w[i]) * (nj - ni)) / ((2. * w[j]) * w[i]);
-            double cp = ((w[j] + w[i]) * (1 + nj + ni)) / ((2. * w[j]) * w[i]);
-            pc[PC_RA * H + k] = sqrt(-0.5 * cm);
-            pc[PC_RB * H + k] = -sqrt(+0.5 * cp);
-            // transpose rescaling coefficients (:3036-3050), [a=i][b=j]
-            double cY = yw[i] * yw[j] * yw[j] + yw[i] * yw[i] * yw[j];
-            double cRA = yw[i] * reaw[j] * yw[j] + yw[i] * reaw[i] * yw[j];
-            // times the half weight of an off-diagonal pair (exact: a power of
-            // two), so the unpack multiplies each entry once
-            double h = (i != j) ? 0.5 : 1.0;
-            pc[PC_TY * H + k] = (cY * 2) * h;
-            pc[PC_TRA * H + k] = (cRA * 2) * h;
-            pc[PC_I * H + k] = i;
-            pc[PC_J * H + k] = j;
-        }
-    }
-    TDS_CUDA(cudaMemcpy(c->pc, pc.data(), sizeof(double) * 12 * H, cudaMemcpyHostToDevice));
-    std::vector<int> tri(2 * H);
-    std::vector<double> ywinv(M);
-    k = 0;
-    for (int i = 0; i < M; ++i)
-        for (int j = i; j < M; ++j, ++k) { tri[2 * k] = i; tri[2 * k + 1] = j; }
-    for (int m = 0; m < M; ++m) ywinv[m] = 1.0 / yw[m];
     if (!c->tri) TDS_CUDA(cudaMalloc(&c->tri, sizeof(int) * 2 * H));
     if (!c->Ywinv) TDS_CUDA(cudaMalloc(&c->Ywinv, sizeof(double) * M));
-    TDS_CUDA(cudaMemcpy(c->tri, tri.data(), sizeof(int) * 2 * H, cudaMemcpyHostToDevice));
+    // the per-mode inputs go through the 4 M doubles past the 12 H coefficients
+    double *d_pm = c->pc + 12 * H;
+    TDS_CUDA(cudaMemcpy(d_pm, pm.data(), sizeof(double) * 4 * M, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->Ywinv, ywinv.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
-    // Wigner double-counting mask (mask_dot_wigner, :5905-5954)
-    std::vector<double> mask(c->P, 1.0);
-    k = 0;
-    for (int i = 0; i < M; ++i)
-        for (int j = i; j < M; ++j, ++k)
-            if (i < j) { mask[M + k] = 2; mask[M + H + k] = 2; }
-    TDS_CUDA(cudaMemcpy(c->mask, mask.data(), sizeof(double) * c->P, cudaMemcpyHostToDevice));
+    dim3 g(ceil_div(M, 128), std::min(M, 65535));
+    k_pair_coeffs<<<g, 128>>>(c->w, d_pm, d_pm + M, d_pm + 2 * M, d_pm + 3 * M, M, H,
+                              c->use_wigner, c->pc, c->tri, c->mask);
+    TDS_CHECK_LAUNCH();
+    TDS_CUDA(cudaDeviceSynchronize());
+    c->pc_wigner = c->use_wigner;
     return TDSCHA_OK;
 }
 
-__device__ __forceinline__ long tri_index(int i, int j, int M) {
-    return (long)i * M - (long)i * (i - 1) / 2 + (j - i);
-}
 
 __global__ void k_unpack(const double *__restrict__ psi, const double *__restrict__ pc, int M,
                          long H, int wigner, int transpose, int ignore_v3,
