@@ -184,6 +184,22 @@ int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t s
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 
+// Device buffers of contexts come from a process-wide cache of freed blocks,
+// reused by exact size: applications create and destroy contexts of the same
+// shapes over and over (one per ensemble, perturbation or q-point), and
+// cudaMalloc / cudaFree of a context's buffers cost about 4 ms of a 22 ms
+// 20-step run at M=573, N=50 000.  At most 16 GiB stay cached (larger
+// surpluses go back to the driver), and an allocation that fails empties the
+// cache and retries once.  cached_free of a pointer that did not come from
+// cached_malloc calls cudaFree.  A block is cached only after its last use:
+// callers free after synchronising.
+cudaError_t cached_malloc(void **p, size_t bytes);
+void cached_free(void *p);
+template <typename T>
+inline cudaError_t cached_malloc(T **p, size_t bytes) {
+    return cached_malloc(reinterpret_cast<void **>(p), bytes);
+}
+
 // Programmatic dependent launch.  A kernel started by launch_pdl is scheduled
 // as the blocks of the kernel before it in the stream exit, so its launch and
 // block set-up (and the barrier / TMEM set-up of the persistent kernels) hide

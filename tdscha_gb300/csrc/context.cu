@@ -4,6 +4,10 @@
 #include <cstdarg>
 #include <cstring>
 
+#include <map>
+#include <mutex>
+#include <unordered_map>
+
 #include "common.cuh"
 
 namespace tdscha {
@@ -83,6 +87,66 @@ static void prof_clear(tdscha_ctx *c) {
     }
 }
 
+namespace {
+struct BlockCache {
+    std::mutex mu;
+    std::unordered_map<void *, std::pair<int, size_t>> live;   // block -> (device, bytes)
+    std::multimap<std::pair<int, size_t>, void *> idle;        // (device, bytes) -> block
+    size_t idle_bytes = 0;
+};
+BlockCache &block_cache() {
+    static BlockCache *bc = new BlockCache();   // never destroyed: no cudaFree at exit
+    return *bc;
+}
+constexpr size_t kCacheCap = size_t(16) << 30;
+}  // namespace
+
+cudaError_t tdscha::cached_malloc(void **p, size_t bytes) {
+    if (bytes == 0) bytes = 1;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    auto it = bc.idle.find({dev, bytes});
+    if (it != bc.idle.end()) {
+        *p = it->second;
+        bc.idle.erase(it);
+        bc.idle_bytes -= bytes;
+        bc.live[*p] = {dev, bytes};
+        return cudaSuccess;
+    }
+    e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && !bc.idle.empty()) {
+        cudaGetLastError();
+        for (auto &kv : bc.idle) cudaFree(kv.second);
+        bc.idle.clear();
+        bc.idle_bytes = 0;
+        e = cudaMalloc(p, bytes);
+    }
+    if (e == cudaSuccess) bc.live[*p] = {dev, bytes};
+    return e;
+}
+
+void tdscha::cached_free(void *p) {
+    if (!p) return;
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    auto it = bc.live.find(p);
+    if (it == bc.live.end()) {
+        cudaFree(p);
+        return;
+    }
+    auto key = it->second;
+    bc.live.erase(it);
+    if (bc.idle_bytes + key.second > kCacheCap) {
+        cudaFree(p);
+        return;
+    }
+    bc.idle.insert({key, p});
+    bc.idle_bytes += key.second;
+}
+
 static void ctx_free(tdscha_ctx *c) {
     if (!c) return;
     prof_clear(c);
@@ -92,10 +156,9 @@ static void ctx_free(tdscha_ctx *c) {
                       c->c2, c->gpart, c->fpart, c->Lq, c->pL, c->rk, c->sk, c->mask,
                       c->dots, c->scal, c->hist_dev, c->pqn, c->rcoef, c->Ywinv,
                       c->stat_dev};
-    for (double *p : bufs)
-        if (p) cudaFree(p);
-    if (c->tri) cudaFree(c->tri);
-    if (c->lam_static) cudaFree(c->lam_static);
+    for (double *p : bufs) cached_free(p);
+    cached_free(c->tri);
+    cached_free(c->lam_static);
     free_translations(c);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
     if (c->stat_host) cudaFreeHost(c->stat_host);
@@ -104,7 +167,7 @@ static void ctx_free(tdscha_ctx *c) {
 
 template <typename T>
 static int dev_alloc(T **p, size_t count) {
-    TDS_CUDA(cudaMalloc((void **)p, sizeof(T) * (count ? count : 1)));
+    TDS_CUDA(cached_malloc(p, sizeof(T) * (count ? count : 1)));
     return TDSCHA_OK;
 }
 
@@ -222,8 +285,9 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
             goto fail;
         }
     }
-    cudaFree(d_X); cudaFree(d_Y); cudaFree(d_ndeg); cudaFree(d_degoff); cudaFree(d_symoff);
-    cudaFree(d_space); cudaFree(d_bid); cudaFree(d_sym); cudaFree(d_bad);
+    cached_free(d_X); cached_free(d_Y); cached_free(d_ndeg); cached_free(d_degoff);
+    cached_free(d_symoff); cached_free(d_space); cached_free(d_bid); cached_free(d_sym);
+    cached_free(d_bad);
     d_X = d_Y = nullptr; d_ndeg = d_degoff = d_space = d_bid = nullptr; d_symoff = nullptr; d_sym = nullptr;
     d_bad = nullptr;
 
@@ -243,15 +307,10 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     *out = c;
     return TDSCHA_OK;
 fail:
-    if (d_X) cudaFree(d_X);
-    if (d_Y) cudaFree(d_Y);
-    if (d_ndeg) cudaFree(d_ndeg);
-    if (d_degoff) cudaFree(d_degoff);
-    if (d_symoff) cudaFree(d_symoff);
-    if (d_space) cudaFree(d_space);
-    if (d_bid) cudaFree(d_bid);
-    if (d_sym) cudaFree(d_sym);
-    if (d_bad) cudaFree(d_bad);
+    cudaDeviceSynchronize();
+    cached_free(d_X); cached_free(d_Y); cached_free(d_ndeg); cached_free(d_degoff);
+    cached_free(d_symoff); cached_free(d_space); cached_free(d_bid); cached_free(d_sym);
+    cached_free(d_bad);
     ctx_free(c);
     return rc;
 #undef TRYC

@@ -109,8 +109,8 @@ int build_pair_coeffs(tdscha_ctx *c) {
         pm[3 * M + m] = 2 * w[m] * n_mu * (n_mu + 1) / (2 * n_mu + 1);
         ywinv[m] = 1.0 / yw;
     }
-    if (!c->tri) TDS_CUDA(cudaMalloc(&c->tri, sizeof(int) * 2 * H));
-    if (!c->Ywinv) TDS_CUDA(cudaMalloc(&c->Ywinv, sizeof(double) * M));
+    if (!c->tri) TDS_CUDA(cached_malloc(&c->tri, sizeof(int) * 2 * H));
+    if (!c->Ywinv) TDS_CUDA(cached_malloc(&c->Ywinv, sizeof(double) * M));
     // the per-mode inputs go through the 4 M doubles past the 12 H coefficients
     double *d_pm = c->pc + 12 * H;
     TDS_CUDA(cudaMemcpy(d_pm, pm.data(), sizeof(double) * 4 * M, cudaMemcpyHostToDevice));

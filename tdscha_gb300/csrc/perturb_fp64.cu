@@ -250,13 +250,13 @@ int alloc_fp64_scratch(tdscha_ctx *c) {
     }
     c->nsplit64 = ns;
     c->nfchunk = (int)std::min<long>(std::max<long>(1, R / 256), 512);
-    TDS_CUDA(cudaMalloc(&c->qp_part, sizeof(double) * 2 * c->nct64 * R));
-    TDS_CUDA(cudaMalloc(&c->alpha, sizeof(double) * R));
-    TDS_CUDA(cudaMalloc(&c->beta, sizeof(double) * R));
-    TDS_CUDA(cudaMalloc(&c->c1, sizeof(double) * R));
-    TDS_CUDA(cudaMalloc(&c->c2, sizeof(double) * R));
-    TDS_CUDA(cudaMalloc(&c->gpart, sizeof(double) * (size_t)ns * M * M));
-    TDS_CUDA(cudaMalloc(&c->fpart, sizeof(double) * (size_t)c->nfchunk * M));
+    TDS_CUDA(cached_malloc(&c->qp_part, sizeof(double) * 2 * c->nct64 * R));
+    TDS_CUDA(cached_malloc(&c->alpha, sizeof(double) * R));
+    TDS_CUDA(cached_malloc(&c->beta, sizeof(double) * R));
+    TDS_CUDA(cached_malloc(&c->c1, sizeof(double) * R));
+    TDS_CUDA(cached_malloc(&c->c2, sizeof(double) * R));
+    TDS_CUDA(cached_malloc(&c->gpart, sizeof(double) * (size_t)ns * M * M));
+    TDS_CUDA(cached_malloc(&c->fpart, sizeof(double) * (size_t)c->nfchunk * M));
     return TDSCHA_OK;
 }
 

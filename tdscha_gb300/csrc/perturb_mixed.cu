@@ -1221,25 +1221,25 @@ int mixed_prepare(tdscha_ctx *c) {
     mx.nsplit = ceil_div(x->nkbB, x->kbps);
     x->nfchunk = ceil_div(R, kWChunk);
     size_t rowN = (size_t)R * Mp, colN = (size_t)Mp * Rp;
-    TDS_CUDA(cudaMalloc(&mx.d_hi, 2 * rowN));
-    TDS_CUDA(cudaMalloc(&mx.d_lo, 2 * rowN));
-    TDS_CUDA(cudaMalloc(&x->d32, 4 * rowN));
-    TDS_CUDA(cudaMalloc(&mx.g32, 4 * rowN));
-    TDS_CUDA(cudaMalloc(&mx.ut_hi, 2 * colN));
-    TDS_CUDA(cudaMalloc(&mx.ut_lo, 2 * colN));
-    TDS_CUDA(cudaMalloc(&mx.ut32, 4 * colN));
-    TDS_CUDA(cudaMalloc(&mx.ft32, 4 * colN));
-    TDS_CUDA(cudaMalloc(&mx.wt_hi, 2 * colN));
-    TDS_CUDA(cudaMalloc(&mx.wt_lo, 2 * colN));
-    TDS_CUDA(cudaMalloc(&mx.y1_hi, 2 * (size_t)Mp * Mp));
-    TDS_CUDA(cudaMalloc(&mx.y1_lo, 2 * (size_t)Mp * Mp));
-    TDS_CUDA(cudaMalloc(&mx.qp, sizeof(float) * 4 * mx.nctile * R));
-    TDS_CUDA(cudaMalloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldG));
+    TDS_CUDA(cached_malloc(&mx.d_hi, 2 * rowN));
+    TDS_CUDA(cached_malloc(&mx.d_lo, 2 * rowN));
+    TDS_CUDA(cached_malloc(&x->d32, 4 * rowN));
+    TDS_CUDA(cached_malloc(&mx.g32, 4 * rowN));
+    TDS_CUDA(cached_malloc(&mx.ut_hi, 2 * colN));
+    TDS_CUDA(cached_malloc(&mx.ut_lo, 2 * colN));
+    TDS_CUDA(cached_malloc(&mx.ut32, 4 * colN));
+    TDS_CUDA(cached_malloc(&mx.ft32, 4 * colN));
+    TDS_CUDA(cached_malloc(&mx.wt_hi, 2 * colN));
+    TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * colN));
+    TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * mx.nctile * R));
+    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldG));
     float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw, &x->tcol, &x->vs, &x->vt};
-    for (float **v : vecs) TDS_CUDA(cudaMalloc(v, sizeof(float) * Mp));
-    TDS_CUDA(cudaMalloc(&x->absmax, sizeof(float) * 2));
-    TDS_CUDA(cudaMalloc(&x->abcc, sizeof(float4) * R));
-    TDS_CUDA(cudaMalloc(&x->fpart, sizeof(float) * (size_t)x->nfchunk * M));
+    for (float **v : vecs) TDS_CUDA(cached_malloc(v, sizeof(float) * Mp));
+    TDS_CUDA(cached_malloc(&x->absmax, sizeof(float) * 2));
+    TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * R));
+    TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)x->nfchunk * M));
     TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
     *mx.err_flag = 0;
     TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * colN));
@@ -1247,7 +1247,7 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * Mp));
     {
         float *dmax = nullptr;
-        TDS_CUDA(cudaMalloc(&dmax, sizeof(float) * Mp));
+        TDS_CUDA(cached_malloc(&dmax, sizeof(float) * Mp));
         TDS_CUDA(cudaMemset(dmax, 0, sizeof(float) * Mp));
         TDS_CUDA(cudaMemset(x->fmx, 0, sizeof(float) * Mp));
         long rpb = 512;
@@ -1257,7 +1257,7 @@ int mixed_prepare(tdscha_ctx *c) {
         k_scales<<<ceil_div(Mp, 128), 128>>>(dmax, c->fY, M, Mp, x->sd, x->su, x->fmx);
         TDS_CHECK_LAUNCH();
         TDS_CUDA(cudaDeviceSynchronize());
-        cudaFree(dmax);
+        cached_free(dmax);
         int nb = (int)std::min<long>((rowN + 255) / 256, 152L * 32);
         k_prep_rows<<<nb, 256>>>(c->D, c->F, c->fpsi, x->sd, R, M, Mp, mx.d_hi, mx.d_lo, x->d32,
                                  mx.g32);
@@ -1294,12 +1294,12 @@ int mixed_release(tdscha_ctx *c) {
     void *bufs[] = {mx.d_hi, mx.d_lo, mx.g32, mx.ut_hi, mx.ut_lo, mx.ut32, mx.ft32, mx.wt_hi,
                     mx.wt_lo, mx.y1_hi, mx.y1_lo, mx.qp, mx.gpart};
     for (void *p : bufs)
-        if (p) cudaFree(p);
+        cached_free(p);
     if (MixedExtra *x = extra(c)) {
         void *xb[] = {x->sd, x->fmx, x->su, x->sw, x->tcol, x->vs, x->vt, x->absmax, x->d32,
                       x->abcc, x->fpart};
         for (void *p : xb)
-            if (p) cudaFree(p);
+            cached_free(p);
         delete x;
     }
     if (mx.err_flag) cudaFreeHost(mx.err_flag);
