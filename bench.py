@@ -369,7 +369,7 @@ def run_ours(args):
                 # DRAM bytes per launch from the ncu captures of the same kernels
                 # at N=20 000 (profiles/k_stageA_tc_m573_n20k.md for stage A,
                 # profiles/k_stageB_tc_m573_n20k.md for stage B), scaled by image rows
-                per_row = {0: 144.9e6 / 20000, 3: 96.0e6 / 20000}[kid]
+                per_row = {0: 147.9e6 / 20000, 3: 96.0e6 / 20000}[kid]
                 if M == 573:
                     roof["traffic"] = per_row * R
                     roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"
