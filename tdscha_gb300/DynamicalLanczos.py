@@ -244,8 +244,16 @@ class Lanczos(object):
         self.initialized = True
         M = self.n_modes
         if no_sym or self.unwrapped:
-            self.set_symmetries([np.ones((1, 1, 1), dtype=np.double)] * M,
-                                [np.array([i], dtype=np.intc) for i in range(M)])
+            # one-mode blocks with the identity as their only image: the tables
+            # set_symmetries would build, without a Python step per mode
+            ident = np.ones((1, 1, 1), dtype=np.double)
+            self.symmetries = [ident] * M
+            self.degenerate_space = list(np.arange(M, dtype=np.intc).reshape(M, 1))
+            self.N_degeneracy = np.ones(M, dtype=np.intc)
+            self.sym_block_id = np.arange(M, dtype=np.intc)
+            self.n_syms = 1
+            self.initialized = True
+            self._invalidate()
             return
         if symmetries is None:
             import spglib

@@ -144,6 +144,16 @@ def i32(a):
 
 def flatten_symmetries(symmetries, degenerate_space):
     """Per-block lists (as the reference passes them) -> flat C-ABI tables."""
+    s0 = symmetries[0] if len(symmetries) else None
+    if (isinstance(s0, np.ndarray) and s0.ndim == 3 and s0.shape[1:] == (1, 1)
+            and len(symmetries) == len(degenerate_space)
+            and all(s is s0 for s in symmetries) and all(len(b) == 1 for b in degenerate_space)):
+        # one-mode blocks sharing one image table (the unsymmetrised layout):
+        # the same tables without a Python step per block
+        nb = len(degenerate_space)
+        deg = i32(np.concatenate(degenerate_space).astype(np.intc, copy=False).ravel())
+        sym = f64(np.tile(np.asarray(s0, dtype=np.float64).ravel(), nb))
+        return np.ones(nb, dtype=np.intc), deg, sym, int(s0.shape[0])
     n_deg = np.array([len(b) for b in degenerate_space], dtype=np.intc)
     deg = i32(np.concatenate([np.asarray(b, dtype=np.intc).ravel() for b in degenerate_space]))
     sym = f64(np.concatenate([np.asarray(s, dtype=np.float64).ravel() for s in symmetries]))

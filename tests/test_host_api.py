@@ -113,3 +113,24 @@ def test_save_load_status_roundtrip(tmp_path):
               "krilov_basis", "arnoldi_matrix", "reverse", "shift", "perturbation_modulus",
               "use_wigner", "ignore_small_w", "sym_julia", "deg_julia", "n_syms"):
         assert k in keys
+
+
+def test_unsymmetrised_tables_match_general_path():
+    """init(use_symmetries=False) and flatten_symmetries take a vectorised path
+    for one-mode identity blocks; it must give the general path's tables."""
+    from tdscha_gb300 import _native as nat
+    M = 37
+    e = make_ensemble(M, 50, seed=3)
+    lz = Lanczos.from_arrays(e["X"], e["Y"], e["w"], e["rho"], e["T"], use_wigner=False)
+    lz.init(use_symmetries=False)
+    ref = Lanczos.from_arrays(e["X"], e["Y"], e["w"], e["rho"], e["T"], use_wigner=False)
+    ref.set_symmetries([np.ones((1, 1, 1))] * M, [np.array([i], np.intc) for i in range(M)])
+    np.testing.assert_array_equal(lz.N_degeneracy, ref.N_degeneracy)
+    np.testing.assert_array_equal(lz.sym_block_id, ref.sym_block_id)
+    assert lz.n_syms == ref.n_syms == 1
+    fast = nat.flatten_symmetries(lz.symmetries, lz.degenerate_space)
+    # general path: distinct (equal) block arrays, so the shared-table shortcut is not taken
+    slow = nat.flatten_symmetries([np.ones((1, 1, 1)) for _ in range(M)], ref.degenerate_space)
+    for a, b in zip(fast, slow):
+        np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
+        assert np.asarray(a).dtype == np.asarray(b).dtype
