@@ -762,7 +762,8 @@ __global__ void k_colmax(const double *__restrict__ D, const double *__restrict_
 // U^T), fmax (column maxima of F); zero columns get 1, padding gets 1 / 0.
 __global__ void k_scales(const float *__restrict__ dmax, const double *__restrict__ fY, int M,
                          int Mp, float *__restrict__ sd, float *__restrict__ su,
-                         float *__restrict__ fmx) {
+                         float *__restrict__ fmx, double *__restrict__ rsd,
+                         double *__restrict__ rsu) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= Mp) return;
     if (m < M) {
@@ -776,24 +777,29 @@ __global__ void k_scales(const float *__restrict__ dmax, const double *__restric
         su[m] = 1.f;
         fmx[m] = 0.f;
     }
+    // float64 reciprocals for the operand preparation
+    rsd[m] = 1.0 / (double)sd[m];
+    rsu[m] = 1.0 / (double)su[m];
 }
 
 // Resident operands from the float64 image rows D, F (R x M):
 //   d_hi/d_lo  (R x Mp)  limbs of D[r][m] / sd_m   (stage A operand)
 //   d32, g32   (R x Mp)  D and f_psi * F in fp32    (stage A epilogue)
+// Rows r over blockIdx.y, modes m over the x dimension (no 64-bit division
+// per element); the mode scales come as float64 reciprocals (a division per
+// element cost most of this pass: float64 runs at 2 FMA per cycle per SM).
 __global__ void k_prep_rows(const double *__restrict__ D, const double *__restrict__ F,
-                            const double *__restrict__ fpsi, const float *__restrict__ sd, long R,
+                            const double *__restrict__ fpsi, const double *__restrict__ rsd, long R,
                             int M, int Mp, __half *__restrict__ d_hi, __half *__restrict__ d_lo,
                             float *__restrict__ d32, float *__restrict__ g32) {
-    long n = R * Mp;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        long r = e / Mp;
-        int m = (int)(e % Mp);
+    for (long r = blockIdx.y; r < R; r += gridDim.y)
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < Mp; m += gridDim.x * blockDim.x) {
+        const long e = r * Mp + m;
         float x = 0.f, g = 0.f, xs = 0.f;
         if (m < M) {
             double dv = D[r * M + m];
             x = (float)dv;
-            xs = (float)(dv / (double)sd[m]);
+            xs = (float)(dv * rsd[m]);
             g = (float)(fpsi[m] * F[r * M + m]);
         }
         __half h, l;
@@ -809,7 +815,7 @@ __global__ void k_prep_rows(const double *__restrict__ D, const double *__restri
 //   ut_hi/ut_lo  limbs of U[r][a] / su_a   (stage B A operand)
 //   ut32, ft32   U and F in fp32            (W build, force average)
 __global__ void k_prep_cols(const double *__restrict__ D, const double *__restrict__ F,
-                            const double *__restrict__ fY, const float *__restrict__ su, long R,
+                            const double *__restrict__ fY, const double *__restrict__ rsu, long R,
                             int M, long Rp, __half *__restrict__ ut_hi, __half *__restrict__ ut_lo,
                             float *__restrict__ ut32, float *__restrict__ ft32) {
     __shared__ double tu[32][33];
@@ -834,9 +840,8 @@ __global__ void k_prep_cols(const double *__restrict__ D, const double *__restri
         long r = r0 + threadIdx.x;
         if (r < Rp) {
             double u = tu[threadIdx.x][k];
-            float s = (m < M) ? su[m] : 1.f;
             __half h, l;
-            split_f16((float)(u / (double)s), h, l);
+            split_f16((float)(u * rsu[m]), h, l);
             long o = (long)m * Rp + r;
             ut_hi[o] = h;
             ut_lo[o] = l;
@@ -1247,25 +1252,30 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * Mp));
     {
         float *dmax = nullptr;
+        double *rsc = nullptr;   // 1 / sd and 1 / su in float64 (Mp each)
         TDS_CUDA(cached_malloc(&dmax, sizeof(float) * Mp));
+        TDS_CUDA(cached_malloc(&rsc, sizeof(double) * 2 * Mp));
         TDS_CUDA(cudaMemset(dmax, 0, sizeof(float) * Mp));
         TDS_CUDA(cudaMemset(x->fmx, 0, sizeof(float) * Mp));
         long rpb = 512;
         dim3 g(ceil_div(M, 128), ceil_div(R, rpb));
         k_colmax<<<g, 128>>>(c->D, c->F, R, M, rpb, dmax, x->fmx);
         TDS_CHECK_LAUNCH();
-        k_scales<<<ceil_div(Mp, 128), 128>>>(dmax, c->fY, M, Mp, x->sd, x->su, x->fmx);
+        k_scales<<<ceil_div(Mp, 128), 128>>>(dmax, c->fY, M, Mp, x->sd, x->su, x->fmx, rsc,
+                                             rsc + Mp);
         TDS_CHECK_LAUNCH();
         TDS_CUDA(cudaDeviceSynchronize());
         cached_free(dmax);
-        int nb = (int)std::min<long>((rowN + 255) / 256, 152L * 32);
-        k_prep_rows<<<nb, 256>>>(c->D, c->F, c->fpsi, x->sd, R, M, Mp, mx.d_hi, mx.d_lo, x->d32,
+        dim3 gr(ceil_div(Mp, 128), (unsigned)std::min<long>(R, 4096));
+        k_prep_rows<<<gr, 128>>>(c->D, c->F, c->fpsi, rsc, R, M, Mp, mx.d_hi, mx.d_lo, x->d32,
                                  mx.g32);
         TDS_CHECK_LAUNCH();
         dim3 gc(ceil_div(Rp, 32), Mp / 32);
-        k_prep_cols<<<gc, dim3(32, 8)>>>(c->D, c->F, c->fY, x->su, R, M, Rp, mx.ut_hi, mx.ut_lo,
-                                         mx.ut32, mx.ft32);
+        k_prep_cols<<<gc, dim3(32, 8)>>>(c->D, c->F, c->fY, rsc + Mp, R, M, Rp, mx.ut_hi,
+                                         mx.ut_lo, mx.ut32, mx.ft32);
         TDS_CHECK_LAUNCH();
+        TDS_CUDA(cudaDeviceSynchronize());
+        cached_free(rsc);
     }
     TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
     TDS_TRY(make_map(&x->tmA.a_lo, mx.d_lo, Mp, R, kBM));
