@@ -189,7 +189,7 @@ inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 // shapes over and over (one per ensemble, perturbation or q-point), and
 // cudaMalloc / cudaFree of a context's buffers cost about 4 ms of a 22 ms
 // 20-step run at M=573, N=50 000.  At most 16 GiB stay cached (larger
-// surpluses go back to the driver), and an allocation that fails empties the
+// surpluses are released with cudaFree), and an allocation that fails empties the
 // cache and retries once.  cached_free of a pointer that did not come from
 // cached_malloc calls cudaFree.  A block is cached only after its last use:
 // callers free after synchronising.
