@@ -36,7 +36,7 @@ extern "C" {
 
 /* precision of the perturbation averages */
 #define TDSCHA_PREC_FP64 0       /* float64 on the CUDA cores                   */
-#define TDSCHA_PREC_MIXED 1      /* split-bf16 x3 tensor-core GEMMs, fp32 accumulate */
+#define TDSCHA_PREC_MIXED 1      /* two-limb fp16 operands, three tensor-core products per K step, fp32 accumulate */
 
 typedef struct tdscha_ctx tdscha_ctx;
 typedef struct tdscha_qctx tdscha_qctx;
@@ -238,6 +238,19 @@ int tdscha_static_hessian_collect(tdscha_ctx *ctx, const double *Y, double *vec,
 /* Synchronise stream and report asynchronous failures (CUDA errors, an expired
  * bounded wait of the tensor-core path). */
 int tdscha_ctx_sync(tdscha_ctx *ctx, void *stream);
+
+/*
+ * Device memory of destroyed contexts (no counterpart in the reference).  The
+ * device buffers of a context come from a process-wide cache of freed blocks,
+ * reused by exact size by later contexts (creating and destroying contexts
+ * of one shape costs no cudaMalloc / cudaFree after the first).  At most
+ * TDSCHA_BLOCK_CACHE_GIB GiB (environment, read once; default 16, 0 turns the
+ * cache off) stay cached, and an allocation that fails empties the cache and
+ * retries.  tdscha_release_cached_memory frees every cached block now (blocks
+ * of live contexts are untouched) and writes the bytes released to *bytes
+ * (may be null).  It synchronises the device.
+ */
+int tdscha_release_cached_memory(unsigned long long *bytes);
 
 /*
  * q-space (Bloch basis) operator, float64 complex, Wigner only

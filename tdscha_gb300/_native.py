@@ -30,6 +30,7 @@ EXPORTS = [
     "tdscha_lanczos_run_batch", "tdscha_mlp_create", "tdscha_mlp_destroy",
     "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
     "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
+    "tdscha_release_cached_memory",
 ]
 
 
@@ -89,6 +90,7 @@ def load():
                                         _i, _vp]
     lib.tdscha_static_L.argtypes = [_vp, _c_int, _vp, _vp, _c_int, _c_double, _c_int, _vp]
     lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
+    lib.tdscha_release_cached_memory.argtypes = [_vp]
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
                                                _c_int, _d, _i, _i]

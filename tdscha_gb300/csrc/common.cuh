@@ -188,9 +188,10 @@ inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 // reused by exact size: applications create and destroy contexts of the same
 // shapes over and over (one per ensemble, perturbation or q-point), and
 // cudaMalloc / cudaFree of a context's buffers cost about 4 ms of a 22 ms
-// 20-step run at M=573, N=50 000.  At most 16 GiB stay cached (larger
-// surpluses are released with cudaFree), and an allocation that fails empties the
-// cache and retries once.  cached_free of a pointer that did not come from
+// 20-step run at M=573, N=50 000.  At most TDSCHA_BLOCK_CACHE_GIB GiB (default
+// 16, 0 turns caching off) stay cached, larger surpluses are released with
+// cudaFree, an allocation that fails empties the cache and retries once, and
+// tdscha_release_cached_memory empties it on request.  cached_free of a pointer that did not come from
 // cached_malloc calls cudaFree.  A block is cached only after its last use:
 // callers free after synchronising.
 cudaError_t cached_malloc(void **p, size_t bytes);

@@ -98,7 +98,16 @@ BlockCache &block_cache() {
     static BlockCache *bc = new BlockCache();   // never destroyed: no cudaFree at exit
     return *bc;
 }
-constexpr size_t kCacheCap = size_t(16) << 30;
+// cap on the cached bytes: TDSCHA_BLOCK_CACHE_GIB (GiB; 0 turns caching off),
+// default 16
+size_t cache_cap() {
+    static const size_t cap = [] {
+        const char *e = getenv("TDSCHA_BLOCK_CACHE_GIB");
+        double gib = e ? atof(e) : 16.0;
+        return gib > 0 ? (size_t)(gib * (double)(size_t(1) << 30)) : size_t(0);
+    }();
+    return cap;
+}
 }  // namespace
 
 cudaError_t tdscha::cached_malloc(void **p, size_t bytes) {
@@ -139,12 +148,33 @@ void tdscha::cached_free(void *p) {
     }
     auto key = it->second;
     bc.live.erase(it);
-    if (bc.idle_bytes + key.second > kCacheCap) {
+    if (bc.idle_bytes + key.second > cache_cap()) {
         cudaFree(p);
         return;
     }
     bc.idle.insert({key, p});
     bc.idle_bytes += key.second;
+}
+
+extern "C" int tdscha_release_cached_memory(unsigned long long *bytes) {
+    set_error("");
+    cudaDeviceSynchronize();
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    unsigned long long freed = 0;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (auto &kv : bc.idle) {
+        // each block is freed on the device it was allocated on
+        if (kv.first.first != cur) cudaSetDevice(kv.first.first);
+        cudaFree(kv.second);
+        if (kv.first.first != cur) cudaSetDevice(cur);
+        freed += kv.first.second;
+    }
+    bc.idle.clear();
+    bc.idle_bytes = 0;
+    if (bytes) *bytes = freed;
+    return TDSCHA_OK;
 }
 
 static void ctx_free(tdscha_ctx *c) {

@@ -132,3 +132,33 @@ def test_mixed_repeat_bitwise_identical(gpu_lib):
             bad.append((i, rel(f, f0), rel(d2v, d0)))
     ctx.close()
     assert not bad, "calls with different results (index, rel f, rel d2v): %s" % bad[:5]
+
+
+def test_release_cached_memory(gpu_lib):
+    """Blocks of destroyed contexts stay cached for the next context of the same
+    shape until tdscha_release_cached_memory hands them back."""
+    import ctypes
+    import torch
+    M, N = 96, 4000
+    ens = make_ensemble(M, N, seed=21)
+    syms, spaces, bid = oracle.identity_symmetries(M)
+    R1, Y1 = random_R1(M, 1), random_sym(M, 2, scale=1e-3)
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    f0, d0 = _mixed_call(ctx, R1, Y1)
+    ctx.close()
+    # a second context of the same shape reuses the cached blocks and computes the same bits
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                      with_mixed=True)
+    f1, d1 = _mixed_call(ctx, R1, Y1)
+    ctx.close()
+    np.testing.assert_array_equal(f0, f1)
+    np.testing.assert_array_equal(d0, d1)
+    free_before = torch.cuda.mem_get_info()[0]
+    got = ctypes.c_ulonglong(0)
+    nat.check(gpu_lib.tdscha_release_cached_memory(ctypes.byref(got)))
+    # at least the ensemble images D and F (2 x N x M doubles) were cached
+    assert got.value >= 2 * N * M * 8
+    assert torch.cuda.mem_get_info()[0] >= free_before + got.value // 2
+    nat.check(gpu_lib.tdscha_release_cached_memory(ctypes.byref(got)))
+    assert got.value == 0
