@@ -14,9 +14,9 @@ C ABI of libtdscha_gb300.so (no CPU path).  The Krylov basis lives in device
 memory (torch tensors) and is copied to the host only when `basis_Q` /
 `basis_P` are read or a status is saved.
 
-Extra knobs: `precision` ("fp64" or "mixed": split-bf16 tensor-core
-perturbation averages with fp32 accumulation; the Lanczos recurrence stays
-in float64) and `Lanczos.from_arrays` for ensembles already projected on the
+Extra knobs: `precision` ("fp64" or "mixed": tensor-core perturbation
+averages on two-limb fp16 operands with fp32 accumulation; the Lanczos
+recurrence stays in float64) and `Lanczos.from_arrays` for ensembles already projected on the
 mode basis.
 """
 import os
