@@ -383,13 +383,13 @@ def run_ours(args):
                     "avg_launch_ms": tot_ms / cnt}
     kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1]}
                for k, v in kern.items()}
-    # kernels launched per step.  One application: psi unpack + assemble and
-    # the averages (mixed: Y1 limbs, stage A, row scalars, W build, stage B,
-    # finalisation; float64: stage A, row scalars, force average, stage B,
-    # finalisation).  Recurrence: dot + a, residuals, b/c, normalisation, and
+    # kernels launched per step.  One application: the averages and the
+    # assemble (mixed: Y1 limbs read straight from psi, stage A, row scalars,
+    # W build, stage B, finalisation; float64: psi unpack, stage A, row
+    # scalars, force average, stage B, finalisation).  Recurrence: dot + a, residuals, b/c, normalisation, and
     # with re-biorthogonalisation the dots, coefficients, apply and weight
     # (one apply pass per 2048 stored vectors, here always one).
-    per_app = 2 + (6 if prec_name == "mixed" else 5)
+    per_app = 1 + 6
     per_step_rec = 5 + (4 if not args.no_reorth else 0)
     gpu_launches = K * (2 * per_app + per_step_rec)
 

@@ -169,6 +169,10 @@ int alloc_fp64_scratch(tdscha_ctx *c);
 int mixed_prepare(tdscha_ctx *c);
 int mixed_release(tdscha_ctx *c);
 int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st);
+// the same with Y1 and R1 unpacked from psi inside the operand preparation
+// (plain layout, or the transposed one with its per-pair factors cty / ctra)
+int perturb_mixed_psi(tdscha_ctx *c, int apply_d4, const double *psi, const double *cty,
+                      const double *ctra, cudaStream_t st);
 int mixed_check_error(tdscha_ctx *c);
 // lanczos.cu
 int build_pair_coeffs(tdscha_ctx *c);

@@ -247,11 +247,19 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
     long H = c->H;
     int with_anh = !c->ignore_v3;
     if (with_anh) {
-        dim3 gu(ceil_div(M, 256), std::min(M, 65535));
-        TDS_CUDA(launch_pdl(k_unpack, gu, 256, 0, st, psi_in, c->pc, M, H, c->use_wigner, transpose,
-                            c->ignore_v3, c->R1, c->Y1));
-        // Y1 from the unpack is symmetric by construction: no symmetrise pass
-        TDS_TRY(run_perturb_sym(c, c->ignore_v4 ? 0 : 1, precision, st));
+        if (precision == TDSCHA_PREC_MIXED && c->with_mixed && !c->use_wigner) {
+            // the tensor-core path reads Y1 and R1 straight from psi while it
+            // forms the Y1 limbs (no Y1 round trip, one launch fewer)
+            TDS_TRY(perturb_mixed_psi(c, c->ignore_v4 ? 0 : 1, psi_in,
+                                      transpose ? c->pc + PC_TY * H : nullptr,
+                                      transpose ? c->pc + PC_TRA * H : nullptr, st));
+        } else {
+            dim3 gu(ceil_div(M, 256), std::min(M, 65535));
+            TDS_CUDA(launch_pdl(k_unpack, gu, 256, 0, st, psi_in, c->pc, M, H, c->use_wigner,
+                                transpose, c->ignore_v3, c->R1, c->Y1));
+            // Y1 from the unpack is symmetric by construction: no symmetrise pass
+            TDS_TRY(run_perturb_sym(c, c->ignore_v4 ? 0 : 1, precision, st));
+        }
         // gamma_only: translation projection of f and d2v (DynamicalLanczos.py:3173-3191)
         if (c->tr_ntrans > 0) TDS_TRY(apply_translation_projection(c, st));
     }

@@ -854,8 +854,35 @@ __global__ void k_prep_cols(const double *__restrict__ D, const double *__restri
 // Per call: Y1 row n scaled by sd (mode axis) and by 1/t_n, t_n its max; one
 // block per row.  Also the epilogue vectors f_Y*R1, R1/f_psi, and the reset
 // of the alpha / beta maxima.
-__global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restrict__ R1,
-                          const double *__restrict__ fY, const double *__restrict__ fpsi,
+// Where k_prep_y1 reads Y1 and R1: the context's buffers (written by the
+// caller or the psi unpack), or psi itself, unpacked on the fly with the
+// unpack's formulas for the plain and transposed layouts
+// (Modules/DynamicalLanczos.py:2887-2948, :3009-3053): row n of Y1 from the
+// upper-triangle sectors of psi, R1 = psi's R sector.
+struct Y1FromBuffers {
+    const double *Y1, *R1;
+    int M;
+    __device__ double y(int n, int m) const { return Y1[(long)n * M + m]; }
+    __device__ double r(int n) const { return R1[n]; }
+};
+struct Y1FromPsi {
+    const double *psi;
+    const double *cty, *ctra;   // transposed layout's per-pair factors; null: plain
+    int M;
+    long H;
+    int ignore_v3;
+    __device__ double y(int n, int m) const {
+        const int i = min(n, m), j = max(n, m);
+        const long k = (long)i * M - (long)i * (i - 1) / 2 + (j - i);
+        const double yv = psi[M + k];
+        if (!cty) return yv;
+        return yv * cty[k] + psi[M + H + k] * ctra[k];
+    }
+    __device__ double r(int n) const { return ignore_v3 ? 0.0 : psi[n]; }
+};
+
+template <class Src>
+__global__ void k_prep_y1(const Src src, const double *__restrict__ fY, const double *__restrict__ fpsi,
                           const float *__restrict__ sd, int M, int Mp, __half *__restrict__ y_hi,
                           __half *__restrict__ y_lo, float *__restrict__ tcol,
                           float *__restrict__ vs, float *__restrict__ vt,
@@ -865,7 +892,7 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
     int n = blockIdx.x;
     float mx = 0.f;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x)
-        if (n < M && m < M) mx = fmaxf(mx, fabsf((float)Y1[(long)n * M + m] * sd[m]));
+        if (n < M && m < M) mx = fmaxf(mx, fabsf((float)src.y(n, m) * sd[m]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
@@ -880,7 +907,7 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
     float t = red[0] > 0.f ? red[0] : 1.f;
     float inv = 1.f / t;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
-        float x = (n < M && m < M) ? (float)Y1[(long)n * M + m] * sd[m] * inv : 0.f;
+        float x = (n < M && m < M) ? (float)src.y(n, m) * sd[m] * inv : 0.f;
         __half h, l;
         split_f16(x, h, l);
         y_hi[(long)n * Mp + m] = h;
@@ -888,8 +915,9 @@ __global__ void k_prep_y1(const double *__restrict__ Y1, const double *__restric
     }
     if (threadIdx.x == 0) {
         tcol[n] = n < M ? t : 0.f;
-        vs[n] = n < M ? (float)(fY[n] * R1[n]) : 0.f;
-        vt[n] = n < M ? (float)(R1[n] / fpsi[n]) : 0.f;
+        const double r1 = n < M ? src.r(n) : 0.0;
+        vs[n] = n < M ? (float)(fY[n] * r1) : 0.f;
+        vt[n] = n < M ? (float)(r1 / fpsi[n]) : 0.f;
         if (n == 0) { absmax[0] = 0.f; absmax[1] = 0.f; }
     }
 }
@@ -1327,7 +1355,21 @@ int mixed_check_error(tdscha_ctx *c) {
     return TDSCHA_OK;
 }
 
+static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
+                             cudaStream_t st);
+
 int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
+    return perturb_mixed_src(c, apply_d4, nullptr, st);
+}
+
+int perturb_mixed_psi(tdscha_ctx *c, int apply_d4, const double *psi, const double *cty,
+                      const double *ctra, cudaStream_t st) {
+    Y1FromPsi src{psi, cty, ctra, c->M, c->H, c->ignore_v3};
+    return perturb_mixed_src(c, apply_d4, &src, st);
+}
+
+static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
+                             cudaStream_t st) {
     MixedStore &mx = c->mx;
     MixedExtra *x = extra(c);
     if (!x) { set_error("mixed store not prepared"); return TDSCHA_ERR_STATE; }
@@ -1337,8 +1379,13 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
     {
         ProfScope ps(c, 5, st);
-        TDS_CUDA(launch_pdl(k_prep_y1, Mp, 256, 0, st, c->Y1, c->R1, c->fY, c->fpsi, x->sd, M, Mp,
-                            mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
+        if (psrc)
+            TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, *psrc, c->fY, c->fpsi, x->sd,
+                                M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
+        else
+            TDS_CUDA(launch_pdl(k_prep_y1<Y1FromBuffers>, Mp, 256, 0, st,
+                                Y1FromBuffers{c->Y1, c->R1, M}, c->fY, c->fpsi, x->sd, M, Mp,
+                                mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
     }
     StageAArgs ga{};
     ga.R = R;
