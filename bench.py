@@ -58,6 +58,18 @@ def parse():
     return ap.parse_args()
 
 
+def emit(line):
+    """Print the JSON line last: C libraries loaded in this process (the
+    reference's module prints its configuration split) buffer their stdout
+    until exit, so flush the C stdio buffers first."""
+    sys.stdout.flush()
+    try:
+        ctypes.CDLL(None).fflush(None)
+    except (OSError, AttributeError):
+        pass
+    print(json.dumps(line), flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -239,7 +251,7 @@ def run_reference(args):
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    emit(line)
 
 
 # ------------------------------------------------------------------ GPU side
@@ -427,7 +439,7 @@ def run_ours(args):
                 "fp64_gpu": fp64, "accuracy_vs_fp64": check,
                 "clocks": clocks, "gpu_launches": gpu_launches, "other_paths": rows,
                 "flops_per_application": flops_app}
-        print(json.dumps(line), flush=True)
+        emit(line)
     if ws > 1:
         dist.destroy_process_group()
 
