@@ -70,6 +70,20 @@ def emit(line):
     print(json.dumps(line), flush=True)
 
 
+def job_throughput(ms_local, K, ws, device=None):
+    """Whole-job steps/s of ws independent replicas that each ran K steps: the
+    slowest rank's time (max over the process group) for ws x K steps.
+    Returns (steps/s, that time in ms); ws = 1 needs no process group."""
+    ms = float(ms_local)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ws * K / (ms / 1e3), ms
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -324,12 +338,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks = clk.stop(t_start, time.time())
     ms = e0.elapsed_time(e1)
+    value, ms = job_throughput(ms, K, ws, dev)
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = ws * K / (ms / 1e3)
 
     # per-kernel device time: the same K steps again with CUDA events around
     # each kernel of the perturbation averages (kept out of the headline pass)
