@@ -1,11 +1,26 @@
 """Drop-in for tdscha.QSpaceHessian (Modules/QSpaceHessian.py) on the GPU.
 
-The free-energy Hessian at each q-point from the static q-space operator:
-L_static = [w^2 on R | 1/Lambda on the W blocks] + the anharmonic coupling,
-solved for every non-acoustic band with GMRES (scipy) as the reference does.
-The anharmonic coupling -- the ensemble average that dominates the cost --
-runs on the GPU through the q-space context (tdscha_qperturb_averages): R1 from
-the R sector, Y1 = -2 Upsilon_1 Upsilon_2 W per pair block (:640-692).
+The free-energy Hessian at a q-point is H_q = G_q^-1, with G_q[:, i] the R part
+of the solution of L_static(q) x = e_i.  The static q-space operator acts on a
+vector [R (n_bands) | W blocks of the unique q-pairs]:
+
+    R -> w_q^2 R - f,     W_p -> W_p / Lambda_p + d2v_p,
+
+where (f, d2v) are the q-space perturbation averages with R1 = R and
+Y1_p = -2 (Y_w1 Y_w2^T) * W_p (Modules/QSpaceHessian.py:605-692).  The
+averages, which carry all the cost, run on the GPU through the q-space context
+(tdscha_qperturb_averages); everything here is host logic around them.
+
+Design.  `_StaticQOperator` is built once per q-point and works on flat
+vectors: the harmonic part is one elementwise product with a precomputed
+diagonal, the W blocks are gathered from / scattered to the flat layout with
+precomputed index arrays (a self-paired block is stored as its upper triangle
+and expanded with its Hermitian conjugate).  The solves run in the metric-
+symmetric variables x~ = sqrt(m) x (m the static inner-product weights), with
+the inverse harmonic diagonal as preconditioner and as starting point; each
+right-hand side goes through a chain of solvers (GMRES, then BiCGSTAB, then
+-- only when allowed -- a least-squares solve of the assembled Hermitian
+matrix), the first one that converges wins.
 """
 import os
 import time
@@ -16,318 +31,343 @@ import scipy.sparse.linalg
 from .QSpaceLanczos import QSpaceLanczos, RY_TO_K
 
 __EPSILON__ = 1e-12
+_DEGENERACY_TOL = 1e-8        # Ry, frequencies closer than this form one block
 
 
+# ----------------------------------------------------------------- physics
+def _occupations(w, valid, T):
+    """Bose occupation of the valid modes (0 at T = 0 and on masked modes)."""
+    n = np.zeros_like(w, dtype=np.float64)
+    if T > __EPSILON__:
+        n[valid] = 1.0 / np.expm1(w[valid] * (RY_TO_K / T))
+    return n
+
+
+def static_propagator(w1, valid1, w2, valid2, T):
+    """Static two-phonon propagator Lambda[nu1, nu2] of a q-pair.
+
+    Lambda = [(1 + n1 + n2) / (w1 + w2) - Dn] / (4 w1 w2), where Dn is the
+    divided difference (n1 - n2) / (w1 - w2) of the Bose function and, for
+    |w1 - w2| < 1e-8 Ry, its derivative dn/dw = -beta n (n + 1).  Zero where
+    either mode is masked (Modules/QSpaceHessian.py:481-544 states the same
+    propagator)."""
+    n1 = _occupations(w1, valid1, T)[:, None]
+    n2 = _occupations(w2, valid2, T)[None, :]
+    a, b = np.asarray(w1, float)[:, None], np.asarray(w2, float)[None, :]
+    ok = valid1[:, None] & valid2[None, :]
+    gap = a - b
+    close = np.abs(gap) < _DEGENERACY_TOL
+    dn = np.zeros(ok.shape)
+    if T > __EPSILON__:
+        beta = RY_TO_K / T
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dn = np.where(close, -beta * n1 * (n1 + 1.0), (n1 - n2) / np.where(close, 1.0, gap))
+        dn = np.where(close & ~ok, 0.0, dn)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lam = ((1.0 + n1 + n2) / (a + b) - dn) / (4.0 * a * b)
+    return np.where(ok, lam, 0.0)
+
+
+def _f_upsilon(w, valid, T):
+    """2 w / (2 n + 1) on valid modes, 0 elsewhere."""
+    out = np.zeros_like(w, dtype=np.float64)
+    n = _occupations(w, valid, T)
+    out[valid] = 2.0 * w[valid] / (1.0 + 2.0 * n[valid])
+    return out
+
+
+def degenerate_groups(w, valid, tol=_DEGENERACY_TOL):
+    """Valid bands grouped into runs of equal frequency (consecutive sorted
+    frequencies closer than tol), each group sorted, groups ordered by their
+    first band."""
+    idx = np.flatnonzero(valid)
+    if idx.size == 0:
+        return []
+    order = idx[np.argsort(w[idx], kind="stable")]
+    cuts = np.flatnonzero(np.diff(w[order]) >= tol) + 1
+    groups = [sorted(int(i) for i in g) for g in np.split(order, cuts)]
+    return sorted(groups, key=lambda g: g[0])
+
+
+# ---------------------------------------------------------------- operator
+class _StaticQOperator:
+    """The static operator of one perturbation q-point on flat vectors."""
+
+    def __init__(self, qlanc, ignore_v3, ignore_v4):
+        q = qlanc
+        nb = q.n_bands
+        self.q, self.nb = q, nb
+        self.ignore_v3, self.ignore_v4 = ignore_v3, ignore_v4
+        self.size = q.get_static_psi_size()
+        self.n_pairs = len(q.unique_pairs)
+        T = q.T
+        vq = q.valid_modes_q
+        wq = q.w_q
+        diag = np.zeros(self.size)          # harmonic static operator
+        weight = np.zeros(self.size)        # inner-product weights
+        iq = q.iq_pert
+        diag[:nb] = wq[:, iq] ** 2
+        weight[:nb] = vq[:, iq]
+        self._precond = np.zeros(self.size)
+        self._precond[:nb] = np.where(vq[:, iq], 1.0 / np.where(vq[:, iq], wq[:, iq], 1.0) ** 2,
+                                      0.0)
+        iu_r, iu_c = np.triu_indices(nb)
+        self._gather = []                   # per pair: (flat positions, rows, cols, self-paired)
+        self._yw = np.zeros((self.n_pairs, nb, nb))
+        for p, (q1, q2) in enumerate(q.unique_pairs):
+            off = q.get_block_offset(p, "a")
+            v1, v2 = vq[:, q1], vq[:, q2]
+            lam = static_propagator(wq[:, q1], v1, wq[:, q2], v2, T)
+            both = v1[:, None] & v2[None, :]
+            if q1 < q2:
+                rows, cols = np.divmod(np.arange(nb * nb), nb)
+                w_el = np.where(both, 2.0, 0.0)[rows, cols]
+            else:
+                rows, cols = iu_r, iu_c
+                w_el = np.where(both[rows, cols], np.where(rows == cols, 1.0, 2.0), 0.0)
+            pos = off + np.arange(rows.size)
+            el = lam[rows, cols]
+            big = np.abs(el) > 1e-30
+            diag[pos] = np.where(big, 1.0 / np.where(big, el, 1.0), 0.0)
+            self._precond[pos] = el
+            weight[pos] = w_el
+            self._gather.append((pos, rows, cols, q1 == q2))
+            self._yw[p] = -2.0 * np.outer(_f_upsilon(wq[:, q1], v1, T), _f_upsilon(wq[:, q2], v2, T))
+        self.diag = diag
+        self.weight = weight
+        self.sqrt_w = np.sqrt(weight)
+        self.inv_sqrt_w = np.where(weight > 0, 1.0 / np.where(weight > 0, self.sqrt_w, 1.0), 0.0)
+        self.applications = 0
+
+    # flat <-> blocks
+    def blocks(self, x):
+        out = np.zeros((self.n_pairs, self.nb, self.nb), dtype=np.complex128)
+        for p, (pos, r, c, herm) in enumerate(self._gather):
+            out[p, r, c] = x[pos]
+            if herm:
+                off = r != c
+                out[p, c[off], r[off]] = np.conj(x[pos][off])
+        return out
+
+    def scatter(self, blocks, x):
+        for p, (pos, r, c, _) in enumerate(self._gather):
+            x[pos] = blocks[p][r, c]
+        return x
+
+    def anharmonic(self, x):
+        """[-f | d2v] of the GPU averages (Modules/QSpaceHessian.py:640-692)."""
+        out = np.zeros(self.size, dtype=np.complex128)
+        if self.ignore_v3 and self.ignore_v4:
+            return out
+        R1 = np.zeros(self.nb, dtype=np.complex128) if self.ignore_v3 else \
+            np.array(x[:self.nb], dtype=np.complex128)
+        Y1 = self._yw * self.blocks(x)
+        f, d2v = self.q.get_perturb_averages_q(R1, list(Y1), not self.ignore_v4)
+        out[:self.nb] = -np.asarray(f)
+        self.applications += 1
+        return self.scatter(np.asarray(d2v), out)
+
+    def apply(self, x):
+        return self.diag * x + self.anharmonic(x)
+
+    # metric-symmetric form
+    def apply_tilde(self, xt):
+        return self.apply(xt * self.inv_sqrt_w) * self.sqrt_w
+
+    def precondition_tilde(self, xt):
+        return self._precond * xt * (self.weight > 0)
+
+    def dense_tilde(self):
+        """The Hermitian part of the operator in x~ variables, column by column."""
+        A = np.empty((self.size, self.size), dtype=np.complex128)
+        e = np.zeros(self.size, dtype=np.complex128)
+        for j in range(self.size):
+            e[j] = 1.0
+            A[:, j] = self.apply_tilde(e)
+            e[j] = 0.0
+        return 0.5 * (A + A.conj().T)
+
+
+# ------------------------------------------------------------------ solvers
+def _scipy_solver(fn):
+    def run(A, b, x0, tol, maxiter, M, counter):
+        kw = dict(x0=x0, maxiter=maxiter, M=M)
+        if counter is not None:
+            kw.update(callback=counter, callback_type="legacy")
+        try:
+            return fn(A, b, rtol=tol, **kw)
+        except TypeError:                   # scipy releases before the rtol keyword
+            return fn(A, b, tol=tol, **kw)
+    return run
+
+
+_gmres = _scipy_solver(scipy.sparse.linalg.gmres)
+_bicgstab_raw = _scipy_solver(scipy.sparse.linalg.bicgstab)
+
+
+def _bicgstab(A, b, x0, tol, maxiter, M, counter):
+    return _bicgstab_raw(A, b, x0, tol, maxiter, M, None)
+
+
+def _solve_chain(op, rhs, x0, tol, max_iters, M, dense_allowed, dense_cache, label):
+    """Solve op x = rhs: GMRES (the operator may be indefinite), then BiCGSTAB
+    from GMRES's last iterate, then a least-squares solve of the assembled
+    matrix if dense_allowed.  Returns (x, iterations)."""
+    iters = [0]
+
+    def count(_):
+        iters[0] += 1
+
+    A = scipy.sparse.linalg.LinearOperator((op.size, op.size), matvec=op.apply_tilde,
+                                           dtype=np.complex128)
+    x, info = x0, 1
+    for solver in (_gmres, _bicgstab):
+        x, info = solver(A, rhs, x, tol, max_iters, M, count)
+        if info == 0:
+            return x, iters[0]
+    if not dense_allowed:
+        raise RuntimeError("Iterative solvers (GMRES, BiCGSTAB) did not converge for {} "
+                           "(info={}). Set dense_fallback=True to use a dense solve "
+                           "(warning: O(psi_size^2) memory).".format(label, info))
+    if "A" not in dense_cache:
+        dense_cache["A"] = op.dense_tilde()
+    return np.linalg.lstsq(dense_cache["A"], rhs, rcond=1e-10)[0], iters[0]
+
+
+def _fill_green(G, groups, solutions, nb):
+    """Columns of G_q from one solve per group (Schur's lemma: between two
+    copies of the same d-dimensional irrep G is a multiple of I_d, between
+    different irreps zero).  solutions[k] is the R part of the solve for the
+    first band of groups[k]; G[C_j, B_j] = x_B[C_0] for every pair of groups
+    B, C of equal size, j = 0..d-1.  Without degeneracies every group is a
+    single band and this is G[c, b] = x_b[c]."""
+    by_size = {}
+    for k, g in enumerate(groups):
+        by_size.setdefault(len(g), []).append(k)
+    for d, members in by_size.items():
+        for kb in members:
+            x = solutions[kb]
+            for kc in members:
+                C = groups[kc]
+                for j in range(d):
+                    G[C[j], groups[kb][j]] = x[C[0]]
+    return G
+
+
+# ------------------------------------------------------------------- driver
 class QSpaceHessian:
+    """Free-energy Hessian of every q-point from the static q-space operator
+    (Modules/QSpaceHessian.py:57).  `H_q_dict[iq]` holds the mode-basis
+    Hessian (n_bands x n_bands, complex) of each solved q-point."""
+
     def __init__(self, ensemble=None, verbose=True, ignore_v3=False, ignore_v4=False, **kwargs):
         qlanc = QSpaceLanczos(ensemble, **kwargs) if ensemble is not None else QSpaceLanczos()
-        self._setup(qlanc, verbose)
+        self._attach(qlanc, verbose)
         self.ensemble = ensemble
         self.ignore_v3 = ignore_v3
         self.ignore_v4 = ignore_v4
 
-    def _setup(self, qlanc, verbose):
+    def _attach(self, qlanc, verbose):
         object.__setattr__(self, "qlanc", qlanc)
         self.verbose = verbose
-        self.n_q = qlanc.n_q
-        self.n_bands = qlanc.n_bands
-        self.q_points = qlanc.q_points
-        self.w_q = qlanc.w_q
-        self.pols_q = qlanc.pols_q
+        for name in ("n_q", "n_bands", "q_points", "w_q", "pols_q"):
+            setattr(self, name, getattr(qlanc, name))
         self.H_q_dict = {}
         self.irr_qpoints = None
         self.q_star_map = None
-        self._cached_w_qp_sq = None
-        self._cached_inv_w_qp_sq = None
-        self._cached_inv_lambda = None
-        self._cached_lambda = None
-        self._cached_yw_outer = None
-        self._has_symmetry_data = False
+        self.last_operator = None
 
     def __setattr__(self, name, value):
-        """ignore_v3 / ignore_v4 propagate to the q-space engine (:107-114)."""
+        """The ignore flags are shared with the q-space engine."""
         super().__setattr__(name, value)
         if name in ("ignore_v3", "ignore_v4") and getattr(self, "qlanc", None) is not None:
             setattr(self.qlanc, name, value)
 
     @classmethod
     def from_qspace_lanczos(cls, qlanc, verbose=True, use_symmetries=True):
-        """Share the data of an initialised QSpaceLanczos (:1071-1129)."""
+        """A Hessian driver on the data of an initialised QSpaceLanczos."""
         hess = cls.__new__(cls)
-        hess._setup(qlanc, verbose)
+        hess._attach(qlanc, verbose)
         hess.ensemble = getattr(qlanc, "ensemble", None)
         hess.ignore_v3 = qlanc.ignore_v3
         hess.ignore_v4 = qlanc.ignore_v4
-        hess._all_qpoints()
+        hess._every_qpoint()
         return hess
 
-    def _all_qpoints(self):
+    def _every_qpoint(self):
+        """No irreducible-q reduction (it needs spglib and the crystal): every
+        q-point is its own star."""
         self.irr_qpoints = list(range(self.n_q))
         self.q_star_map = {iq: [(iq, np.eye(3), np.zeros(3), False)] for iq in range(self.n_q)}
 
     def init(self, use_symmetries=True):
-        """Initialise the engine.  The irreducible-q reduction of the reference
-        needs spglib and the crystal structure (:249-338); without them every
-        q-point is solved, as the reference does when spglib is missing."""
+        """Initialise the q-space engine; all q-points are solved."""
         self.qlanc.init(use_symmetries=use_symmetries)
-        self._all_qpoints()
+        self._every_qpoint()
 
-    # --------------------------------------------------------------- layout
-    def _get_static_psi_size(self):
-        return self.qlanc.get_static_psi_size()
+    def static_operator(self, iq):
+        """The static operator with the perturbation at q-point iq."""
+        self.qlanc.build_q_pair_map(iq)
+        return _StaticQOperator(self.qlanc, self.ignore_v3, self.ignore_v4)
 
-    def _get_W_block(self, psi, pair_idx):
-        return self.qlanc.get_block(pair_idx, sector="a", source=psi)
-
-    def _set_W_block(self, psi, pair_idx, matrix):
-        self.qlanc.set_block_in_psi(pair_idx, matrix, "a", psi)
-
-    def _static_mask(self):
-        """Inner-product weights of the static psi (:434-479): R sector 1 (0 on
-        masked modes), W blocks 2 (1 on self-paired diagonals, 0 if either mode
-        is masked)."""
-        psi_size = self._get_static_psi_size()
-        mask = np.ones(psi_size, dtype=np.float64)
-        nb = self.n_bands
-        q = self.qlanc
-        mask[:nb] = np.where(q.valid_modes_q[:, q.iq_pert], 1.0, 0.0)
-        iu = np.triu_indices(nb)
-        for p, (iq1, iq2) in enumerate(q.unique_pairs):
-            off = q.get_block_offset(p, "a")
-            v1, v2 = q.valid_modes_q[:, iq1], q.valid_modes_q[:, iq2]
-            invalid = ~v1[:, None] | ~v2[None, :]
-            full = np.where(invalid, 0.0, 2.0)
-            if iq1 < iq2:
-                mask[off:off + nb * nb] = full.ravel()
-            else:
-                np.fill_diagonal(full, np.where(v1 & v2, 1.0, 0.0))
-                mask[off:off + q.get_block_size(p)] = full[iu]
-        return mask
-
-    # ----------------------------------------------------- static quantities
-    def _bose(self, iq):
-        w = self.w_q[:, iq]
-        valid = self.qlanc.valid_modes_q[:, iq]
-        n = np.zeros_like(w)
-        if self.qlanc.T > __EPSILON__:
-            n[valid] = 1.0 / (np.exp(w[valid] * (RY_TO_K / self.qlanc.T)) - 1.0)
-        return n, valid
-
-    def _compute_lambda_q(self, iq1, iq2):
-        """Static two-phonon propagator of pair (iq1, iq2) (:481-544)."""
-        T = self.qlanc.T
-        w1, w2 = self.w_q[:, iq1][:, None], self.w_q[:, iq2][None, :]
-        n1, v1 = self._bose(iq1)
-        n2, v2 = self._bose(iq2)
-        n1, n2 = n1[:, None], n2[None, :]
-        valid = np.outer(v1, v2)
-        diff_n = np.zeros(np.broadcast(w1, w2).shape)
-        w_equal = np.abs(w1 - w2) < 1e-8
-        if T > __EPSILON__:
-            beta = RY_TO_K / T
-            safe = np.where(w_equal, 1.0, w1 - w2)
-            diff_n = np.where(w_equal, 0.0, (n1 - n2) / safe)
-            w_eq = np.where(w_equal & valid, w1, 0.0)
-            n_eq = np.where(w_equal & valid, n1, 0.0)
-            deg = np.where(w_equal & valid, -beta * np.exp(w_eq * beta) * n_eq ** 2, 0.0)
-            diff_n = np.where(w_equal, deg, diff_n)
-        wsum = np.where(valid, w1 + w2, 1.0)
-        wprod = np.where(valid, w1 * w2, 1.0)
-        return np.where(valid, ((n1 + n2 + 1) / wsum - diff_n) / (4 * wprod), 0.0)
-
-    def _compute_Y_w(self, iq):
-        """2w / (2n + 1), 0 on masked modes (:546-562)."""
-        w = self.w_q[:, iq]
-        valid = self.qlanc.valid_modes_q[:, iq]
-        n = np.zeros_like(w)
-        if self.qlanc.T > __EPSILON__:
-            n[valid] = 1.0 / (np.exp(w[valid] * RY_TO_K / self.qlanc.T) - 1.0)
-        out = np.zeros_like(w)
-        out[valid] = 2.0 * w[valid] / (2.0 * n[valid] + 1.0)
-        return out
-
-    def _precompute_static_quantities(self):
-        """w^2, 1/w^2, Lambda, 1/Lambda, -2 Y_w1 Y_w2^T per pair (:564-600)."""
-        q = self.qlanc
-        w_qp = self.w_q[:, q.iq_pert]
-        vp = q.valid_modes_q[:, q.iq_pert]
-        self._cached_w_qp_sq = w_qp ** 2
-        self._cached_inv_w_qp_sq = np.where(vp, 1.0 / np.where(vp, w_qp, 1.0) ** 2, 0.0)
-        n_pairs = len(q.unique_pairs)
-        self._cached_lambda = [None] * n_pairs
-        self._cached_inv_lambda = [None] * n_pairs
-        self._cached_yw_outer = [None] * n_pairs
-        for p, (iq1, iq2) in enumerate(q.unique_pairs):
-            lam = self._compute_lambda_q(iq1, iq2)
-            self._cached_lambda[p] = lam
-            ok = np.abs(lam) > 1e-30
-            self._cached_inv_lambda[p] = np.where(ok, 1.0 / np.where(ok, lam, 1.0), 0.0)
-            self._cached_yw_outer[p] = -2.0 * np.outer(self._compute_Y_w(iq1), self._compute_Y_w(iq2))
-
-    # -------------------------------------------------------------- operator
-    def _apply_L_static_q(self, psi):
-        nb = self.n_bands
-        out = np.zeros_like(psi)
-        out[:nb] = self._cached_w_qp_sq * psi[:nb]
-        for p in range(len(self.qlanc.unique_pairs)):
-            self._set_W_block(out, p, self._cached_inv_lambda[p] * self._get_W_block(psi, p))
-        return out + self._apply_anharmonic_static_q(psi)
-
-    def _apply_anharmonic_static_q(self, psi):
-        """R <- -f, W <- d2v from the GPU averages with R1 = psi_R and
-        Y1 = -2 Y_w1 Y_w2 W (:640-692)."""
-        nb = self.n_bands
-        out = np.zeros_like(psi)
-        if self.ignore_v3 and self.ignore_v4:
-            return out
-        R1 = np.array(psi[:nb], dtype=np.complex128)
-        if self.ignore_v3:
-            R1[:] = 0.0
-        Y1 = [self._cached_yw_outer[p] * self._get_W_block(psi, p)
-              for p in range(len(self.qlanc.unique_pairs))]
-        f, d2v = self.qlanc.get_perturb_averages_q(R1, Y1, not self.ignore_v4)
-        out[:nb] = -f
-        for p in range(len(self.qlanc.unique_pairs)):
-            self._set_W_block(out, p, d2v[p])
-        return out
-
-    def _apply_harmonic_preconditioner(self, psi_tilde, sqrt_mask, inv_sqrt_mask):
-        nb = self.n_bands
-        psi = psi_tilde * inv_sqrt_mask
-        res = np.zeros_like(psi)
-        res[:nb] = self._cached_inv_w_qp_sq * psi[:nb]
-        for p in range(len(self.qlanc.unique_pairs)):
-            self._set_W_block(res, p, self._cached_lambda[p] * self._get_W_block(psi, p))
-        return res * sqrt_mask
-
-    def _find_degenerate_blocks(self, iq, threshold=1e-8):
-        """Non-acoustic bands at iq grouped by equal frequency (|dw| < threshold Ry)."""
-        w = self.w_q[:, iq]
-        valid = self.qlanc.valid_modes_q[:, iq]
-        seen, blocks = set(), []
-        for nu in range(self.n_bands):
-            if nu in seen:
-                continue
-            if not valid[nu]:
-                seen.add(nu)
-                continue
-            block = [b for b in range(self.n_bands)
-                     if valid[b] and abs(w[b] - w[nu]) < threshold and b not in seen]
-            seen.update(block)
-            blocks.append(block)
-        return blocks
-
-    # ---------------------------------------------------------------- solver
+    # ---------------------------------------------------------------- solve
     def compute_hessian_at_q(self, iq, tol=1e-6, max_iters=500, use_preconditioner=True,
                              dense_fallback=False, use_mode_symmetry=True):
-        """H_q = inv(G_q), G_q[:, i] the R sector of L_static^-1 e_i (:720-956)."""
+        """H_q at one q-point: one static solve per degenerate group of bands
+        (or per band without use_mode_symmetry), G_q filled by Schur's lemma,
+        H_q the inverse of G_q's Hermitian part on the non-acoustic bands."""
         nb = self.n_bands
-        self.qlanc.build_q_pair_map(iq)
-        psi_size = self._get_static_psi_size()
-        self._precompute_static_quantities()
-        mask = self._static_mask()
-        sqrt_mask = np.sqrt(mask)
-        inv_sqrt_mask = np.zeros_like(sqrt_mask)
-        nz = mask > 0
-        inv_sqrt_mask[nz] = 1.0 / sqrt_mask[nz]
-
-        def apply_L_tilde(x_tilde):
-            return self._apply_L_static_q(x_tilde * inv_sqrt_mask) * sqrt_mask
-
-        L_op = scipy.sparse.linalg.LinearOperator((psi_size, psi_size), matvec=apply_L_tilde,
-                                                  dtype=np.complex128)
-        M_op = None
-        if use_preconditioner:
-            def apply_M_tilde(x_tilde):
-                return self._apply_harmonic_preconditioner(x_tilde, sqrt_mask, inv_sqrt_mask)
-            M_op = scipy.sparse.linalg.LinearOperator((psi_size, psi_size), matvec=apply_M_tilde,
-                                                      dtype=np.complex128)
-        non_acoustic = [nu for nu in range(nb) if self.qlanc.valid_modes_q[nu, iq]]
+        op = self.static_operator(iq)
+        self.last_operator = op
+        valid = self.qlanc.valid_modes_q[:, iq]
         if use_mode_symmetry:
-            schedule = [(b[0], b) for b in self._find_degenerate_blocks(iq)]
+            groups = degenerate_groups(self.w_q[:, iq], valid)
         else:
-            schedule = [(nu, [nu]) for nu in non_acoustic]
+            groups = [[int(b)] for b in np.flatnonzero(valid)]
         if self.verbose:
             print("  Solving at q={} ({} non-acoustic bands, {} solves)".format(
-                iq, len(non_acoustic), len(schedule)))
-        G_q = np.zeros((nb, nb), dtype=np.complex128)
-        total_iters = 0
-        L_dense = None
-        for band_i, block in schedule:
-            rhs = np.zeros(psi_size, dtype=np.complex128)
-            rhs[band_i] = 1.0
-            rhs_tilde = rhs * sqrt_mask
-            x0 = apply_M_tilde(rhs_tilde) if use_preconditioner else None
-            n_it = [0]
-
-            def _count(xk):
-                n_it[0] += 1
-
-            t1 = time.time()
-            x_tilde, info = _gmres(L_op, rhs_tilde, x0, tol, max_iters, M_op, _count)
-            if info != 0:
-                x_tilde, info = _bicgstab(L_op, rhs_tilde, x_tilde, tol, max_iters, M_op)
-                if info != 0:
-                    if not dense_fallback:
-                        raise RuntimeError(
-                            "Iterative solvers (GMRES, BiCGSTAB) did not converge for band {} at "
-                            "iq={} (info={}). Set dense_fallback=True to use a dense solve "
-                            "(warning: O(psi_size^2) memory).".format(band_i, iq, info))
-                    if L_dense is None:
-                        L_dense = np.zeros((psi_size, psi_size), dtype=np.complex128)
-                        for j in range(psi_size):
-                            e_j = np.zeros(psi_size, dtype=np.complex128)
-                            e_j[j] = 1.0
-                            L_dense[:, j] = apply_L_tilde(e_j)
-                        L_dense = (L_dense + L_dense.conj().T) / 2
-                    x_tilde = np.linalg.lstsq(L_dense, rhs_tilde, rcond=1e-10)[0]
-            total_iters += n_it[0]
-            x = x_tilde * inv_sqrt_mask
-            if len(block) == 1:
-                G_q[:, band_i] = x[:nb]
-                for _, other in schedule:
-                    if len(other) >= 2:
-                        for m in other:
-                            G_q[m, band_i] = 0.0
-            else:
-                d = len(block)
-                c_diag = x[band_i]
-                for j in range(d):
-                    col = block[j]
-                    G_q[col, col] = c_diag
-                    for _, other in schedule:
-                        if other[0] == band_i:
-                            continue
-                        if len(other) == d:
-                            G_q[other[j], col] = x[other[0]]
+                iq, int(valid.sum()), len(groups)))
+        M = None
+        if use_preconditioner:
+            M = scipy.sparse.linalg.LinearOperator((op.size, op.size),
+                                                   matvec=op.precondition_tilde,
+                                                   dtype=np.complex128)
+        dense_cache = {}
+        solutions, total = [], 0
+        for g in groups:
+            rhs = np.zeros(op.size, dtype=np.complex128)
+            rhs[g[0]] = op.sqrt_w[g[0]]
+            x0 = op.precondition_tilde(rhs) if use_preconditioner else None
+            t0 = time.time()
+            xt, n_it = _solve_chain(op, rhs, x0, tol, max_iters, M, dense_fallback, dense_cache,
+                                    "band {} at iq={}".format(g[0], iq))
+            total += n_it
+            solutions.append((xt * op.inv_sqrt_w)[:nb])
             if self.verbose:
-                print("    Band {}: {} iters, {:.2f}s".format(band_i, n_it[0], time.time() - t1))
-        G_q = (G_q + G_q.conj().T) / 2
-        H_q = np.zeros((nb, nb), dtype=np.complex128)
-        if non_acoustic:
-            na = np.array(non_acoustic)
-            H_q[np.ix_(na, na)] = np.linalg.inv(G_q[np.ix_(na, na)])
-        H_q = (H_q + H_q.conj().T) / 2
+                print("    Band {}: {} iters, {:.2f}s".format(g[0], n_it, time.time() - t0))
+        G = _fill_green(np.zeros((nb, nb), dtype=np.complex128), groups, solutions, nb)
+        H = np.zeros((nb, nb), dtype=np.complex128)
+        na = np.flatnonzero(valid)
+        if na.size:
+            Gs = G[np.ix_(na, na)]
+            H[np.ix_(na, na)] = np.linalg.inv(0.5 * (Gs + Gs.conj().T))
+        H = 0.5 * (H + H.conj().T)
         if self.verbose:
-            print("  Total L applications: {}".format(total_iters))
-        self.H_q_dict[iq] = H_q
-        return H_q
+            print("  Total L applications: {}".format(total))
+        self.H_q_dict[iq] = H
+        return H
 
     def compute_full_hessian(self, tol=1e-6, max_iters=500, use_preconditioner=True,
                              dense_fallback=False, use_mode_symmetry=True, checkpoint=None):
-        """H_q at every (irreducible) q-point (:958-1049); returns the dict of
-        mode-basis matrices, or a CC.Phonons object when cellconstructor and
-        the crystal structure are available."""
+        """H_q at every q-point, resumable from `checkpoint` (an npz written
+        after each q-point).  Returns the dict of mode-basis matrices, or a
+        CC.Phonons object when cellconstructor and the dynamical matrix exist."""
         if self.irr_qpoints is None:
-            self._all_qpoints()
+            self._every_qpoint()
         done = set()
-        if checkpoint is not None:
-            f = checkpoint if checkpoint.lower().endswith(".npz") else checkpoint + ".npz"
-            if os.path.exists(f):
-                done = self.load_status(checkpoint)
-        for iq in self.irr_qpoints:
-            if iq in done:
-                continue
+        if checkpoint is not None and os.path.exists(_npz_name(checkpoint)):
+            done = self.load_status(checkpoint)
+        for iq in (i for i in self.irr_qpoints if i not in done):
             self.compute_hessian_at_q(iq, tol=tol, max_iters=max_iters,
                                       use_preconditioner=use_preconditioner,
                                       dense_fallback=dense_fallback,
@@ -336,73 +376,68 @@ class QSpaceHessian:
                 self.save_status(checkpoint)
         if getattr(self.qlanc, "dyn", None) is None:
             return self.H_q_dict
-        return self._build_phonons()
+        return self._as_phonons()
 
-    def _build_phonons(self):
+    def _as_phonons(self):
+        """Cartesian force constants Phi_q = P H_q P^dagger, P the mass-scaled
+        polarisation vectors, as a cellconstructor Phonons object."""
         import cellconstructor as CC
-        import cellconstructor.Phonons
-        q_points = np.array(self.qlanc.dyn.q_tot)
-        hessian = CC.Phonons.Phonons(self.qlanc.dyn.structure.copy(), nqirr=self.n_q)
+        import cellconstructor.Phonons  # noqa: F401
+        dyn = self.qlanc.dyn
+        out = CC.Phonons.Phonons(dyn.structure.copy(), nqirr=self.n_q)
+        sqrt_m = np.sqrt(self.qlanc.m)[:, None]
         for iq in range(self.n_q):
-            pol_m = np.einsum("a, ab -> ab", np.sqrt(self.qlanc.m), self.pols_q[:, :, iq])
-            hessian.dynmats[iq] = pol_m @ self.H_q_dict[iq] @ np.conj(pol_m).T
-            hessian.q_tot[iq] = q_points[iq]
-        hessian.AdjustQStar()
-        return hessian
+            P = sqrt_m * self.pols_q[:, :, iq]
+            out.dynmats[iq] = P.dot(self.H_q_dict[iq]).dot(P.conj().T)
+            out.q_tot[iq] = np.array(dyn.q_tot)[iq]
+        out.AdjustQStar()
+        return out
 
-    # ------------------------------------------------------------------- I/O
+    # ---------------------------------------------------------------- files
+    def _metadata(self):
+        return {"T": np.float64(self.qlanc.T), "n_q": np.int64(self.n_q),
+                "n_bands": np.int64(self.n_bands), "ignore_v3": np.bool_(self.ignore_v3),
+                "ignore_v4": np.bool_(self.ignore_v4)}
+
     def save_status(self, fname):
-        if not fname.lower().endswith(".npz"):
-            fname += ".npz"
-        d = dict(T=np.float64(self.qlanc.T), n_q=np.int64(self.n_q),
-                 n_bands=np.int64(self.n_bands), ignore_v3=np.bool_(self.ignore_v3),
-                 ignore_v4=np.bool_(self.ignore_v4))
+        """Checkpoint: the metadata, the solved q-points and their H_q, under
+        the reference's npz keys."""
+        keys = np.array(sorted(self.H_q_dict), dtype=np.int64)
+        values = (np.stack([self.H_q_dict[int(k)] for k in keys]) if keys.size else
+                  np.zeros((0, self.n_bands, self.n_bands), dtype=np.complex128))
+        payload = dict(self._metadata(), completed_irr_qpoints=keys, H_q_keys=keys,
+                       H_q_values=values)
         uci = getattr(self.qlanc, "uci_structure", None)
         if uci is not None:
-            d.update(unit_cell=uci.unit_cell, coords=uci.coords, atom_types=uci.get_atomic_types())
-        done = sorted(self.H_q_dict.keys())
-        d["completed_irr_qpoints"] = np.array(done, dtype=np.int64)
-        d["H_q_keys"] = np.array(done, dtype=np.int64)
-        d["H_q_values"] = (np.stack([self.H_q_dict[iq] for iq in done]) if done else
-                           np.zeros((0, self.n_bands, self.n_bands), dtype=np.complex128))
-        np.savez_compressed(fname, **d)
+            payload.update(unit_cell=uci.unit_cell, coords=uci.coords,
+                           atom_types=uci.get_atomic_types())
+        np.savez_compressed(_npz_name(fname), **payload)
 
     def load_status(self, fname):
-        if not fname.lower().endswith(".npz"):
-            fname += ".npz"
+        """Read a checkpoint into H_q_dict after checking that it belongs to
+        this calculation; returns the set of completed q-points."""
+        fname = _npz_name(fname)
         if not os.path.exists(fname):
             raise IOError("Checkpoint file not found: {}".format(fname))
         data = dict(np.load(fname, allow_pickle=True))
-        bad = []
-        if not np.isclose(float(data["T"]), self.qlanc.T, atol=1e-10):
-            bad.append("T: checkpoint={}, current={}".format(float(data["T"]), self.qlanc.T))
-        if int(data["n_q"]) != self.n_q:
-            bad.append("n_q: checkpoint={}, current={}".format(int(data["n_q"]), self.n_q))
-        if int(data["n_bands"]) != self.n_bands:
-            bad.append("n_bands: checkpoint={}, current={}".format(int(data["n_bands"]),
-                                                                  self.n_bands))
-        if bool(data["ignore_v3"]) != self.ignore_v3:
-            bad.append("ignore_v3 differs")
-        if bool(data["ignore_v4"]) != self.ignore_v4:
-            bad.append("ignore_v4 differs")
-        if bad:
-            raise ValueError("Checkpoint metadata mismatch:\n  " + "\n  ".join(bad))
-        for i, iq in enumerate(data["H_q_keys"].astype(int)):
-            self.H_q_dict[int(iq)] = data["H_q_values"][i]
-        return set(data["completed_irr_qpoints"].astype(int).tolist())
+        mine = self._metadata()
+        problems = []
+        if not np.isclose(float(data["T"]), float(mine["T"]), atol=1e-10):
+            problems.append("T: checkpoint={}, current={}".format(float(data["T"]),
+                                                                 float(mine["T"])))
+        for k in ("n_q", "n_bands"):
+            if int(data[k]) != int(mine[k]):
+                problems.append("{}: checkpoint={}, current={}".format(k, int(data[k]),
+                                                                      int(mine[k])))
+        for k in ("ignore_v3", "ignore_v4"):
+            if bool(data[k]) != bool(mine[k]):
+                problems.append("{} differs".format(k))
+        if problems:
+            raise ValueError("Checkpoint metadata mismatch:\n  " + "\n  ".join(problems))
+        for k, H in zip(data["H_q_keys"].astype(int), data["H_q_values"]):
+            self.H_q_dict[int(k)] = H
+        return {int(k) for k in data["completed_irr_qpoints"]}
 
 
-def _gmres(A, b, x0, tol, maxiter, M, cb):
-    try:
-        return scipy.sparse.linalg.gmres(A, b, x0=x0, rtol=tol, maxiter=maxiter, M=M, callback=cb,
-                                         callback_type="legacy")
-    except TypeError:       # scipy before the rtol keyword
-        return scipy.sparse.linalg.gmres(A, b, x0=x0, tol=tol, maxiter=maxiter, M=M, callback=cb,
-                                         callback_type="legacy")
-
-
-def _bicgstab(A, b, x0, tol, maxiter, M):
-    try:
-        return scipy.sparse.linalg.bicgstab(A, b, x0=x0, rtol=tol, maxiter=maxiter, M=M)
-    except TypeError:
-        return scipy.sparse.linalg.bicgstab(A, b, x0=x0, tol=tol, maxiter=maxiter, M=M)
+def _npz_name(fname):
+    return fname if fname.lower().endswith(".npz") else fname + ".npz"

@@ -36,7 +36,9 @@ def test_spectral_function_and_io(tmp_path):
     w = np.linspace(0, 0.015, 300)
     got = k.get_spectral_function_KPM(w)
     ref = oq.kpm_spectral(w, k.kpm_moments, 1.3, k.kpm_lambda_min, k.kpm_lambda_max)
-    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=0)
+    # the host sums the series by Clenshaw's recurrence, the oracle forward:
+    # equal to rounding, relative to the largest value
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
     np.testing.assert_allclose(QSpaceKPM._jackson_kernel(30), oq.jackson_kernel(30))
     f = str(tmp_path / "m.txt")
     k.save_kpm(f)

@@ -38,3 +38,34 @@ def test_single_q_static_hessian_matches_reference_gpu(gpu_lib, golden):
     H = _hessian(d, use_oracle=False)
     ref = d["hessian"]
     np.testing.assert_allclose(H.real, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+
+
+def test_static_propagator_limits():
+    """Lambda is continuous across the degenerate limit and reduces to
+    1 / (4 w1 w2 (w1 + w2)) at T = 0."""
+    from tdscha_gb300.QSpaceHessian import static_propagator
+    w = np.array([1e-3, 2e-3, 2e-3 + 1e-9, 3e-3])
+    v = np.ones(4, bool)
+    lam = static_propagator(w, v, w, v, 300.0)
+    np.testing.assert_allclose(lam[1, 2], lam[1, 1], rtol=1e-5)
+    # inside the 1e-8 Ry window the derivative is taken at the row mode
+    np.testing.assert_allclose(lam, lam.T, rtol=1e-6)
+    lam0 = static_propagator(w, v, w, v, 0.0)
+    np.testing.assert_allclose(lam0, 1.0 / (4 * np.outer(w, w) * np.add.outer(w, w)), rtol=1e-14)
+    v[0] = False
+    assert np.all(static_propagator(w, v, w, v, 300.0)[0] == 0)
+
+
+def test_degenerate_groups_and_schur_fill():
+    from tdscha_gb300.QSpaceHessian import _fill_green, degenerate_groups
+    w = np.array([0.0, 5.0, 2.0, 5.0, 2.0, 7.0, 5.0])
+    valid = np.array([False, True, True, True, True, True, True])
+    groups = degenerate_groups(w, valid)
+    assert groups == [[1, 3, 6], [2, 4], [5]]
+    nb = len(w)
+    x = {k: np.arange(nb) + 10.0 * k for k in range(3)}
+    G = _fill_green(np.zeros((nb, nb)), groups, [x[0], x[1], x[2]], nb)
+    # triplet: c * I on its own block, nothing else of its size
+    assert G[1, 1] == G[3, 3] == G[6, 6] == x[0][1] and G[3, 1] == 0
+    assert G[2, 2] == G[4, 4] == x[1][2]
+    assert G[5, 5] == x[2][5] and G[1, 5] == 0 and G[2, 5] == 0
