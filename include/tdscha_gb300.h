@@ -193,7 +193,14 @@ int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, in
  * All pointers are device memory owned by the caller: X, Y (N x M), w (M),
  * rho (N), R1 (M), Y1 (M x M) in; f_out (M), d2v_out (M x M) out, written
  * with the same convention as tdscha_perturb_averages (no symmetry images:
- * one identity image per configuration).  Asynchronous on `stream`.
+ * one identity image per configuration).  Asynchronous on `stream`.  The
+ * results agree with tdscha_perturb_averages (float64) to rounding, not bit
+ * for bit: stage B here uses the smallest split-K count.
+ *
+ * Inputs are checked on the device, not on the host: a non-finite entry of
+ * X, Y, R1, Y1 or w, a frequency w <= 0, a negative or non-finite weight in
+ * rho, or sum(rho) = 0 makes every entry of f_out and d2v_out NaN (the call
+ * itself still returns TDSCHA_OK, since it does not wait for the device).
  *
  * Intermediate arrays live in one static 32 MiB device array that every
  * process loading this library holds on each GPU it uses until exit.  Sizes
@@ -202,8 +209,12 @@ int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, in
  * uses the same array (each call writes every word it reads, so nothing
  * carries over), so calls that overlap on the GPU -- on different streams or
  * from different host threads -- race and must be serialised by the caller.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.
+ * The array's device address belongs to a CUDA context (each context that
+ * loads the library gets its own copy).  Every call made outside a stream
+ * capture looks the address up in the current context; a call made while
+ * its stream is being captured reuses the address recorded for the current
+ * context, so make a first call in each context before any stream capture
+ * (otherwise the call returns TDSCHA_ERR_STATE).
  */
 int tdscha_perturb_averages_noalloc(int M, int N, const double *X, const double *Y,
                                     const double *w, const double *rho, const double *R1,

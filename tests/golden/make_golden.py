@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Run in a checkout that has the reference tree (default /root/reference, or
-$TDSCHA_REFERENCE_ROOT) after `oracle/build_ref.sh`:
+Run where the reference tree is available ($TDSCHA_REFERENCE_ROOT, or a
+directory "reference" beside this repository) after `oracle/build_ref.sh`:
 
     python tests/golden/make_golden.py
 
