@@ -184,6 +184,19 @@ int tdscha_ctx_profile(tdscha_ctx *ctx, int enable);
 int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, int *launches);
 
 /*
+ * How the context holds the symmetry images (no counterpart in the reference,
+ * which forms every image row inside its loops, CModules/LanczosFunctions.c:
+ * 2158-2170).  *images_on_perturbation = S when the images are applied to the
+ * perturbation (Y1 -> S_j^T Y1 S_j, R1 -> S_j^T R1, results carried back by
+ * S_j): the ensemble is resident once, *ensemble_rows = N.  This is the case
+ * whenever every symmetry matrix maps only between modes of equal frequency
+ * factors f_Y and f_psi (degenerate modes).  Otherwise, or with
+ * TDSCHA_SYMMETRY_IMAGES=rows in the environment at creation, the N*S image
+ * rows are stored: *images_on_perturbation = 1, *ensemble_rows = N*S.
+ */
+int tdscha_ctx_layout(tdscha_ctx *ctx, int *images_on_perturbation, long long *ensemble_rows);
+
+/*
  * Float64 perturbation averages that allocate no device memory (no
  * counterpart in the reference).  For callers that cannot let a library call
  * cudaMalloc: host programs that reserve the GPU's memory for their own pool

@@ -30,7 +30,7 @@ EXPORTS = [
     "tdscha_lanczos_run_batch", "tdscha_mlp_create", "tdscha_mlp_destroy",
     "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
     "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
-    "tdscha_release_cached_memory",
+    "tdscha_release_cached_memory", "tdscha_ctx_layout",
 ]
 
 
@@ -90,6 +90,7 @@ def load():
                                         _i, _vp]
     lib.tdscha_static_L.argtypes = [_vp, _c_int, _vp, _vp, _c_int, _c_double, _c_int, _vp]
     lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
+    lib.tdscha_ctx_layout.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_longlong)]
     lib.tdscha_release_cached_memory.argtypes = [_vp]
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
@@ -193,6 +194,12 @@ class Context:
                                     1 if with_mixed else 0))
         self.handle = h
         self._opts = None
+
+    def layout(self):
+        """(images applied on the perturbation side, resident ensemble rows)."""
+        j, rows = ctypes.c_int(0), ctypes.c_longlong(0)
+        check(load().tdscha_ctx_layout(self.handle, ctypes.byref(j), ctypes.byref(rows)))
+        return j.value, rows.value
 
     def set_options(self, use_wigner, ignore_harmonic, ignore_v3, ignore_v4, reverse_L, shift):
         opts = (int(bool(use_wigner)), int(bool(ignore_harmonic)), int(bool(ignore_v3)),

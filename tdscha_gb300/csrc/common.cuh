@@ -94,8 +94,23 @@ struct tdscha_ctx {
     double *tr_pols = nullptr, *tr_proj = nullptr, *tr_w1 = nullptr, *tr_w2 = nullptr,
            *tr_w3 = nullptr, *tr_f = nullptr;
     int *tr_perms = nullptr;
-    // image rows (device), R x M
+    // rows of the ensemble (device), Nrows x M: the N configurations when the
+    // symmetry images act on the perturbation (J > 1, symmetry.cu), else the
+    // R = N*S image rows r = i*S + j
     double *D = nullptr, *F = nullptr;
+    long Nrows = 0;
+    int rho_div = 1;            // row r of D belongs to configuration r / rho_div
+    // perturbation-side images: J = S when the images are applied to the
+    // perturbation, 1 when they are materialised (or S = 1).  S_j as sparse
+    // tables of maxdeg entries per mode: column-sparse (rows k with
+    // S_j[k][m] != 0) and row-sparse (columns k with S_j[m][k] != 0), index -1
+    // for unused slots.  [J][M][maxdeg] each.
+    int J = 1, maxdeg = 1;
+    int *sc_idx = nullptr, *sr_idx = nullptr;
+    double *sc_val = nullptr, *sr_val = nullptr;
+    double *Y1all = nullptr;    // float64 path, J x M x M: S_j^T Y1 S_j
+    double *vsv = nullptr;      // J x M: S_j^T (f_Y R1), then J x M: S_j^T R1
+    double *hs = nullptr;       // J x M x M: G_j + G_j^T summed over the splits
     // per-pair coefficients (device), length H, rebuilt by set_options
     double *pc = nullptr;       // 10 arrays of H: see lanczos.cu
     // per-application scratch (device)
@@ -185,6 +200,21 @@ int apply_translation_projection(tdscha_ctx *c, cudaStream_t st);
 void free_translations(tdscha_ctx *c);
 // shared: f / d2v finalisation from the row scalars and G partials
 int finalize_avgs(tdscha_ctx *c, int nsplit, const double *gpart, cudaStream_t st);
+// symmetry.cu: perturbation-side symmetry images
+int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_space,
+              const double *sym, const int *blocks_ids, const std::vector<double> &fy,
+              const std::vector<double> &fp);
+void psi_free(tdscha_ctx *c);
+// J x M vectors S_j^T (f_Y R1) and S_j^T R1 into c->vsv, and (float64 path) the
+// J matrices S_j^T Y1 S_j into c->Y1all
+int psi_perturbation64(tdscha_ctx *c, cudaStream_t st);
+// d2v = -(1 / (S sum rho)) sum_j S_j (G_j + G_j^T) S_j^T and f = (1 / (S sum
+// rho)) sum_j S_j fsum_j from split-K partials G_js[a][b] = gpart[s*sstride +
+// j*jstride + a*lda + b] and force partials fpart[(j*nfchunk + chunk)*M + m]
+int psi_finalize64(tdscha_ctx *c, const double *gpart, int nsplit, long sstride, long jstride,
+                   long lda, const double *fpart, int nfchunk, cudaStream_t st);
+int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, long jstride,
+                   long lda, const float *fpart, int nfchunk, cudaStream_t st);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 

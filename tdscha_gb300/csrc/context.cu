@@ -72,6 +72,13 @@ __global__ void k_expand_images(const double *__restrict__ X, const double *__re
     }
 }
 
+// The smallest index of a non-finite entry of X or Y (N x M, already copied).
+__global__ void k_first_nonfinite(const double *__restrict__ X, const double *__restrict__ Y,
+                                  long n, unsigned long long *__restrict__ first_bad) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        if (!isfinite(X[e]) || !isfinite(Y[e])) atomicMin(first_bad, (unsigned long long)e);
+}
+
 }  // namespace tdscha
 
 using namespace tdscha;
@@ -190,6 +197,7 @@ static void ctx_free(tdscha_ctx *c) {
     cached_free(c->tri);
     cached_free(c->lam_static);
     free_translations(c);
+    psi_free(c);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
     if (c->stat_host) cudaFreeHost(c->stat_host);
     delete c;
@@ -286,6 +294,31 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     CUC(cudaMemcpy(c->Yw, yw.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
     CUC(cudaMemcpy(c->ReAw, reaw.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
     CUC(cudaMemcpy(c->rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice));
+    // symmetry images on the perturbation side when the tables allow it
+    TRYC(psi_setup(c, n_blocks, n_deg, deg_space, sym, blocks_ids, fy, fp));
+    c->Nrows = c->J > 1 ? (long)N : c->R;
+    c->rho_div = c->J > 1 ? 1 : N_syms;
+    if (c->J > 1) {
+        // the N configurations once; no image rows
+        TRYC(dev_alloc(&c->D, (size_t)N * M)); TRYC(dev_alloc(&c->F, (size_t)N * M));
+        TRYC(dev_alloc(&d_bad, 1));
+        CUC(cudaMemcpy(d_bad, &h_bad, sizeof(h_bad), cudaMemcpyHostToDevice));
+        CUC(cudaMemcpy(c->D, X, sizeof(double) * N * M, cudaMemcpyHostToDevice));
+        CUC(cudaMemcpy(c->F, Y, sizeof(double) * N * M, cudaMemcpyHostToDevice));
+        long total = (long)N * M;
+        int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+        k_first_nonfinite<<<blocks, 256>>>(c->D, c->F, total, d_bad);
+        CUC(cudaGetLastError());
+        CUC(cudaMemcpy(&h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost));
+        if (h_bad != ~0ULL) {
+            set_error("ctx_create: non-finite X/Y at %ld", (long)h_bad);
+            rc = TDSCHA_ERR_NAN;
+            goto fail;
+        }
+        cached_free(d_bad);
+        d_bad = nullptr;
+        goto images_done;
+    }
 
     TRYC(dev_alloc(&c->D, (size_t)c->R * M)); TRYC(dev_alloc(&c->F, (size_t)c->R * M));
     TRYC(dev_alloc(&d_X, (size_t)N * M)); TRYC(dev_alloc(&d_Y, (size_t)N * M));
@@ -320,6 +353,7 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
     cached_free(d_bad);
     d_X = d_Y = nullptr; d_ndeg = d_degoff = d_space = d_bid = nullptr; d_symoff = nullptr; d_sym = nullptr;
     d_bad = nullptr;
+images_done:
 
     TRYC(dev_alloc(&c->R1, M)); TRYC(dev_alloc(&c->Y1, (size_t)M * M));
     TRYC(dev_alloc(&c->f, M)); TRYC(dev_alloc(&c->d2v, (size_t)M * M));
@@ -483,6 +517,18 @@ extern "C" int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *t
     }
     *total_ms = tot;
     *launches = (int)ctx->prof_ev[kernel_id].size();
+    return TDSCHA_OK;
+}
+
+extern "C" int tdscha_ctx_layout(tdscha_ctx *ctx, int *images_on_perturbation,
+                                 long long *ensemble_rows) {
+    set_error("");
+    if (!ctx || !images_on_perturbation || !ensemble_rows) {
+        set_error("ctx_layout: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    *images_on_perturbation = ctx->J;
+    *ensemble_rows = ctx->Nrows;
     return TDSCHA_OK;
 }
 

@@ -25,12 +25,15 @@ constexpr int kBK = 16;    // K step
 
 // Stage A: per 64-row x 64-column tile of V = D Y1, partial row dots with d
 // and g over the tile's columns.  qp_part[(ct*2 + 0)*R + r] = q partial,
-// [(ct*2 + 1)*R + r] = p partial.
+// [(ct*2 + 1)*R + r] = p partial.  blockIdx.z = j selects the perturbation
+// image: Y1 the j-th of consecutive M x M matrices, partials at j*nct*2*R.
 __global__ void __launch_bounds__(256) k_stageA64(const double *__restrict__ D,
                                                   const double *__restrict__ F,
                                                   const double *__restrict__ Y1,
                                                   const double *__restrict__ fpsi, int M,
                                                   long R, double *__restrict__ qp_part) {
+    Y1 += blockIdx.z * (long)M * M;
+    qp_part += blockIdx.z * (long)gridDim.y * 2 * R;
     __shared__ double As[kBK][kT + 1];
     __shared__ double Bs[kBK][kT];
     int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -125,11 +128,56 @@ __global__ void k_rows64(const double *__restrict__ D, const double *__restrict_
     }
 }
 
+// Row scalars of the pairs (configuration i, perturbation image j), one warp
+// per pair r = j*N + i: s = x_i . vs_j, t = y_i . vt_j (vs_j = S_j^T (f_Y R1),
+// vt_j = S_j^T R1), q, p from the stage A partials of image j.
+__global__ void k_rows64_img(const double *__restrict__ D, const double *__restrict__ F,
+                             const double *__restrict__ vs, const double *__restrict__ vt,
+                             const double *__restrict__ rho, const double *__restrict__ qp_part,
+                             int nct, int M, long N, int J, int apply_d4,
+                             double *__restrict__ alpha, double *__restrict__ beta,
+                             double *__restrict__ c1, double *__restrict__ c2) {
+    int lane = threadIdx.x & 31;
+    long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (r >= (long)J * N) return;
+    long j = r / N, i = r - j * N;
+    const double *x = D + i * M, *y = F + i * M, *a = vs + j * M, *b = vt + j * M;
+    double s = 0, t = 0;
+    for (int m = lane; m < M; m += 32) {
+        s = fma(a[m], x[m], s);
+        t = fma(b[m], y[m], t);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    if (lane == 0) {
+        double q = 0, p = 0;
+        const double *qp = qp_part + j * nct * 2 * N;
+        for (int ct = 0; ct < nct; ++ct) {
+            q += qp[(long)(ct * 2 + 0) * N + i];
+            p += qp[(long)(ct * 2 + 1) * N + i];
+        }
+        double rw = rho[i];
+        double d4 = apply_d4 ? 1.0 : 0.0;
+        alpha[r] = rw * (s / 3 - d4 * q / 8);
+        beta[r] = rw * (t / 3 - d4 * p / 4);
+        c1[r] = -rw * q / 6;
+        c2[r] = -rw * p / 3;
+    }
+}
+
 // f partials: fpart[chunk][m] = sum_{r in chunk} c1_r f_r[m] + c2_r u_r[m].
+// blockIdx.z = j: row scalars of perturbation image j (at j*R), partials at
+// j*nchunk*M.
 __global__ void k_favg64(const double *__restrict__ D, const double *__restrict__ F,
                          const double *__restrict__ fY, const double *__restrict__ c1,
                          const double *__restrict__ c2, int M, long R, long chunk,
                          double *__restrict__ fpart) {
+    c1 += blockIdx.z * R;
+    c2 += blockIdx.z * R;
+    fpart += (long)blockIdx.z * gridDim.y * M;
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     long rb = (long)blockIdx.y * chunk, re = min(R, rb + chunk);
@@ -142,6 +190,8 @@ __global__ void k_favg64(const double *__restrict__ D, const double *__restrict_
 }
 
 // Stage B: split-K partial of G = U^T W over the rows of one chunk.
+// blockIdx.z = j: alpha, beta of perturbation image j (at j*R), partial tiles
+// at (j*nsplit + split)*M*M.
 __global__ void __launch_bounds__(256) k_stageB64(const double *__restrict__ D,
                                                   const double *__restrict__ F,
                                                   const double *__restrict__ fY,
@@ -149,6 +199,9 @@ __global__ void __launch_bounds__(256) k_stageB64(const double *__restrict__ D,
                                                   const double *__restrict__ beta, int M,
                                                   long R, long chunk, int ntile,
                                                   double *__restrict__ gpart) {
+    alpha += blockIdx.z * R;
+    beta += blockIdx.z * R;
+    gpart += (long)blockIdx.z * gridDim.y * M * M;
     __shared__ double As[kBK][kT];
     __shared__ double Bs[kBK][kT];
     int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -225,7 +278,9 @@ __global__ void k_finalize(const T *__restrict__ gpart, int nsplit, long split_s
 
 int alloc_fp64_scratch(tdscha_ctx *c) {
     int M = c->M;
-    long R = c->R;
+    long R = c->R;          // (configuration, image) pairs
+    long Nr = c->Nrows;     // rows of D, F (R, or N with perturbation-side images)
+    const int J = c->J;
     c->nct64 = ceil_div(M, kT);
     int ntile = ceil_div(M, kT);
     int tiles = ntile * ntile;
@@ -234,13 +289,13 @@ int alloc_fp64_scratch(tdscha_ctx *c) {
     // blocks per SM and 64 rows per split as before; above that minimum, up
     // to 64 splits, the count whose blocks fill whole rounds of 152 SMs best
     // (ties: fewer splits, less partial-tile traffic).
-    const long n_hi = std::max<long>(1, std::min<long>(64, R / 64));
-    const long n_lo = std::min<long>(n_hi, ceil_div(2 * 152, tiles));
+    const long n_hi = std::max<long>(1, std::min<long>(64, Nr / 64));
+    const long n_lo = std::min<long>(n_hi, ceil_div(2 * 152, (long)tiles * J));
     int ns = (int)n_lo;
     {
         double best = -1;
         for (long n = n_lo; n <= n_hi; ++n) {
-            long blocks = (long)tiles * n;
+            long blocks = (long)tiles * J * n;
             double fill = (double)blocks / (double)(ceil_div(blocks, 152) * 152L);
             if (fill > best + 1e-9) {
                 best = fill;
@@ -249,14 +304,14 @@ int alloc_fp64_scratch(tdscha_ctx *c) {
         }
     }
     c->nsplit64 = ns;
-    c->nfchunk = (int)std::min<long>(std::max<long>(1, R / 256), 512);
+    c->nfchunk = (int)std::min<long>(std::max<long>(1, Nr / 256), 512);
     TDS_CUDA(cached_malloc(&c->qp_part, sizeof(double) * 2 * c->nct64 * R));
     TDS_CUDA(cached_malloc(&c->alpha, sizeof(double) * R));
     TDS_CUDA(cached_malloc(&c->beta, sizeof(double) * R));
     TDS_CUDA(cached_malloc(&c->c1, sizeof(double) * R));
     TDS_CUDA(cached_malloc(&c->c2, sizeof(double) * R));
-    TDS_CUDA(cached_malloc(&c->gpart, sizeof(double) * (size_t)ns * M * M));
-    TDS_CUDA(cached_malloc(&c->fpart, sizeof(double) * (size_t)c->nfchunk * M));
+    TDS_CUDA(cached_malloc(&c->gpart, sizeof(double) * (size_t)J * ns * M * M));
+    TDS_CUDA(cached_malloc(&c->fpart, sizeof(double) * (size_t)J * c->nfchunk * M));
     return TDSCHA_OK;
 }
 
@@ -301,7 +356,48 @@ int finalize_avgs_f32(tdscha_ctx *c, int nsplit, const float *gpart, long split_
     return TDSCHA_OK;
 }
 
+// Symmetry images on the perturbation side (symmetry.cu): the same kernels
+// over the N configurations with blockIdx.z = image j, then the S_j applied
+// to the J partial results.
+static int perturb_fp64_img(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
+    const int M = c->M, J = c->J, nct = c->nct64, ns = c->nsplit64, nfc = c->nfchunk;
+    const long N = c->Nrows;
+    TDS_TRY(psi_perturbation64(c, st));
+    {
+        ProfScope ps(c, 0, st);
+        k_stageA64<<<dim3(ceil_div(N, kT), nct, J), 256, 0, st>>>(c->D, c->F, c->Y1all, c->fpsi,
+                                                                   M, N, c->qp_part);
+        TDS_CHECK_LAUNCH();
+    }
+    {
+        ProfScope ps(c, 1, st);
+        k_rows64_img<<<ceil_div((long)J * N, 8), 256, 0, st>>>(
+            c->D, c->F, c->vsv, c->vsv + (long)J * M, c->rho, c->qp_part, nct, M, N, J, apply_d4,
+            c->alpha, c->beta, c->c1, c->c2);
+        TDS_CHECK_LAUNCH();
+    }
+    {
+        ProfScope ps(c, 2, st);
+        long fchunk = (N + nfc - 1) / nfc;
+        k_favg64<<<dim3(ceil_div(M, 128), nfc, J), 128, 0, st>>>(c->D, c->F, c->fY, c->c1, c->c2,
+                                                                 M, N, fchunk, c->fpart);
+        TDS_CHECK_LAUNCH();
+    }
+    const int ntile = ceil_div(M, kT);
+    {
+        ProfScope ps(c, 3, st);
+        long chunk = (N + ns - 1) / ns;
+        k_stageB64<<<dim3(ntile * ntile, ns, J), 256, 0, st>>>(c->D, c->F, c->fY, c->alpha,
+                                                               c->beta, M, N, chunk, ntile,
+                                                               c->gpart);
+        TDS_CHECK_LAUNCH();
+    }
+    const long MM = (long)M * M;
+    return psi_finalize64(c, c->gpart, ns, MM, (long)ns * MM, M, c->fpart, nfc, st);
+}
+
 int perturb_fp64(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
+    if (c->J > 1) return perturb_fp64_img(c, apply_d4, st);
     int M = c->M;
     long R = c->R;
     dim3 gA(ceil_div(R, kT), c->nct64);

@@ -222,14 +222,15 @@ constexpr size_t kPSmem = 1024 + kPStages * (size_t)kPStageBytes + 2 * (size_t)k
 static_assert(kPSmem <= 232448, "stage A shared memory above the per-block limit");
 
 struct StageAArgs {
-    long R;
+    long R;               // rows of D
     int Mp;
     int nkb;              // k-blocks per tile (Mp / 64)
-    int nct;              // column tiles (ceil(Mp / 128))
+    int nct;              // column tiles per perturbation image (ceil(Mp / 128))
+    int J;                // perturbation images: B = [Y1_0 ... Y1_{J-1}] (J x Mp rows)
     int b_box;            // rows of one B (Y1) box: min(128, Mp)
     long ntiles;
     const float *tcol, *vec_s, *vec_t;
-    float *qpst;          // [nct][4][R]
+    float *qpst;          // [J][nct][4][R]
     int *err;
     long long budget;
 };
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
     const long t0 = args.ntiles * blockIdx.x / G;
     const long nloc = args.ntiles * (blockIdx.x + 1) / G - t0;
     const int nct = args.nct, Mp = args.Mp;
+    const long jn = (long)args.J * nct;   // tiles per row block: images x column tiles
     const uint32_t b_bytes = (uint32_t)args.b_box * kPBK * 2;
 
     if (threadIdx.x == 0) {
@@ -319,7 +321,9 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
             long g = 0;
             for (long i = 0; i < nloc && !fail_code; ++i) {
                 long t = t0 + i;
-                int arow = (int)(t / nct) * kBM, brow = (int)(t % nct) * kPBN;
+                const long rem = t % jn;
+                int arow = (int)(t / jn) * kBM;
+                int brow = (int)(rem / nct) * Mp + (int)(rem % nct) * kPBN;   // row of Y1_j
                 for (int kb = 0; kb < args.nkb; ++kb, ++g) {
                     int s = (int)(g % kPStages);
                     uint32_t n = (uint32_t)(g / kPStages);
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
             long g = 0;
             for (long i = 0; i < nloc && !fail_code; ++i) {
                 long t = t0 + i;
-                int brow = (int)(t % nct) * kPBN;
+                int brow = (int)((t % jn) % nct) * kPBN;
                 int ncols = min(kPBN, Mp - brow);
                 const uint32_t idesc = idesc_f16(kBM, ncols);
                 int j = (int)(i & 1);
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
         auto issue_next = [&]() {
             if (iss_i >= nloc) return;
             long t = t0 + iss_i;
-            int arow = (int)(t / nct) * kBM, brow = (int)(t % nct) * kPBN;
+            int arow = (int)(t / jn) * kBM, brow = (int)((t % jn) % nct) * kPBN;
             int e = (int)(issued & 1);
             uint32_t buf = smem_u32(epi + e * kPEpiBytes), bar = efull0 + 8 * e;
             int x = brow + iss_p * kPEpiCols;
@@ -422,9 +426,10 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
         long consumed = 0;
         for (long i = 0; i < nloc; ++i) {
             long t = t0 + i;
-            const int ct = (int)(t % nct);
+            const int jimg = (int)((t % jn) / nct);
+            const int ct = (int)((t % jn) % nct);
             const int brow = ct * kPBN;
-            const long row = (long)(t / nct) * kBM + row_in;
+            const long row = (long)(t / jn) * kBM + row_in;
             const int np = min(kPBN, Mp - brow) / 32;   // 32-column TMEM chunks
             const int j = (int)(i & 1);
             const uint32_t u = (uint32_t)(i >> 1);
@@ -434,9 +439,10 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
             {
                 int c = brow + row_in;
                 bool in = c < Mp;
-                cv[row_in] = in ? args.tcol[c] : 0.f;
-                cv[kPBN + row_in] = in ? args.vec_s[c] : 0.f;
-                cv[2 * kPBN + row_in] = in ? args.vec_t[c] : 0.f;
+                long cj = (long)jimg * Mp + c;
+                cv[row_in] = in ? args.tcol[cj] : 0.f;
+                cv[kPBN + row_in] = in ? args.vec_s[cj] : 0.f;
+                cv[2 * kPBN + row_in] = in ? args.vec_t[cj] : 0.f;
             }
             bool ok = mbar_wait_ab(tfull0 + 8 * j, u & 1, budget, abort);
             __syncwarp();
@@ -500,7 +506,7 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
             if (fail_code) break;
             if (row < args.R) {
                 const long R = args.R;
-                float *o = args.qpst + (long)ct * 4 * R;
+                float *o = args.qpst + ((long)jimg * nct + ct) * 4 * R;
                 o[row] = q;
                 o[R + row] = p;
                 o[2 * R + row] = sacc;
@@ -546,11 +552,14 @@ struct StageBArgs {
     int nkb;              // K blocks per split
     int nkb_total;        // K blocks in all
     int Mp;
-    int ldG;              // leading dimension of the partial tiles
-    int ntile;            // tiles per dimension (ldG / 128)
-    long nitems;          // ntile^2 x nsplit
-    const float *su, *sw; // row scales of U^T and W^T (Mp)
-    float *gpart;         // [nsplit][ldG][ldG]
+    int ldG;              // rows of a partial tile (a: modes, ldG = ntile x 128)
+    int ntile;            // tiles along a
+    int ntile_b;          // tiles along b (the J x Mp rows of W^T, all images)
+    int ldGb;             // columns of a partial tile (ntile_b x 128)
+    int JMp;              // J x Mp
+    long nitems;          // ntile x ntile_b x nsplit
+    const float *su, *sw; // row scales of U^T and W^T (Mp; W^T row j*Mp + b uses sw[b])
+    float *gpart;         // [nsplit][ldG][ldGb]
     int *err;
     long long budget;
 };
@@ -570,7 +579,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
     const long long budget = args.budget;
     const long G = gridDim.x;
     const long nloc = args.nitems > (long)blockIdx.x ? (args.nitems - 1 - blockIdx.x) / G + 1 : 0;
-    const int tiles = args.ntile * args.ntile;
+    const int tiles = args.ntile * args.ntile_b;
     constexpr uint32_t kIdesc = idesc_f16(kBM, kBNB);
 
     if (threadIdx.x == 0) {
@@ -604,7 +613,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
             for (long i = 0; i < nloc && !fail_code; ++i) {
                 long w = blockIdx.x + i * G;
                 int split = (int)(w / tiles), tile = (int)(w % tiles);
-                int arow = (tile / args.ntile) * kBM, brow = (tile % args.ntile) * kBNB;
+                int arow = (tile / args.ntile_b) * kBM, brow = (tile % args.ntile_b) * kBNB;
                 int kb0 = split * args.nkb, nkb = min(args.nkb, args.nkb_total - kb0);
                 for (int kb = 0; kb < nkb; ++kb, ++g) {
                     int s = (int)(g % kQStages);
@@ -681,7 +690,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
         for (long i = 0; i < nloc; ++i) {
             long w = blockIdx.x + i * G;
             int split = (int)(w / tiles), tile = (int)(w % tiles);
-            int arow = (tile / args.ntile) * kBM, brow = (tile % args.ntile) * kBNB;
+            int arow = (tile / args.ntile_b) * kBM, brow = (tile % args.ntile_b) * kBNB;
             const int j = (int)(i & 1);
             const uint32_t u = (uint32_t)(i >> 1);
             // W^T row scales of this tile's columns (two buffers: a thread is at
@@ -689,7 +698,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
             float *cv = colv + j * kBNB;
             {
                 int c = brow + row_in;
-                cv[row_in] = c < args.Mp ? args.sw[c] : 0.f;
+                cv[row_in] = c < args.JMp ? args.sw[c % args.Mp] : 0.f;
             }
             const int a = arow + row_in;
             const float sa = a < args.Mp ? args.su[a] : 0.f;
@@ -700,7 +709,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
                 break;
             }
             tc_fence_after();
-            float *dst = args.gpart + (long)split * args.ldG * args.ldG + (long)a * args.ldG + brow;
+            float *dst = args.gpart + (long)split * args.ldG * args.ldGb + (long)a * args.ldGb + brow;
 #pragma unroll 1
             for (int ch = 0; ch < kBNB / 32; ++ch) {
                 float v[32];
@@ -922,24 +931,96 @@ __global__ void k_prep_y1(const Src src, const double *__restrict__ fY, const do
     }
 }
 
+// The same for perturbation-side symmetry images (symmetry.cu): block
+// (j, n) forms row n of Y1_j = S_j^T Y1 S_j, and the epilogue vectors of image
+// j, (S_j^T (f_Y R1)) and (S_j^T R1) / f_psi, all at j*Mp + n.  The row is
+// staged in dynamic shared memory (Mp floats) between its max and its limbs.
+template <class Src>
+__global__ void k_prep_y1_img(const Src src, const int *__restrict__ sc_idx,
+                              const double *__restrict__ sc_val, int md,
+                              const double *__restrict__ fY, const double *__restrict__ fpsi,
+                              const float *__restrict__ sd, int M, int Mp,
+                              __half *__restrict__ y_hi, __half *__restrict__ y_lo,
+                              float *__restrict__ tcol, float *__restrict__ vs,
+                              float *__restrict__ vt, float *__restrict__ absmax) {
+    pdl_enter();
+    extern __shared__ float yrow[];
+    __shared__ float red[32];
+    const int n = blockIdx.x % Mp, j = blockIdx.x / Mp;
+    const int *ia = sc_idx + ((long)j * M + (n < M ? n : 0)) * md;
+    const double *va = sc_val + ((long)j * M + (n < M ? n : 0)) * md;
+    float mx = 0.f;
+    for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
+        double y = 0;
+        if (n < M && m < M) {
+            const int *ib = sc_idx + ((long)j * M + m) * md;
+            const double *vb = sc_val + ((long)j * M + m) * md;
+            for (int p = 0; p < md && ia[p] >= 0; ++p) {
+                double inner = 0;
+                for (int q = 0; q < md && ib[q] >= 0; ++q)
+                    inner = fma(vb[q], src.y(ia[p], ib[q]), inner);
+                y = fma(va[p], inner, y);
+            }
+        }
+        float ys = (m < M) ? (float)y * sd[m] : 0.f;
+        yrow[m] = ys;
+        mx = fmaxf(mx, fabsf(ys));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) red[0] = v;
+    }
+    __syncthreads();
+    const float t = red[0] > 0.f ? red[0] : 1.f, inv = 1.f / t;
+    const long row = (long)j * Mp + n;
+    for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
+        __half h, l;
+        split_f16(yrow[m] * inv, h, l);
+        y_hi[row * Mp + m] = h;
+        y_lo[row * Mp + m] = l;
+    }
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        if (n < M)
+            for (int p = 0; p < md && ia[p] >= 0; ++p) {
+                const double r1 = src.r(ia[p]);
+                a = fma(va[p], fY[ia[p]] * r1, a);
+                b = fma(va[p], r1, b);
+            }
+        tcol[row] = n < M ? t : 0.f;
+        vs[row] = n < M ? (float)a : 0.f;
+        vt[row] = n < M ? (float)(b / fpsi[n]) : 0.f;
+        if (row == 0) { absmax[0] = 0.f; absmax[1] = 0.f; }
+    }
+}
+
 // Row scalars from the stage A partials (sums in float64), and max |alpha|,
-// max |beta| for the W scales.
-__global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, int S,
+// max |beta| for the W scales.  Row r = j*Nr + i: configuration row i of
+// perturbation image j (J = 1: the image rows themselves, i = r).
+__global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long Nr, int J, int rho_div,
                              const double *__restrict__ rho, int apply_d4,
                              float4 *__restrict__ abcc, float *__restrict__ absmax) {
     pdl_enter();
     long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
     float ma = 0.f, mb = 0.f;
-    if (r < R) {
+    if (r < (long)J * Nr) {
+        const long jj = r / Nr, i = r - jj * Nr;
+        const float *base = qpst + jj * nct * 4 * Nr;
         double q = 0, p = 0, s = 0, t = 0;
         for (int ct = 0; ct < nct; ++ct) {
-            const float *o = qpst + (long)ct * 4 * R;
-            q += o[r];
-            p += o[R + r];
-            s += o[2 * R + r];
-            t += o[3 * R + r];
+            const float *o = base + (long)ct * 4 * Nr;
+            q += o[i];
+            p += o[Nr + i];
+            s += o[2 * Nr + i];
+            t += o[3 * Nr + i];
         }
-        double rw = rho[r / S];
+        double rw = rho[i / rho_div];
         double d4 = apply_d4 ? 1.0 : 0.0;
         // constant reciprocals: float64 division is slow on this part and the
         // results are rounded to fp32 anyway
@@ -978,17 +1059,23 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long R, in
 // fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
 constexpr int kWRows = 8;      // b rows per block
 constexpr int kWChunk = 2048;  // r per block (256 threads x 4 r x 2 passes)
+// blockIdx.z = j: row scalars of perturbation image j (at j*R), W^T rows at
+// j*Mp, force partials at j*nchunk*M.
 __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
                                                 const float *__restrict__ ut32,
                                                 const float4 *__restrict__ abcc,
                                                 const float *__restrict__ absmax,
                                                 const float *__restrict__ fmax,
                                                 const float *__restrict__ su, long R, long Rp,
-                                                int M, __half *__restrict__ wt_hi,
+                                                int M, int Mp, __half *__restrict__ wt_hi,
                                                 __half *__restrict__ wt_lo,
                                                 float *__restrict__ sw_out,
                                                 float *__restrict__ fpart) {
     pdl_enter();
+    abcc += blockIdx.z * R;
+    wt_hi += (long)blockIdx.z * Mp * Rp;
+    wt_lo += (long)blockIdx.z * Mp * Rp;
+    fpart += (long)blockIdx.z * gridDim.y * M;
     __shared__ float red[kWRows][8];
     int b0 = blockIdx.x * kWRows;
     long r0 = (long)blockIdx.y * kWChunk;
@@ -1001,7 +1088,7 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
         if (!(sw > 0.f)) sw = 1.f;
         inv[k] = 1.f / sw;
         facc[k] = 0.f;
-        if (blockIdx.y == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
+        if (blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
     }
     // Rp is a multiple of 64 and r0 of 2048, so each 4-group is in bounds of
     // the padded rows; rows r >= R carry alpha = beta = c1 = c2 = 0 there.
@@ -1202,6 +1289,7 @@ struct MixedExtra {
     float *fpart = nullptr;
     int nfchunk = 0;
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
+    int ntBb = 0, ldGb = 0;   // stage B tiles / columns along the J x Mp rows of W^T
     int nsm = 1;
     long long budget = kDefaultBudget;
 };
@@ -1210,8 +1298,8 @@ static MixedExtra *extra(tdscha_ctx *c) { return reinterpret_cast<MixedExtra *>(
 
 int mixed_prepare(tdscha_ctx *c) {
     MixedStore &mx = c->mx;
-    const int M = c->M;
-    const long R = c->R;
+    const int M = c->M, J = c->J;
+    const long R = c->Nrows;   // rows of D, F: image rows, or the N configurations
     mx.Mp = ((M + 63) / 64) * 64;
     mx.Rp = ((R + 63) / 64) * 64;
     const int Mp = mx.Mp;
@@ -1229,6 +1317,8 @@ int mixed_prepare(tdscha_ctx *c) {
     }
     x->ldG = ((Mp + kBM - 1) / kBM) * kBM;
     x->ntB = x->ldG / kBM;
+    x->ntBb = ceil_div((long)J * Mp, kBNB);
+    x->ldGb = x->ntBb * kBNB;
     x->nkbB = (int)(Rp / kBK);
     long split_rows = kSplitRows;
     if (const char *e = getenv("TDSCHA_SPLIT_ROWS")) split_rows = std::max(64L, atol(e));
@@ -1237,7 +1327,7 @@ int mixed_prepare(tdscha_ctx *c) {
     {
         // among split counts up to `want`, take the one whose grid fills the
         // 152 SMs in whole waves best (ties: more splits)
-        const int tiles = x->ntB * x->ntB;
+        const int tiles = x->ntB * x->ntBb;
         int best = want;
         double best_fill = 0;
         for (int n = std::max(1, want / 2); n <= want; ++n) {
@@ -1262,21 +1352,23 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cached_malloc(&mx.ut_lo, 2 * colN));
     TDS_CUDA(cached_malloc(&mx.ut32, 4 * colN));
     TDS_CUDA(cached_malloc(&mx.ft32, 4 * colN));
-    TDS_CUDA(cached_malloc(&mx.wt_hi, 2 * colN));
-    TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * colN));
-    TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)Mp * Mp));
-    TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)Mp * Mp));
-    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * mx.nctile * R));
-    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldG));
-    float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw, &x->tcol, &x->vs, &x->vt};
+    TDS_CUDA(cached_malloc(&mx.wt_hi, 2 * (size_t)J * colN));
+    TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * (size_t)J * colN));
+    TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)J * Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)J * Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * mx.nctile * (size_t)J * R));
+    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldGb));
+    float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw};
     for (float **v : vecs) TDS_CUDA(cached_malloc(v, sizeof(float) * Mp));
+    float **jvecs[] = {&x->tcol, &x->vs, &x->vt};
+    for (float **v : jvecs) TDS_CUDA(cached_malloc(v, sizeof(float) * (size_t)J * Mp));
     TDS_CUDA(cached_malloc(&x->absmax, sizeof(float) * 2));
-    TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * R));
-    TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)x->nfchunk * M));
+    TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * (size_t)J * R));
+    TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)J * x->nfchunk * M));
     TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
     *mx.err_flag = 0;
-    TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * colN));
-    TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * colN));
+    TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * (size_t)J * colN));
+    TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * (size_t)J * colN));
     TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * Mp));
     {
         float *dmax = nullptr;
@@ -1307,12 +1399,12 @@ int mixed_prepare(tdscha_ctx *c) {
     }
     TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
     TDS_TRY(make_map(&x->tmA.a_lo, mx.d_lo, Mp, R, kBM));
-    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, Mp, x->bnA));
-    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, Mp, x->bnA));
+    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, x->bnA));
+    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, x->bnA));
     TDS_TRY(make_map(&x->tmB.a_hi, mx.ut_hi, Rp, Mp, kBM));
     TDS_TRY(make_map(&x->tmB.a_lo, mx.ut_lo, Rp, Mp, kBM));
-    TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, Mp, kBNB));
-    TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, Mp, kBNB));
+    TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, (uint64_t)J * Mp, kBNB));
+    TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, (uint64_t)J * Mp, kBNB));
     TDS_TRY(make_map_f32(&x->te.d, x->d32, Mp, R));
     TDS_TRY(make_map_f32(&x->te.g, mx.g32, Mp, R));
     static bool attr_done = false;
@@ -1373,11 +1465,24 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     MixedStore &mx = c->mx;
     MixedExtra *x = extra(c);
     if (!x) { set_error("mixed store not prepared"); return TDSCHA_ERR_STATE; }
-    const int M = c->M, Mp = mx.Mp;
-    const long R = c->R, Rp = mx.Rp;
+    const int M = c->M, Mp = mx.Mp, J = c->J;
+    const long R = c->Nrows, Rp = mx.Rp;
     int *err_dev = nullptr;
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
-    {
+    if (J > 1) {
+        // perturbation-side symmetry images: Y1_j = S_j^T Y1 S_j for every j
+        ProfScope ps(c, 5, st);
+        const size_t sm = sizeof(float) * Mp;
+        if (psrc)
+            TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, J * Mp, 256, sm, st, *psrc, c->sc_idx,
+                                c->sc_val, c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi,
+                                mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
+        else
+            TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st,
+                                Y1FromBuffers{c->Y1, c->R1, M}, c->sc_idx, c->sc_val, c->maxdeg,
+                                c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs,
+                                x->vt, x->absmax));
+    } else {
         ProfScope ps(c, 5, st);
         if (psrc)
             TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, *psrc, c->fY, c->fpsi, x->sd,
@@ -1392,8 +1497,9 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     ga.Mp = Mp;
     ga.nkb = Mp / kPBK;
     ga.nct = mx.nctile;
+    ga.J = J;
     ga.b_box = x->bnA;
-    ga.ntiles = (long)ceil_div(R, kBM) * mx.nctile;
+    ga.ntiles = (long)ceil_div(R, kBM) * J * mx.nctile;
     ga.tcol = x->tcol;
     ga.vec_s = x->vs;
     ga.vec_t = x->vt;
@@ -1407,14 +1513,14 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     }
     {
         ProfScope ps(c, 1, st);
-        TDS_CUDA(launch_pdl(k_rows_mixed, ceil_div(R, 128), 128, 0, st, mx.qp, mx.nctile, R, c->S,
-                            c->rho, apply_d4, x->abcc, x->absmax));
+        TDS_CUDA(launch_pdl(k_rows_mixed, ceil_div((long)J * R, 128), 128, 0, st, mx.qp,
+                            mx.nctile, R, J, c->rho_div, c->rho, apply_d4, x->abcc, x->absmax));
     }
     {
         ProfScope ps(c, 2, st);
-        dim3 g(ceil_div(M, kWRows), x->nfchunk);
+        dim3 g(ceil_div(M, kWRows), x->nfchunk, J);
         TDS_CUDA(launch_pdl(k_wbuild, g, 256, 0, st, mx.ft32, mx.ut32, x->abcc, x->absmax, x->fmx,
-                            x->su, R, Rp, M, mx.wt_hi, mx.wt_lo, x->sw, x->fpart));
+                            x->su, R, Rp, M, Mp, mx.wt_hi, mx.wt_lo, x->sw, x->fpart));
     }
     StageBArgs gb{};
     gb.nkb = x->kbps;
@@ -1422,7 +1528,10 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     gb.Mp = Mp;
     gb.ldG = x->ldG;
     gb.ntile = x->ntB;
-    gb.nitems = (long)x->ntB * x->ntB * mx.nsplit;
+    gb.ntile_b = x->ntBb;
+    gb.ldGb = x->ldGb;
+    gb.JMp = J * Mp;
+    gb.nitems = (long)x->ntB * x->ntBb * mx.nsplit;
     gb.su = x->su;
     gb.sw = x->sw;
     gb.gpart = mx.gpart;
@@ -1433,6 +1542,9 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
         int grid = (int)std::min<long>(gb.nitems, x->nsm);
         TDS_CUDA(launch_pdl(k_stageB_tc, grid, 192, kQSmem, st, x->tmB, gb));
     }
+    if (J > 1)
+        return psi_finalize32(c, mx.gpart, mx.nsplit, (long)x->ldG * x->ldGb, Mp, x->ldGb,
+                              x->fpart, x->nfchunk, st);
     {
         ProfScope ps(c, 4, st);
         const int nt = ceil_div(M, 32);

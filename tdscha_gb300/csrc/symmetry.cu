@@ -1,0 +1,240 @@
+// Symmetry images on the perturbation side.
+//
+// The reference forms every image row d = S_j X_i, f = S_j Y_i inside its
+// loops (CModules/LanczosFunctions.c:2158-2170, :2360-2372, :2673-2685;
+// Modules/tdscha_core.jl:86-87).  The symmetry matrices only mix modes of one
+// degenerate block; when each of them maps only between modes of equal f_Y
+// and equal f_psi (degenerate modes have equal frequencies), S_j commutes
+// with diag(f_Y) and diag(f_psi), and every sum over the image rows becomes a
+// sum over the N configurations of the perturbation carried to the image:
+//
+//   q_ij = x_i . (Y1_j x_i),        Y1_j = S_j^T Y1 S_j
+//   p_ij = g_i . (Y1_j x_i),        g_i  = f_psi * y_i
+//   s_ij = x_i . S_j^T (f_Y * R1),  t_ij = y_i . S_j^T R1
+//   f    =  sum_j S_j [sum_i c1_ij y_i + c2_ij u_i]              / (S sum rho)
+//   d2v  = -sum_j S_j (G_j + G_j^T) S_j^T                        / (S sum rho)
+//   G_j  =  sum_i u_i (alpha_ij y_i + beta_ij/2 u_i)^T,          u_i = f_Y * x_i
+//
+// with alpha, beta, c1, c2 the reference's row scalars of image row (i, j).
+// No image row is stored: stage A is one GEMM X [Y1_1 ... Y1_S] that reads
+// the ensemble once for all images, stage B weights the same rows once per
+// image, and the S_j act only on M-vectors and M x M matrices.  Contexts
+// whose symmetry tables do not commute with the frequency factors (or with
+// TDSCHA_SYMMETRY_IMAGES=rows in the environment) keep the image rows.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace tdscha {
+
+// vs[j][m] = (S_j^T (f_Y R1))[m], vt[j][m] = (S_j^T R1)[m]
+__global__ void k_psi_vec(const int *__restrict__ sc_idx, const double *__restrict__ sc_val,
+                          const double *__restrict__ fY, const double *__restrict__ R1, int J,
+                          int M, int md, double *__restrict__ vs, double *__restrict__ vt) {
+    long n = (long)J * M;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int *ix = sc_idx + e * md;
+        const double *vv = sc_val + e * md;
+        double a = 0, b = 0;
+        for (int k = 0; k < md; ++k) {
+            int r = ix[k];
+            if (r < 0) break;
+            a = fma(vv[k], fY[r] * R1[r], a);
+            b = fma(vv[k], R1[r], b);
+        }
+        vs[e] = a;
+        vt[e] = b;
+    }
+}
+
+// Y1all[j][a][b] = sum_{k, l} S_j[k][a] Y1[k][l] S_j[l][b] (Y1 symmetric)
+__global__ void k_psi_y1(const int *__restrict__ sc_idx, const double *__restrict__ sc_val,
+                         const double *__restrict__ Y1, int J, int M, int md,
+                         double *__restrict__ Y1all) {
+    long MM = (long)M * M, n = (long)J * MM;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        long j = e / MM;
+        int a = (int)((e - j * MM) / M), b = (int)(e % M);
+        const int *ia = sc_idx + (j * M + a) * md, *ib = sc_idx + (j * M + b) * md;
+        const double *va = sc_val + (j * M + a) * md, *vb = sc_val + (j * M + b) * md;
+        double acc = 0;
+        for (int p = 0; p < md && ia[p] >= 0; ++p) {
+            double inner = 0;
+            const double *row = Y1 + (long)ia[p] * M;
+            for (int q = 0; q < md && ib[q] >= 0; ++q) inner = fma(vb[q], row[ib[q]], inner);
+            acc = fma(va[p], inner, acc);
+        }
+        Y1all[e] = acc;
+    }
+}
+
+// hs[j][k][l] = sum_s G_js[k][l] + G_js[l][k], G_js[k][l] = g[s*ss + j*js + k*lda + l],
+// summed in float64 in split order; fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m].
+template <typename T>
+__global__ void k_psi_hsum(const T *__restrict__ g, int nsplit, long ss, long js, long lda,
+                           const T *__restrict__ fpart, int nfc, int J, int M,
+                           double *__restrict__ hs, double *__restrict__ fs) {
+    long MM = (long)M * M, n = (long)J * MM;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        long j = e / MM;
+        int k = (int)((e - j * MM) / M), l = (int)(e % M);
+        const T *base = g + j * js;
+        double acc = 0;
+        for (int s = 0; s < nsplit; ++s) {
+            const T *gs = base + s * ss;
+            acc += (double)gs[k * lda + l] + (double)gs[l * lda + k];
+        }
+        hs[e] = acc;
+        if (k == 0) {
+            double f = 0;
+            for (int ch = 0; ch < nfc; ++ch) f += (double)fpart[(j * nfc + ch) * M + l];
+            fs[j * M + l] = f;
+        }
+    }
+}
+
+// d2v[a][b] = -inv sum_j sum_{k, l} S_j[a][k] hs[j][k][l] S_j[b][l]
+// f[a]      =  inv sum_j sum_k S_j[a][k] fs[j][k]
+__global__ void k_psi_sandwich(const int *__restrict__ sr_idx, const double *__restrict__ sr_val,
+                               const double *__restrict__ hs, const double *__restrict__ fs,
+                               int J, int M, int md, double inv, double *__restrict__ f,
+                               double *__restrict__ d2v) {
+    long MM = (long)M * M;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < MM; e += (long)gridDim.x * blockDim.x) {
+        int a = (int)(e / M), b = (int)(e % M);
+        double acc = 0, facc = 0;
+        for (int j = 0; j < J; ++j) {
+            const int *ia = sr_idx + ((long)j * M + a) * md, *ib = sr_idx + ((long)j * M + b) * md;
+            const double *va = sr_val + ((long)j * M + a) * md, *vb = sr_val + ((long)j * M + b) * md;
+            const double *H = hs + (long)j * MM;
+            for (int p = 0; p < md && ia[p] >= 0; ++p) {
+                double inner = 0;
+                const double *row = H + (long)ia[p] * M;
+                for (int q = 0; q < md && ib[q] >= 0; ++q) inner = fma(vb[q], row[ib[q]], inner);
+                acc = fma(va[p], inner, acc);
+                if (b == 0) facc = fma(va[p], fs[(long)j * M + ia[p]], facc);
+            }
+        }
+        d2v[e] = -acc * inv;
+        if (b == 0) f[a] = facc * inv;
+    }
+}
+
+static int grid_for(long n) { return (int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 16)); }
+
+int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_space,
+              const double *sym, const int *blocks_ids, const std::vector<double> &fy,
+              const std::vector<double> &fp) {
+    const int M = c->M, S = c->S;
+    c->J = 1;
+    c->maxdeg = 1;
+    if (S <= 1) return TDSCHA_OK;
+    const char *mode = getenv("TDSCHA_SYMMETRY_IMAGES");
+    if (mode && !strcmp(mode, "rows")) return TDSCHA_OK;
+    std::vector<int> off(n_blocks);
+    std::vector<long> soff(n_blocks);
+    int md = 1;
+    for (int b = 0, acc = 0; b < n_blocks; ++b) {
+        off[b] = acc;
+        acc += n_deg[b];
+        md = std::max(md, n_deg[b]);
+    }
+    for (int b = 1; b < n_blocks; ++b) soff[b] = soff[b - 1] + (long)S * n_deg[b - 1] * n_deg[b - 1];
+    // row-sparse S_j: row mu from block blocks_ids[mu], mu_id = mu - space[0]
+    // (the reference's convention, LanczosFunctions.c:2158-2170)
+    const size_t cells = (size_t)S * M * md;
+    std::vector<int> ri(cells, -1), ci(cells, -1);
+    std::vector<double> rv(cells, 0.0), cv(cells, 0.0);
+    std::vector<int> ccount((size_t)S * M, 0);
+    for (int j = 0; j < S; ++j)
+        for (int mu = 0; mu < M; ++mu) {
+            int b = blocks_ids[mu], bd = n_deg[b];
+            const int *space = deg_space + off[b];
+            int mu_id = mu - space[0];
+            const double *row = sym + soff[b] + ((long)j * bd + mu_id) * bd;
+            int nr = 0;
+            for (int k = 0; k < bd; ++k) {
+                if (row[k] == 0.0) continue;
+                int nu = space[k];
+                // the images must not mix modes of different f_Y or f_psi
+                if (fy[mu] != fy[nu] || fp[mu] != fp[nu]) return TDSCHA_OK;
+                size_t rs = ((size_t)j * M + mu) * md + nr++;
+                ri[rs] = nu;
+                rv[rs] = row[k];
+                int &cnt = ccount[(size_t)j * M + nu];
+                if (cnt >= md) return TDSCHA_OK;   // overlapping blocks: keep image rows
+                size_t cs = ((size_t)j * M + nu) * md + cnt++;
+                ci[cs] = mu;
+                cv[cs] = row[k];
+            }
+        }
+    TDS_CUDA(cached_malloc(&c->sr_idx, sizeof(int) * cells));
+    TDS_CUDA(cached_malloc(&c->sc_idx, sizeof(int) * cells));
+    TDS_CUDA(cached_malloc(&c->sr_val, sizeof(double) * cells));
+    TDS_CUDA(cached_malloc(&c->sc_val, sizeof(double) * cells));
+    TDS_CUDA(cudaMemcpy(c->sr_idx, ri.data(), sizeof(int) * cells, cudaMemcpyHostToDevice));
+    TDS_CUDA(cudaMemcpy(c->sc_idx, ci.data(), sizeof(int) * cells, cudaMemcpyHostToDevice));
+    TDS_CUDA(cudaMemcpy(c->sr_val, rv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
+    TDS_CUDA(cudaMemcpy(c->sc_val, cv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
+    TDS_CUDA(cached_malloc(&c->vsv, sizeof(double) * 2 * (size_t)S * M));
+    TDS_CUDA(cached_malloc(&c->hs, sizeof(double) * ((size_t)S * M * M + (size_t)S * M)));
+    c->J = S;
+    c->maxdeg = md;
+    return TDSCHA_OK;
+}
+
+void psi_free(tdscha_ctx *c) {
+    cached_free(c->sr_idx);
+    cached_free(c->sc_idx);
+    cached_free(c->sr_val);
+    cached_free(c->sc_val);
+    cached_free(c->Y1all);
+    cached_free(c->vsv);
+    cached_free(c->hs);
+    c->sr_idx = c->sc_idx = nullptr;
+    c->sr_val = c->sc_val = c->Y1all = c->vsv = c->hs = nullptr;
+}
+
+int psi_perturbation64(tdscha_ctx *c, cudaStream_t st) {
+    const int M = c->M, J = c->J, md = c->maxdeg;
+    k_psi_vec<<<grid_for((long)J * M), 256, 0, st>>>(c->sc_idx, c->sc_val, c->fY, c->R1, J, M, md,
+                                                     c->vsv, c->vsv + (long)J * M);
+    TDS_CHECK_LAUNCH();
+    if (!c->Y1all) TDS_CUDA(cached_malloc(&c->Y1all, sizeof(double) * (size_t)J * M * M));
+    k_psi_y1<<<grid_for((long)J * M * M), 256, 0, st>>>(c->sc_idx, c->sc_val, c->Y1, J, M, md,
+                                                        c->Y1all);
+    TDS_CHECK_LAUNCH();
+    return TDSCHA_OK;
+}
+
+template <typename T>
+static int psi_finalize(tdscha_ctx *c, const T *gpart, int nsplit, long sstride, long jstride,
+                        long lda, const T *fpart, int nfchunk, cudaStream_t st) {
+    const int M = c->M, J = c->J;
+    double *hs = c->hs, *fs = c->hs + (size_t)J * M * M;
+    {
+        ProfScope ps(c, 4, st);
+        k_psi_hsum<T><<<grid_for((long)J * M * M), 256, 0, st>>>(gpart, nsplit, sstride, jstride,
+                                                                 lda, fpart, nfchunk, J, M, hs, fs);
+        TDS_CHECK_LAUNCH();
+        k_psi_sandwich<<<grid_for((long)M * M), 256, 0, st>>>(c->sr_idx, c->sr_val, hs, fs, J, M,
+                                                             c->maxdeg, 1.0 / (c->sum_rho * c->S),
+                                                             c->f, c->d2v);
+        TDS_CHECK_LAUNCH();
+    }
+    return TDSCHA_OK;
+}
+
+int psi_finalize64(tdscha_ctx *c, const double *gpart, int nsplit, long sstride, long jstride,
+                   long lda, const double *fpart, int nfchunk, cudaStream_t st) {
+    return psi_finalize<double>(c, gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, st);
+}
+
+int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, long jstride,
+                   long lda, const float *fpart, int nfchunk, cudaStream_t st) {
+    return psi_finalize<float>(c, gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, st);
+}
+
+}  // namespace tdscha

@@ -136,7 +136,9 @@ def random_sym(M, seed=2, scale=1.0):
 # Workloads named by what they are (mode count, configurations, images, steps).
 WORKLOADS = {
     "m21_n1k": dict(M=21, N=1000, n_syms=1, rho_sigma=0.0, steps=50),
-    "m189_n10k_s48": dict(M=189, N=10000, n_syms=48, rho_sigma=0.1, steps=200),
+    # check_steps: the mixed-vs-float64 spectral check runs over the window in
+    # which two float64 runs of this symmetric operator reproduce each other
+    "m189_n10k_s48": dict(M=189, N=10000, n_syms=48, rho_sigma=0.1, steps=200, check_steps=50),
     "m573_n50k": dict(M=573, N=50000, n_syms=1, rho_sigma=0.1, steps=300),
     # same modes, 20 000 configurations: the operands still exceed L2 but the
     # whole context stays under 1 GB (used for full profiler captures)
