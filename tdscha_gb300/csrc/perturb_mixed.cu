@@ -46,7 +46,11 @@ constexpr int kBM = 128;          // tile rows (TMEM lanes)
 constexpr int kBK = 64;           // K block: 64 fp16 = one 128-byte swizzle row
 constexpr uint32_t kABytes = kBM * kBK * 2;
 constexpr int kBNB = 128;         // stage B tile width
-constexpr int kSplitRows = 2048;  // stage B rows per split (fp32 accumulation length)
+// stage B rows per split: the length of one fp32 accumulation in TMEM.  1024
+// rather than 2048 halves the spectral error of a 300-step run at M=573,
+// N=50 000 on four of five seeded ensembles (e.g. 8.97e-5 -> 4.53e-5) for 3 %
+// more run time (more partial tiles to sum).
+constexpr int kSplitRows = 1024;
 constexpr float kLoScale = 2048.f;
 constexpr float kLoInv = 1.f / 2048.f;
 constexpr long long kDefaultBudget = 4000000000LL;   // ~2 s at 2 GHz
@@ -488,6 +492,328 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc(const __grid_constant__ Tm
                             p = fmaf(gg[k], vv, p);
                             sacc = fmaf(cp[kPBN + c], dd[k], sacc);
                             tacc = fmaf(cp[2 * kPBN + c], gg[k], tacc);
+                        }
+                    }
+                    ++consumed;
+                    // every epilogue thread is done with buffer e: refill it.
+                    // The reads above are generic-proxy and the refill is a TMA
+                    // write (async proxy); the barrier alone does not order the
+                    // two, and a refill that landed before a slow warp's loads
+                    // had read the part gave wrong d values in a few rows of one
+                    // tile in about one call in 1500 (M=573, N=20 000)
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    if (leader) issue_next();
+                }
+                if (fail_code) break;
+            }
+            if (fail_code) break;
+            if (row < args.R) {
+                const long R = args.R;
+                float *o = args.qpst + ((long)jimg * nct + ct) * 4 * R;
+                o[row] = q;
+                o[R + row] = p;
+                o[2 * R + row] = sacc;
+                o[3 * R + row] = tacc;
+            }
+        }
+        if (fail_code) {
+            *abort = 1;
+            if (leader)
+                for (long k = consumed; k < issued; ++k)
+                    mbar_wait(efull0 + 8 * (int)(k & 1), (uint32_t)(k >> 1) & 1, kDefaultBudget);
+        }
+    }
+    if (fail_code && lane == 0) *(volatile int *)args.err = fail_code;
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 5) {
+        // every MMA has completed before the TMEM is freed
+        mbar_wait(done, 0, kDefaultBudget);
+        __syncwarp();
+        tc_fence_after();
+        tmem_dealloc<512>(tmem);
+    }
+}
+
+// ------------------------------ stage A with one accumulator per tile
+// The same product as k_stageA_tc (tiles of V = D [Y1_0 ... Y1_{J-1}], fused
+// row dots) with 128 x 192 tiles, so that a whole 189-mode image or a third
+// of 573 modes is one N=192 MMA.  The hi*lo + lo*hi products of a tile are
+// accumulated first over the whole K range; the first hi*hi MMA then scales
+// the accumulator by 2^-11 on the way in (tcgen05.mma's scale-input-d), and
+// the rest of the hi*hi products follow, so D = sum hi*hi + 2^-11 sum
+// (hi*lo + lo*hi) sits in one fp32 accumulator (192 TMEM columns) and two
+// tiles' accumulators fit in the 512 columns (double buffering).  The
+// operands pass through the ring twice per tile (the hi limbs twice), in
+// 40 KB slots: [A limb 128 x 64 | B limb 192 x 64].
+constexpr int kRBN = 192;
+constexpr int kRSlots = 4;
+constexpr uint32_t kRLimbA = kBM * kBK * 2;                  // 16 KB
+constexpr uint32_t kRSlotBytes = kRLimbA + kRBN * kBK * 2;   // 40 KB
+constexpr int kRBars = 2 * kRSlots + 7;
+constexpr size_t kRSmem = 1024 + kRSlots * (size_t)kRSlotBytes + 2 * (size_t)kPEpiBytes +
+                          3 * kRBN * sizeof(float) + 8 * kRBars + 16;
+static_assert(kRSmem <= 232448, "stage A (one accumulator) shared memory above the limit");
+
+__device__ __forceinline__ void mma_f16_scaled11(uint32_t tmem, uint64_t a, uint64_t b,
+                                                 uint32_t idesc) {
+    // D = A B + D 2^-11
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, 1, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p, 11;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ TmaQuad tm,
+                                                       const __grid_constant__ TmaEpi te,
+                                                       const StageAArgs args) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *epi = smem + kRSlots * kRSlotBytes;
+    float *colv = reinterpret_cast<float *>(epi + 2 * kPEpiBytes);   // [3][kRBN]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(colv + 3 * kRBN);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kRBars);
+    volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * kRSlots,
+                   tfull0 = empty0 + 8 * kRSlots, tempty0 = tfull0 + 16, efull0 = tempty0 + 16,
+                   done = efull0 + 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long budget = args.budget;
+    const long G = gridDim.x;
+    // this CTA's tiles: [t0, t0 + nloc), an even split of the tile sequence
+    const long t0 = args.ntiles * blockIdx.x / G;
+    const long nloc = args.ntiles * (blockIdx.x + 1) / G - t0;
+    const int nct = args.nct, Mp = args.Mp;
+    const long jn = (long)args.J * nct;   // tiles per row block: images x column tiles
+    const uint32_t b_bytes = (uint32_t)args.b_box * kBK * 2;
+    const int nkb = args.nkb;
+    const int slots_per_tile = 3 * nkb;   // cross pass: 2 slots per K block, hi pass: 1
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kRSlots; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int j = 0; j < 2; ++j) {
+            mbar_init(tfull0 + 8 * j, 1);
+            mbar_init(tempty0 + 8 * j, 128);
+            mbar_init(efull0 + 8 * j, 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 5) tmem_alloc<512>(smem_u32(tmem_slot));
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    // barriers and TMEM are set up; global memory only after the kernels
+    // before this one in the stream have completed
+    pdl_enter();
+    int fail_code = 0;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            // ---- TMA producer: per tile the cross pass (slot pairs (A hi, B lo),
+            // (A lo, B hi) per K block), then the hi pass ((A hi, B hi) per K block)
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long t = t0 + i;
+                const long rem = t % jn;
+                int arow = (int)(t / jn) * kBM;
+                int brow = (int)(rem / nct) * Mp + (int)(rem % nct) * kRBN;   // row of Y1_j
+                for (int q = 0; q < slots_per_tile; ++q, ++g) {
+                    const bool cross = q < 2 * nkb;
+                    const int kb = cross ? q >> 1 : q - 2 * nkb;
+                    const bool second = cross && (q & 1);
+                    int s = (int)(g % kRSlots);
+                    uint32_t n = (uint32_t)(g / kRSlots);
+                    if (g >= kRSlots && !mbar_wait_ab(empty0 + 8 * s, (n & 1) ^ 1, budget, abort)) {
+                        fail_code = 1;
+                        break;
+                    }
+                    uint32_t base = smem_u32(smem + s * kRSlotBytes);
+                    uint32_t bar = full0 + 8 * s;
+                    int kx = kb * kBK;
+                    mbar_expect_tx(bar, kRLimbA + b_bytes);
+                    tma_load_2d(base, second ? &tm.a_lo : &tm.a_hi, bar, kx, arow);
+                    tma_load_2d(base + kRLimbA, (cross && !second) ? &tm.b_lo : &tm.b_hi, bar, kx,
+                                brow);
+                }
+            }
+            if (fail_code) {
+                *abort = 1;
+                // every issued slot must land before the CTA exits
+                for (long gg = g > kRSlots ? g - kRSlots : 0; gg < g; ++gg)
+                    mbar_wait(full0 + 8 * (int)(gg % kRSlots), (uint32_t)(gg / kRSlots) & 1,
+                              kDefaultBudget);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // ---- MMA issuer: one accumulator per tile, tile i in TMEM columns
+            // 256 (i & 1): D = sum hi*lo + lo*hi over K, then D = hi*hi + D 2^-11
+            // (the scale on the first hi*hi MMA), then D += hi*hi over K
+            long g = 0;
+            for (long i = 0; i < nloc && !fail_code; ++i) {
+                long t = t0 + i;
+                int brow = (int)((t % jn) % nct) * kRBN;
+                int ncols = min(kRBN, Mp - brow);
+                const uint32_t idesc = idesc_f16(kBM, ncols);
+                int j = (int)(i & 1);
+                uint32_t u = (uint32_t)(i >> 1);
+                if (i >= 2 && !mbar_wait_ab(tempty0 + 8 * j, (u - 1) & 1, budget, abort)) {
+                    fail_code = 2;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + 256 * j;
+                for (int q = 0; q < slots_per_tile && !fail_code;) {
+                    const bool cross = q < 2 * nkb;
+                    const int nsl = cross ? 2 : 1;
+                    uint32_t base[2] = {0u, 0u};
+                    for (int h = 0; h < nsl; ++h) {
+                        int s = (int)((g + h) % kRSlots);
+                        uint32_t n = (uint32_t)((g + h) / kRSlots);
+                        if (!mbar_wait_ab(full0 + 8 * s, n & 1, budget, abort)) {
+                            fail_code = 2;
+                            break;
+                        }
+                        base[h] = smem_u32(smem + s * kRSlotBytes);
+                    }
+                    if (fail_code) break;
+                    tc_fence_after();
+                    const int kb = cross ? q >> 1 : q - 2 * nkb;
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; ++kk) {
+                        uint64_t a0 = sdesc_sw128(base[0] + kk * 32);
+                        uint64_t b0 = sdesc_sw128(base[0] + kRLimbA + kk * 32);
+                        if (cross) {
+                            uint64_t a1 = sdesc_sw128(base[1] + kk * 32);
+                            uint64_t b1 = sdesc_sw128(base[1] + kRLimbA + kk * 32);
+                            mma_f16(d, a0, b0, idesc, (kb | kk) != 0);   // hi * lo
+                            mma_f16(d, a1, b1, idesc, 1);                // lo * hi
+                        } else if ((kb | kk) == 0) {
+                            mma_f16_scaled11(d, a0, b0, idesc);          // hi * hi + D 2^-11
+                        } else {
+                            mma_f16(d, a0, b0, idesc, 1);
+                        }
+                    }
+                    for (int h = 0; h < nsl; ++h) mma_commit(empty0 + 8 * (int)((g + h) % kRSlots));
+                    g += nsl;
+                    q += nsl;
+                }
+                if (fail_code) break;
+                mma_commit(tfull0 + 8 * j);
+            }
+            if (fail_code) *abort = 1;
+            mma_commit(done);   // tracks every MMA issued, also after a failure
+        }
+    } else {
+        // ---- epilogue (warps 0-3): thread = tile row = TMEM lane
+        const int row_in = warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        const bool leader = threadIdx.x == 0;
+        // leader's cursor over the (tile, part) sequence of epilogue loads
+        long iss_i = 0, issued = 0;
+        int iss_p = 0;
+        auto issue_next = [&]() {
+            if (iss_i >= nloc) return;
+            long t = t0 + iss_i;
+            int arow = (int)(t / jn) * kBM, brow = (int)((t % jn) % nct) * kRBN;
+            int e = (int)(issued & 1);
+            uint32_t buf = smem_u32(epi + e * kPEpiBytes), bar = efull0 + 8 * e;
+            int x = brow + iss_p * kPEpiCols;
+            mbar_expect_tx(bar, kPEpiBytes);
+            tma_load_2d(buf, &te.d, bar, x, arow);
+            tma_load_2d(buf + kPEpiBox, &te.g, bar, x, arow);
+            ++issued;
+            if (++iss_p == min(kRBN, Mp - brow) / kPEpiCols) {
+                iss_p = 0;
+                ++iss_i;
+            }
+        };
+        if (leader) {
+            issue_next();
+            issue_next();
+        }
+        long consumed = 0;
+        for (long i = 0; i < nloc; ++i) {
+            long t = t0 + i;
+            const int jimg = (int)((t % jn) / nct);
+            const int ct = (int)((t % jn) % nct);
+            const int brow = ct * kRBN;
+            const long row = (long)(t / jn) * kBM + row_in;
+            const int np = min(kRBN, Mp - brow) / 32;   // 32-column TMEM chunks
+            const int j = (int)(i & 1);
+            const uint32_t u = (uint32_t)(i >> 1);
+            // column factors of this tile; the previous tile's last reads of
+            // them came before its last part barrier
+            float *cv = colv;
+            for (int cc = row_in; cc < kRBN; cc += kBM) {
+                int c = brow + cc;
+                bool in = c < Mp;
+                long cj = (long)jimg * Mp + c;
+                cv[cc] = in ? args.tcol[cj] : 0.f;
+                cv[kRBN + cc] = in ? args.vec_s[cj] : 0.f;
+                cv[2 * kRBN + cc] = in ? args.vec_t[cj] : 0.f;
+            }
+            bool ok = mbar_wait_ab(tfull0 + 8 * j, u & 1, budget, abort);
+            __syncwarp();
+            if (epi_sync_or(!ok)) {   // also publishes cv to the other warps
+                fail_code = 3;
+                break;
+            }
+            tc_fence_after();
+            float q = 0.f, p = 0.f, sacc = 0.f, tacc = 0.f;
+            for (int chunk = 0; chunk < np; ++chunk) {
+                float v[32];
+                {
+                    uint32_t raw[32];
+                    tmem_ld32(lane_base + 256 * j + chunk * 32, raw);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(raw[e]);
+                }
+                if (chunk == np - 1) {
+                    // this tile's accumulators are read: release the TMEM half
+                    tc_fence_before();
+                    mbar_arrive(tempty0 + 8 * j);
+                }
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    const int e = (int)(consumed & 1);
+                    bool landed = mbar_wait_ab(efull0 + 8 * e, (uint32_t)(consumed >> 1) & 1,
+                                               budget, abort);
+                    __syncwarp();
+                    if (epi_sync_or(!landed)) {
+                        fail_code = 3;
+                        break;
+                    }
+                    // 64-byte rows, 16-byte granule c stored at c ^ ((row >> 1) & 3)
+                    const uint8_t *bd = epi + e * kPEpiBytes + row_in * 64;
+                    const uint8_t *bg = bd + kPEpiBox;
+                    const int sw = (row_in >> 1) & 3;
+                    const float *cp = cv + chunk * 32 + half * 16;
+#pragma unroll
+                    for (int ch = 0; ch < 4; ++ch) {
+                        float4 d4 = *reinterpret_cast<const float4 *>(bd + ((ch ^ sw) << 4));
+                        float4 g4 = *reinterpret_cast<const float4 *>(bg + ((ch ^ sw) << 4));
+                        float dd[4] = {d4.x, d4.y, d4.z, d4.w}, gg[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            int c = 4 * ch + k;
+                            float vv = v[half * 16 + c] * cp[c];
+                            q = fmaf(dd[k], vv, q);
+                            p = fmaf(gg[k], vv, p);
+                            sacc = fmaf(cp[kRBN + c], dd[k], sacc);
+                            tacc = fmaf(cp[2 * kRBN + c], gg[k], tacc);
                         }
                     }
                     ++consumed;
@@ -1290,6 +1616,7 @@ struct MixedExtra {
     int nfchunk = 0;
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
     int ntBb = 0, ldGb = 0;   // stage B tiles / columns along the J x Mp rows of W^T
+    int one_acc = 0;          // stage A with one accumulator per 128 x 192 tile
     int nsm = 1;
     long long budget = kDefaultBudget;
 };
@@ -1307,8 +1634,10 @@ int mixed_prepare(tdscha_ctx *c) {
     MixedExtra *x = new MixedExtra();
     mx.tmaps = x;
     if (const char *b = getenv("TDSCHA_WAIT_BUDGET_CYCLES")) x->budget = atoll(b);
-    x->bnA = std::min(kPBN, Mp);
-    mx.nctile = ceil_div(Mp, kPBN);
+    if (const char *e = getenv("TDSCHA_STAGEA_ACC")) x->one_acc = atoi(e) == 1;
+    const int bnA = x->one_acc ? kRBN : kPBN;
+    x->bnA = std::min(bnA, Mp);
+    mx.nctile = ceil_div(Mp, bnA);
     {
         int dev = 0, nsm = 0;
         TDS_CUDA(cudaGetDevice(&dev));
@@ -1411,6 +1740,8 @@ int mixed_prepare(tdscha_ctx *c) {
     if (!attr_done) {
         TDS_CUDA(cudaFuncSetAttribute(k_stageA_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)kPSmem));
+        TDS_CUDA(cudaFuncSetAttribute(k_stageA_tc1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kRSmem));
         TDS_CUDA(cudaFuncSetAttribute(k_stageB_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)kQSmem));
         attr_done = true;
@@ -1509,7 +1840,10 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     {
         ProfScope ps(c, 0, st);
         int grid = (int)std::min<long>(ga.ntiles, x->nsm);
-        TDS_CUDA(launch_pdl(k_stageA_tc, grid, 192, kPSmem, st, x->tmA, x->te, ga));
+        if (x->one_acc)
+            TDS_CUDA(launch_pdl(k_stageA_tc1, grid, 192, kRSmem, st, x->tmA, x->te, ga));
+        else
+            TDS_CUDA(launch_pdl(k_stageA_tc, grid, 192, kPSmem, st, x->tmA, x->te, ga));
     }
     {
         ProfScope ps(c, 1, st);

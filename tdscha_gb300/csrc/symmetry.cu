@@ -70,55 +70,86 @@ __global__ void k_psi_y1(const int *__restrict__ sc_idx, const double *__restric
     }
 }
 
-// hs[j][k][l] = sum_s G_js[k][l] + G_js[l][k], G_js[k][l] = g[s*ss + j*js + k*lda + l],
-// summed in float64 in split order; fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m].
+// hs[j][k][l] = sum_s G_js[k][l] + sum_s G_js[l][k], G_js[k][l] = g[s*ss + j*js + k*lda + l],
+// each sum in float64 in split order, through a 32 x 32 shared-memory tile so
+// that both the direct and the transposed partials are read along rows.
+// Blocks of the first tile row also form fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m].
 template <typename T>
-__global__ void k_psi_hsum(const T *__restrict__ g, int nsplit, long ss, long js, long lda,
-                           const T *__restrict__ fpart, int nfc, int J, int M,
-                           double *__restrict__ hs, double *__restrict__ fs) {
-    long MM = (long)M * M, n = (long)J * MM;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        long j = e / MM;
-        int k = (int)((e - j * MM) / M), l = (int)(e % M);
-        const T *base = g + j * js;
+__global__ void __launch_bounds__(256) k_psi_hsum(const T *__restrict__ g, int nsplit, long ss,
+                                                  long js, long lda, const T *__restrict__ fpart,
+                                                  int nfc, int M, double *__restrict__ hs,
+                                                  double *__restrict__ fs) {
+    __shared__ double tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;    // 32 x 8
+    const int l0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    const long j = blockIdx.z;
+    const T *base = g + j * js;
+    // transposed part: rows l of the tile's column range, columns k
+    for (int r = ty; r < 32; r += 8) {
+        int l = l0 + r, k = k0 + tx;
         double acc = 0;
-        for (int s = 0; s < nsplit; ++s) {
-            const T *gs = base + s * ss;
-            acc += (double)gs[k * lda + l] + (double)gs[l * lda + k];
+        if (l < M && k < M)
+            for (int s = 0; s < nsplit; ++s) acc += (double)base[s * ss + (long)l * lda + k];
+        tile[r][tx] = acc;            // tile[l - l0][k - k0]
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        int k = k0 + r, l = l0 + tx;
+        if (k < M && l < M) {
+            double acc = 0;
+            for (int s = 0; s < nsplit; ++s) acc += (double)base[s * ss + (long)k * lda + l];
+            hs[(j * M + k) * M + l] = acc + tile[tx][r];
         }
-        hs[e] = acc;
-        if (k == 0) {
+    }
+    if (blockIdx.y == 0 && ty == 0) {
+        int m = l0 + tx;
+        if (m < M) {
             double f = 0;
-            for (int ch = 0; ch < nfc; ++ch) f += (double)fpart[(j * nfc + ch) * M + l];
-            fs[j * M + l] = f;
+            for (int ch = 0; ch < nfc; ++ch) f += (double)fpart[(j * nfc + ch) * M + m];
+            fs[j * M + m] = f;
         }
     }
 }
 
-// d2v[a][b] = -inv sum_j sum_{k, l} S_j[a][k] hs[j][k][l] S_j[b][l]
-// f[a]      =  inv sum_j sum_k S_j[a][k] fs[j][k]
+// Per image: tj[j][a][b] = sum_{k, l} S_j[a][k] hs[j][k][l] S_j[b][l] and
+// tf[j][a] = sum_k S_j[a][k] fs[j][k].
 __global__ void k_psi_sandwich(const int *__restrict__ sr_idx, const double *__restrict__ sr_val,
                                const double *__restrict__ hs, const double *__restrict__ fs,
-                               int J, int M, int md, double inv, double *__restrict__ f,
-                               double *__restrict__ d2v) {
-    long MM = (long)M * M;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < MM; e += (long)gridDim.x * blockDim.x) {
-        int a = (int)(e / M), b = (int)(e % M);
+                               int J, int M, int md, double *__restrict__ tj,
+                               double *__restrict__ tf) {
+    const long MM = (long)M * M, n = (long)J * MM;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const long j = e / MM;
+        const int a = (int)((e - j * MM) / M), b = (int)(e % M);
+        const int *ia = sr_idx + (j * M + a) * md, *ib = sr_idx + (j * M + b) * md;
+        const double *va = sr_val + (j * M + a) * md, *vb = sr_val + (j * M + b) * md;
+        const double *H = hs + j * MM;
         double acc = 0, facc = 0;
-        for (int j = 0; j < J; ++j) {
-            const int *ia = sr_idx + ((long)j * M + a) * md, *ib = sr_idx + ((long)j * M + b) * md;
-            const double *va = sr_val + ((long)j * M + a) * md, *vb = sr_val + ((long)j * M + b) * md;
-            const double *H = hs + (long)j * MM;
-            for (int p = 0; p < md && ia[p] >= 0; ++p) {
-                double inner = 0;
-                const double *row = H + (long)ia[p] * M;
-                for (int q = 0; q < md && ib[q] >= 0; ++q) inner = fma(vb[q], row[ib[q]], inner);
-                acc = fma(va[p], inner, acc);
-                if (b == 0) facc = fma(va[p], fs[(long)j * M + ia[p]], facc);
-            }
+        for (int p = 0; p < md && ia[p] >= 0; ++p) {
+            double inner = 0;
+            const double *row = H + (long)ia[p] * M;
+            for (int q = 0; q < md && ib[q] >= 0; ++q) inner = fma(vb[q], row[ib[q]], inner);
+            acc = fma(va[p], inner, acc);
+            if (b == 0) facc = fma(va[p], fs[j * M + ia[p]], facc);
         }
+        tj[e] = acc;
+        if (b == 0) tf[j * M + a] = facc;
+    }
+}
+
+// d2v[a][b] = -inv sum_j tj[j][a][b], f[a] = inv sum_j tf[j][a], in image order.
+__global__ void k_psi_jsum(const double *__restrict__ tj, const double *__restrict__ tf, int J,
+                           int M, double inv, double *__restrict__ f, double *__restrict__ d2v) {
+    const long MM = (long)M * M;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < MM; e += (long)gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int j = 0; j < J; ++j) acc += tj[j * MM + e];
         d2v[e] = -acc * inv;
-        if (b == 0) f[a] = facc * inv;
+        if (e < M) {
+            double fa = 0;
+            for (int j = 0; j < J; ++j) fa += tf[(long)j * M + e];
+            f[e] = fa * inv;
+        }
     }
 }
 
@@ -179,7 +210,8 @@ int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_spac
     TDS_CUDA(cudaMemcpy(c->sr_val, rv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->sc_val, cv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cached_malloc(&c->vsv, sizeof(double) * 2 * (size_t)S * M));
-    TDS_CUDA(cached_malloc(&c->hs, sizeof(double) * ((size_t)S * M * M + (size_t)S * M)));
+    // hs and tj (J x M x M each), fs and tf (J x M each)
+    TDS_CUDA(cached_malloc(&c->hs, sizeof(double) * 2 * ((size_t)S * M * M + (size_t)S * M)));
     c->J = S;
     c->maxdeg = md;
     return TDSCHA_OK;
@@ -213,17 +245,19 @@ template <typename T>
 static int psi_finalize(tdscha_ctx *c, const T *gpart, int nsplit, long sstride, long jstride,
                         long lda, const T *fpart, int nfchunk, cudaStream_t st) {
     const int M = c->M, J = c->J;
-    double *hs = c->hs, *fs = c->hs + (size_t)J * M * M;
-    {
-        ProfScope ps(c, 4, st);
-        k_psi_hsum<T><<<grid_for((long)J * M * M), 256, 0, st>>>(gpart, nsplit, sstride, jstride,
-                                                                 lda, fpart, nfchunk, J, M, hs, fs);
-        TDS_CHECK_LAUNCH();
-        k_psi_sandwich<<<grid_for((long)M * M), 256, 0, st>>>(c->sr_idx, c->sr_val, hs, fs, J, M,
-                                                             c->maxdeg, 1.0 / (c->sum_rho * c->S),
-                                                             c->f, c->d2v);
-        TDS_CHECK_LAUNCH();
-    }
+    const size_t JMM = (size_t)J * M * M, JM = (size_t)J * M;
+    double *hs = c->hs, *tj = hs + JMM, *fs = tj + JMM, *tf = fs + JM;
+    ProfScope ps(c, 4, st);
+    dim3 gt(ceil_div(M, 32), ceil_div(M, 32), J);
+    k_psi_hsum<T><<<gt, 256, 0, st>>>(gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, M, hs,
+                                      fs);
+    TDS_CHECK_LAUNCH();
+    k_psi_sandwich<<<grid_for((long)JMM), 256, 0, st>>>(c->sr_idx, c->sr_val, hs, fs, J, M,
+                                                        c->maxdeg, tj, tf);
+    TDS_CHECK_LAUNCH();
+    k_psi_jsum<<<grid_for((long)M * M), 256, 0, st>>>(tj, tf, J, M, 1.0 / (c->sum_rho * c->S),
+                                                      c->f, c->d2v);
+    TDS_CHECK_LAUNCH();
     return TDSCHA_OK;
 }
 
