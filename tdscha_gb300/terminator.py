@@ -134,11 +134,13 @@ def windows(a, b, sigma, k_min=WINDOW, window=WINDOW, horizon=HORIZON, stride=1)
 
 
 def generate_runs(n_runs, n_steps, seed=0, m_range=(48, 160), n_configs=4000, batch=20,
-                  anh_range=(0.01, 0.1), precision="mixed", verbose=False):
-    """Coefficient sequences of symmetric Wigner Lanczos runs (full
-    re-orthogonalisation) on seeded synthetic ensembles: M log-uniform in
-    m_range, N = n_configs, the cubic / quartic force scale uniform in
-    anh_range; random unit R1 start.  Returns [(a, b, sigma, M)]."""
+                  anh_range=(0.01, 0.1), precision="mixed", reorth=True, verbose=False):
+    """Coefficient sequences of symmetric Wigner Lanczos runs on seeded
+    synthetic ensembles: M log-uniform in m_range, N = n_configs, the cubic /
+    quartic force scale uniform in anh_range; random unit R1 start; full
+    re-orthogonalisation, or (reorth=False) the reference's default
+    recurrence, whose cost per step does not grow with the step index.
+    Returns [(a, b, sigma, M)]."""
     from .batch import run_batch
     from .DynamicalLanczos import Lanczos
     from .synthetic import make_ensemble, random_R1
@@ -154,7 +156,7 @@ def generate_runs(n_runs, n_steps, seed=0, m_range=(48, 160), n_configs=4000, ba
             lz = Lanczos.from_arrays(e["X"], e["Y"], e["w"], e["rho"], e["T"], use_wigner=True,
                                      precision=precision)
             lz.init(use_symmetries=False)
-            lz.full_reorth = True
+            lz.full_reorth = bool(reorth)
             lz.prepare_perturbation(random_R1(M, int(rng.integers(1 << 30))), masses_exp=0)
             runs.append(lz)
         run_batch(runs, n_steps)
@@ -265,11 +267,13 @@ def evaluate(term, runs, k, n_total, n_w=2000, w_max_cm=1100.0, smearing_cm=5.0,
     points, 5 cm^-1 smearing, square-root terminator): the first k steps with
     the standard terminator, and the first k steps extended by the network to
     n_total.  `saved_applications` is, per run, how many more steps the plain
-    method needs (on k_grid) to be as close to the full spectrum as the
-    extended k-step run (0 when it never is worse)."""
+    method needs (every step count from k on, unless k_grid says otherwise)
+    to be as close to the full spectrum as the extended k-step run (0 when it
+    never is worse)."""
     w = np.linspace(0, w_max_cm, n_w) / RY_TO_CM
     sm = smearing_cm / RY_TO_CM
-    k_grid = list(range(k, n_total + 1, 10)) if k_grid is None else k_grid
+    every = k_grid is None
+    k_grid = list(range(k, n_total + 1)) if k_grid is None else k_grid
     plain, learned, saved = [], [], []
     for a, b, sigma, _ in runs:
         g_ref = continued_fraction(a[:n_total], b[:n_total], w, sm)
@@ -281,6 +285,7 @@ def evaluate(term, runs, k, n_total, n_w=2000, w_max_cm=1100.0, smearing_cm=5.0,
         need = next((kk for kk in k_grid if errs[kk] <= el), n_total)
         saved.append(max(0, need - k))
     return {"k": k, "n_total": n_total, "runs": len(runs),
+            "step_grid": "every step" if every else "%d points" % len(k_grid),
             "plain_terminator_err_median": float(np.median(plain)),
             "learned_err_median": float(np.median(learned)),
             "plain_terminator_err_mean": float(np.mean(plain)),
@@ -294,23 +299,39 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train"])
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
-    ap.add_argument("--n-train", type=int, default=400)
+    ap.add_argument("--n-train", type=int, default=200)
     ap.add_argument("--n-test", type=int, default=20)
-    ap.add_argument("--steps", type=int, default=320)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--k", type=int, default=100)
     ap.add_argument("--iters", type=int, default=20000)
+    ap.add_argument("--m-range", type=int, nargs=2, default=(96, 384))
+    ap.add_argument("--n-configs", type=int, default=20000)
+    ap.add_argument("--train-precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--test-precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=20)
+    ap.add_argument("--reorth", action="store_true",
+                    help="full re-orthogonalisation in the generated runs (its cost grows "
+                         "with the step index; off: the reference's default recurrence)")
     ap.add_argument("--report", default=None)
     args = ap.parse_args()
     t0 = time.time()
-    train_runs = generate_runs(args.n_train, args.steps, seed=1)
-    test_runs = generate_runs(args.n_test, args.steps, seed=2)
+    gen = dict(m_range=tuple(args.m_range), n_configs=args.n_configs, batch=args.batch,
+               reorth=args.reorth)
+    train_runs = generate_runs(args.n_train, args.steps, seed=1, precision=args.train_precision,
+                               verbose=True, **gen)
+    t_tr = time.time()
+    test_runs = generate_runs(args.n_test, args.steps, seed=2, precision=args.test_precision,
+                              verbose=True, **gen)
     t1 = time.time()
     mlp, hist = train(train_runs, iters=args.iters)
     t2 = time.time()
     term = LearnedTerminator(mlp.get_params())
     rep = evaluate(term, test_runs, args.k, args.steps)
-    rep.update(train_runs=args.n_train, steps=args.steps, data_s=t1 - t0, train_s=t2 - t1,
-               loss_first=hist[0][1], loss_last=hist[-1][1], iters=args.iters)
+    rep.update(train_runs=args.n_train, steps=args.steps, data_s=t1 - t0,
+               train_data_s=t_tr - t0, train_s=t2 - t1, loss_first=hist[0][1],
+               loss_last=hist[-1][1], iters=args.iters, m_range=list(args.m_range),
+               n_configs=args.n_configs, train_precision=args.train_precision,
+               test_precision=args.test_precision, reorth=bool(args.reorth))
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     term.save(args.out, report=json.dumps(rep))
     print(json.dumps(rep))
