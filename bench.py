@@ -303,6 +303,12 @@ def run_ours(args):
                       with_mixed=(prec_name == "mixed"))
     ctx.set_options(False, False, False, False, False, 0.0)     # bi-Lanczos (normal repr.)
     n_img, rows = ctx.layout()
+    tuning = None
+    if prec_name == "mixed":
+        t_acc, t_split, t_ms = ctx.tuning()
+        tuning = {"stage_a": "one accumulator, 128x192 tiles" if t_acc else
+                  "two accumulators, 128x128 tiles", "stage_b_splits": t_split,
+                  "application_ms_at_tuning": t_ms}
     P = ctx.P
     W, K = args.warmup, args.steps
     cap = n_run + 2
@@ -465,6 +471,7 @@ def run_ours(args):
                                      "full re-biorthogonalisation against the stored basis (float64)",
                            "symmetry_images": ("applied to the perturbation (%d), ensemble rows "
                                                "resident: %d" % (n_img, rows)) if S > 1 else "none",
+                           "tuning": tuning,
                            "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (ensemble %.0f MB)" % (2 * rows * M * 8 / 1e6)},
                 "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,

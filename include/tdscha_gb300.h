@@ -197,6 +197,20 @@ int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, in
 int tdscha_ctx_layout(tdscha_ctx *ctx, int *images_on_perturbation, long long *ensemble_rows);
 
 /*
+ * The tensor-core shapes the autotuner chose for a context created with the
+ * mixed path (no counterpart in the reference).  At creation the context
+ * times one mixed application for each candidate -- stage A with two
+ * accumulators on 128 x 128 tiles or one accumulator on 128 x 192 tiles,
+ * stage B split counts whose fp32 accumulations stay within about 1.1 x 1024
+ * rows -- and keeps the fastest, cached per (modes, rows, images) shape for
+ * the process.  TDSCHA_AUTOTUNE=0 keeps the rule-based shape (two
+ * accumulators, best wave fill); TDSCHA_STAGEA_ACC=0/1 fixes the stage A
+ * kernel.  *application_ms = the timed application (0 when not tuned).
+ */
+int tdscha_ctx_tuning(tdscha_ctx *ctx, int *stage_a_one_accumulator, int *stage_b_splits,
+                      double *application_ms);
+
+/*
  * Float64 perturbation averages that allocate no device memory (no
  * counterpart in the reference).  For callers that cannot let a library call
  * cudaMalloc: host programs that reserve the GPU's memory for their own pool

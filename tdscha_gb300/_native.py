@@ -30,7 +30,7 @@ EXPORTS = [
     "tdscha_lanczos_run_batch", "tdscha_mlp_create", "tdscha_mlp_destroy",
     "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
     "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
-    "tdscha_release_cached_memory", "tdscha_ctx_layout",
+    "tdscha_release_cached_memory", "tdscha_ctx_layout", "tdscha_ctx_tuning",
 ]
 
 
@@ -91,6 +91,7 @@ def load():
     lib.tdscha_static_L.argtypes = [_vp, _c_int, _vp, _vp, _c_int, _c_double, _c_int, _vp]
     lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
     lib.tdscha_ctx_layout.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_longlong)]
+    lib.tdscha_ctx_tuning.argtypes = [_vp, _i, _i, _d]
     lib.tdscha_release_cached_memory.argtypes = [_vp]
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
@@ -200,6 +201,13 @@ class Context:
         j, rows = ctypes.c_int(0), ctypes.c_longlong(0)
         check(load().tdscha_ctx_layout(self.handle, ctypes.byref(j), ctypes.byref(rows)))
         return j.value, rows.value
+
+    def tuning(self):
+        """(stage A one-accumulator kernel, stage B splits, tuned application ms)."""
+        a, n, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        check(load().tdscha_ctx_tuning(self.handle, ctypes.byref(a), ctypes.byref(n),
+                                       ctypes.byref(ms)))
+        return a.value, n.value, ms.value
 
     def set_options(self, use_wigner, ignore_harmonic, ignore_v3, ignore_v4, reverse_L, shift):
         opts = (int(bool(use_wigner)), int(bool(ignore_harmonic)), int(bool(ignore_v3)),

@@ -189,6 +189,9 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st);
 int perturb_mixed_psi(tdscha_ctx *c, int apply_d4, const double *psi, const double *cty,
                       const double *ctra, cudaStream_t st);
 int mixed_check_error(tdscha_ctx *c);
+// the autotuner's choice: stage A kernel (1: one accumulator per 128 x 192
+// tile), stage B split count, and the timed application (ms; 0: not tuned)
+int mixed_tuning(tdscha_ctx *c, int *one_acc, int *nsplit, double *ms);
 // lanczos.cu
 int build_pair_coeffs(tdscha_ctx *c);
 int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int transpose,

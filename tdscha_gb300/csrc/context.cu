@@ -532,6 +532,16 @@ extern "C" int tdscha_ctx_layout(tdscha_ctx *ctx, int *images_on_perturbation,
     return TDSCHA_OK;
 }
 
+extern "C" int tdscha_ctx_tuning(tdscha_ctx *ctx, int *stage_a_one_accumulator, int *stage_b_splits,
+                                 double *application_ms) {
+    set_error("");
+    if (!ctx || !stage_a_one_accumulator || !stage_b_splits || !application_ms) {
+        set_error("ctx_tuning: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    return mixed_tuning(ctx, stage_a_one_accumulator, stage_b_splits, application_ms);
+}
+
 extern "C" int tdscha_ctx_sync(tdscha_ctx *ctx, void *stream) {
     set_error("");
     if (!ctx) { set_error("ctx_sync: null context"); return TDSCHA_ERR_ARG; }

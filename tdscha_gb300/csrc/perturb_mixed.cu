@@ -36,7 +36,12 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -1606,6 +1611,7 @@ static int make_map_f32(CUtensorMap *m, const void *base, uint64_t inner, uint64
 
 struct MixedExtra {
     TmaQuad tmA, tmB;
+    TmaQuad tmA1;             // stage A operand maps for the 192-row B boxes (one accumulator)
     TmaEpi te;
     int bnA = 0;
     float *sd = nullptr, *fmx = nullptr, *su = nullptr, *sw = nullptr, *tcol = nullptr;
@@ -1617,11 +1623,106 @@ struct MixedExtra {
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
     int ntBb = 0, ldGb = 0;   // stage B tiles / columns along the J x Mp rows of W^T
     int one_acc = 0;          // stage A with one accumulator per 128 x 192 tile
+    double tuned_ms = 0;      // autotuner: time of one application with the chosen shape
+    int force_acc = -1;       // TDSCHA_STAGEA_ACC: the stage A kernel fixed by the environment
+    std::vector<int> split_cands;
     int nsm = 1;
     long long budget = kDefaultBudget;
 };
 
 static MixedExtra *extra(tdscha_ctx *c) { return reinterpret_cast<MixedExtra *>(c->mx.tmaps); }
+
+static void set_stage_a(MixedExtra *x, MixedStore &mx, int one_acc) {
+    x->one_acc = one_acc;
+    const int bn = one_acc ? kRBN : kPBN;
+    x->bnA = std::min(bn, mx.Mp);
+    mx.nctile = ceil_div(mx.Mp, bn);
+}
+
+static void set_splits(MixedExtra *x, MixedStore &mx, int n) {
+    x->kbps = ceil_div(x->nkbB, n);
+    mx.nsplit = ceil_div(x->nkbB, x->kbps);
+}
+
+// Autotuner of the tensor-core shapes.  For each new (modes, rows, images)
+// shape it times one mixed application (stage A kernel: two accumulators on
+// 128-wide tiles or one accumulator on 192-wide tiles; stage B split counts
+// within the accuracy budget, see split_cands) on the context's own operands,
+// one warm-up and three timed calls each, and keeps the fastest; the choice
+// is cached per shape for the life of the process, so contexts of one shape
+// give the same bits.  TDSCHA_AUTOTUNE=0 keeps the rule-based shape.
+static std::mutex g_tune_mu;
+struct Tuned {
+    int one_acc, nsplit;
+    double ms;
+};
+static std::map<std::array<long, 3>, Tuned> g_tuned;
+
+static int autotune(tdscha_ctx *c) {
+    MixedExtra *x = extra(c);
+    MixedStore &mx = c->mx;
+    if (const char *e = getenv("TDSCHA_AUTOTUNE"))
+        if (atoi(e) == 0) return TDSCHA_OK;
+    const std::array<long, 3> key{(long)c->M, c->Nrows, (long)c->J};
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+        if (x->force_acc < 0) set_stage_a(x, mx, it->second.one_acc);
+        set_splits(x, mx, it->second.nsplit);
+        x->tuned_ms = it->second.ms;
+        return TDSCHA_OK;
+    }
+    const int M = c->M;
+    // a fixed perturbation of typical magnitude in the per-call buffers
+    std::vector<double> r1(M), y1((size_t)M * M);
+    for (int a = 0; a < M; ++a) {
+        r1[a] = 1.0 / std::sqrt((double)M) * ((a % 3) - 1.0);
+        for (int b = 0; b < M; ++b)
+            y1[(size_t)a * M + b] = 1e-3 * std::cos(0.37 * (a + 1) * (b + 1));
+    }
+    TDS_CUDA(cudaMemcpy(c->R1, r1.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+    TDS_CUDA(cudaMemcpy(c->Y1, y1.data(), sizeof(double) * M * M, cudaMemcpyHostToDevice));
+    std::vector<int> accs;
+    if (x->force_acc >= 0) accs.push_back(x->force_acc);
+    else accs = {0, 1};
+    cudaEvent_t e0, e1;
+    TDS_CUDA(cudaEventCreate(&e0));
+    TDS_CUDA(cudaEventCreate(&e1));
+    double best = 1e300;
+    int best_acc = x->one_acc, best_n = mx.nsplit;
+    int rc = TDSCHA_OK;
+    for (int acc : accs) {
+        for (int n : x->split_cands) {
+            set_stage_a(x, mx, acc);
+            set_splits(x, mx, n);
+            rc = perturb_mixed(c, 1, 0);
+            if (rc == TDSCHA_OK && cudaEventRecord(e0, 0) != cudaSuccess) rc = TDSCHA_ERR_CUDA;
+            for (int k = 0; k < 3 && rc == TDSCHA_OK; ++k) rc = perturb_mixed(c, 1, 0);
+            float ms = 0;
+            if (rc == TDSCHA_OK && (cudaEventRecord(e1, 0) != cudaSuccess ||
+                                    cudaEventSynchronize(e1) != cudaSuccess ||
+                                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                rc = TDSCHA_ERR_CUDA;
+            if (rc == TDSCHA_OK) rc = mixed_check_error(c);
+            if (rc != TDSCHA_OK) break;
+            // a candidate replaces the current best only if more than 1 % faster
+            if (ms / 3.0 < best * 0.99) {
+                best = ms / 3.0;
+                best_acc = acc;
+                best_n = n;
+            }
+        }
+        if (rc != TDSCHA_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != TDSCHA_OK) return rc;
+    set_stage_a(x, mx, best_acc);
+    set_splits(x, mx, best_n);
+    x->tuned_ms = best;
+    g_tuned[key] = Tuned{best_acc, best_n, best};
+    return TDSCHA_OK;
+}
 
 int mixed_prepare(tdscha_ctx *c) {
     MixedStore &mx = c->mx;
@@ -1634,10 +1735,14 @@ int mixed_prepare(tdscha_ctx *c) {
     MixedExtra *x = new MixedExtra();
     mx.tmaps = x;
     if (const char *b = getenv("TDSCHA_WAIT_BUDGET_CYCLES")) x->budget = atoll(b);
-    if (const char *e = getenv("TDSCHA_STAGEA_ACC")) x->one_acc = atoi(e) == 1;
+    int force_acc = -1;
+    if (const char *e = getenv("TDSCHA_STAGEA_ACC")) force_acc = atoi(e) == 1 ? 1 : 0;
+    x->force_acc = force_acc;
+    x->one_acc = force_acc == 1;
     const int bnA = x->one_acc ? kRBN : kPBN;
     x->bnA = std::min(bnA, Mp);
     mx.nctile = ceil_div(Mp, bnA);
+    const int nct_max = ceil_div(Mp, kPBN);
     {
         int dev = 0, nsm = 0;
         TDS_CUDA(cudaGetDevice(&dev));
@@ -1671,6 +1776,28 @@ int mixed_prepare(tdscha_ctx *c) {
     }
     x->kbps = ceil_div(x->nkbB, want);
     mx.nsplit = ceil_div(x->nkbB, x->kbps);
+    // split counts the autotuner may pick: accumulations of at most ~1.1 x the
+    // split length (the accuracy budget), the best wave fills of 152 SMs
+    std::vector<int> split_cands{mx.nsplit};
+    {
+        const int tiles = x->ntB * x->ntBb;
+        const int lo = std::max(1, (int)std::ceil(0.9 * (double)ceil_div(R, split_rows)));
+        const int hi = std::min(x->nkbB, 2 * std::max(1, ceil_div(R, split_rows)));
+        std::vector<std::pair<double, int>> fills;
+        for (int n = lo; n <= hi; ++n) {
+            int kb = ceil_div(x->nkbB, n), ns = ceil_div(x->nkbB, kb);
+            if (ns != n) continue;
+            long ctas = (long)tiles * n;
+            fills.push_back({(double)ctas / (double)(ceil_div(ctas, 152) * 152L) + 1e-6 * n, n});
+        }
+        std::sort(fills.rbegin(), fills.rend());
+        for (size_t k = 0; k < fills.size() && split_cands.size() < 4; ++k)
+            if (std::find(split_cands.begin(), split_cands.end(), fills[k].second) ==
+                split_cands.end())
+                split_cands.push_back(fills[k].second);
+    }
+    x->split_cands = split_cands;
+    const int nsplit_max = *std::max_element(split_cands.begin(), split_cands.end());
     x->nfchunk = ceil_div(R, kWChunk);
     size_t rowN = (size_t)R * Mp, colN = (size_t)Mp * Rp;
     TDS_CUDA(cached_malloc(&mx.d_hi, 2 * rowN));
@@ -1685,8 +1812,8 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * (size_t)J * colN));
     TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)J * Mp * Mp));
     TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)J * Mp * Mp));
-    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * mx.nctile * (size_t)J * R));
-    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)mx.nsplit * x->ldG * x->ldGb));
+    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * nct_max * (size_t)J * R));
+    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)nsplit_max * x->ldG * x->ldGb));
     float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw};
     for (float **v : vecs) TDS_CUDA(cached_malloc(v, sizeof(float) * Mp));
     float **jvecs[] = {&x->tcol, &x->vs, &x->vt};
@@ -1728,8 +1855,11 @@ int mixed_prepare(tdscha_ctx *c) {
     }
     TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
     TDS_TRY(make_map(&x->tmA.a_lo, mx.d_lo, Mp, R, kBM));
-    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, x->bnA));
-    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, x->bnA));
+    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, std::min(kPBN, Mp)));
+    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, std::min(kPBN, Mp)));
+    x->tmA1 = x->tmA;
+    TDS_TRY(make_map(&x->tmA1.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, std::min(kRBN, Mp)));
+    TDS_TRY(make_map(&x->tmA1.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, std::min(kRBN, Mp)));
     TDS_TRY(make_map(&x->tmB.a_hi, mx.ut_hi, Rp, Mp, kBM));
     TDS_TRY(make_map(&x->tmB.a_lo, mx.ut_lo, Rp, Mp, kBM));
     TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, (uint64_t)J * Mp, kBNB));
@@ -1747,6 +1877,15 @@ int mixed_prepare(tdscha_ctx *c) {
         attr_done = true;
     }
     TDS_CUDA(cudaDeviceSynchronize());
+    return autotune(c);
+}
+
+int mixed_tuning(tdscha_ctx *c, int *one_acc, int *nsplit, double *ms) {
+    MixedExtra *x = extra(c);
+    if (!x) { set_error("ctx_tuning: context created without the mixed path"); return TDSCHA_ERR_STATE; }
+    *one_acc = x->one_acc;
+    *nsplit = c->mx.nsplit;
+    *ms = x->tuned_ms;
     return TDSCHA_OK;
 }
 
@@ -1841,7 +1980,7 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
         ProfScope ps(c, 0, st);
         int grid = (int)std::min<long>(ga.ntiles, x->nsm);
         if (x->one_acc)
-            TDS_CUDA(launch_pdl(k_stageA_tc1, grid, 192, kRSmem, st, x->tmA, x->te, ga));
+            TDS_CUDA(launch_pdl(k_stageA_tc1, grid, 192, kRSmem, st, x->tmA1, x->te, ga));
         else
             TDS_CUDA(launch_pdl(k_stageA_tc, grid, 192, kPSmem, st, x->tmA, x->te, ga));
     }

@@ -74,6 +74,23 @@ __global__ void k_psi_y1(const int *__restrict__ sc_idx, const double *__restric
 // each sum in float64 in split order, through a 32 x 32 shared-memory tile so
 // that both the direct and the transposed partials are read along rows.
 // Blocks of the first tile row also form fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m].
+// sum_s p[s * stride] in float64, in split order, eight loads in flight
+// (the sums are load-latency bound)
+template <typename T>
+__device__ __forceinline__ double split_sum(const T *__restrict__ p, int n, long stride) {
+    double acc = 0;
+    int s = 0;
+    for (; s + 8 <= n; s += 8) {
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = p[(long)(s + u) * stride];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += (double)v[u];
+    }
+    for (; s < n; ++s) acc += (double)p[(long)s * stride];
+    return acc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_psi_hsum(const T *__restrict__ g, int nsplit, long ss,
                                                   long js, long lda, const T *__restrict__ fpart,
@@ -88,26 +105,18 @@ __global__ void __launch_bounds__(256) k_psi_hsum(const T *__restrict__ g, int n
     for (int r = ty; r < 32; r += 8) {
         int l = l0 + r, k = k0 + tx;
         double acc = 0;
-        if (l < M && k < M)
-            for (int s = 0; s < nsplit; ++s) acc += (double)base[s * ss + (long)l * lda + k];
+        if (l < M && k < M) acc = split_sum(base + (long)l * lda + k, nsplit, ss);
         tile[r][tx] = acc;            // tile[l - l0][k - k0]
     }
     __syncthreads();
     for (int r = ty; r < 32; r += 8) {
         int k = k0 + r, l = l0 + tx;
-        if (k < M && l < M) {
-            double acc = 0;
-            for (int s = 0; s < nsplit; ++s) acc += (double)base[s * ss + (long)k * lda + l];
-            hs[(j * M + k) * M + l] = acc + tile[tx][r];
-        }
+        if (k < M && l < M)
+            hs[(j * M + k) * M + l] = split_sum(base + (long)k * lda + l, nsplit, ss) + tile[tx][r];
     }
     if (blockIdx.y == 0 && ty == 0) {
         int m = l0 + tx;
-        if (m < M) {
-            double f = 0;
-            for (int ch = 0; ch < nfc; ++ch) f += (double)fpart[(j * nfc + ch) * M + m];
-            fs[j * M + m] = f;
-        }
+        if (m < M) fs[j * M + m] = split_sum(fpart + j * nfc * M + m, nfc, M);
     }
 }
 
@@ -142,14 +151,8 @@ __global__ void k_psi_jsum(const double *__restrict__ tj, const double *__restri
                            int M, double inv, double *__restrict__ f, double *__restrict__ d2v) {
     const long MM = (long)M * M;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < MM; e += (long)gridDim.x * blockDim.x) {
-        double acc = 0;
-        for (int j = 0; j < J; ++j) acc += tj[j * MM + e];
-        d2v[e] = -acc * inv;
-        if (e < M) {
-            double fa = 0;
-            for (int j = 0; j < J; ++j) fa += tf[(long)j * M + e];
-            f[e] = fa * inv;
-        }
+        d2v[e] = -split_sum(tj + e, J, MM) * inv;
+        if (e < M) f[e] = split_sum(tf + e, J, (long)M) * inv;
     }
 }
 
@@ -255,8 +258,8 @@ static int psi_finalize(tdscha_ctx *c, const T *gpart, int nsplit, long sstride,
     k_psi_sandwich<<<grid_for((long)JMM), 256, 0, st>>>(c->sr_idx, c->sr_val, hs, fs, J, M,
                                                         c->maxdeg, tj, tf);
     TDS_CHECK_LAUNCH();
-    k_psi_jsum<<<grid_for((long)M * M), 256, 0, st>>>(tj, tf, J, M, 1.0 / (c->sum_rho * c->S),
-                                                      c->f, c->d2v);
+    k_psi_jsum<<<std::max(1, ceil_div((long)M * M, 64)), 64, 0, st>>>(
+        tj, tf, J, M, 1.0 / (c->sum_rho * c->S), c->f, c->d2v);
     TDS_CHECK_LAUNCH();
     return TDSCHA_OK;
 }

@@ -162,3 +162,29 @@ def test_release_cached_memory(gpu_lib):
     assert torch.cuda.mem_get_info()[0] >= free_before + got.value // 2
     nat.check(gpu_lib.tdscha_release_cached_memory(ctypes.byref(got)))
     assert got.value == 0
+
+
+def test_autotuner_choice_is_cached_and_accurate(gpu_lib):
+    """The shape autotuner picks a stage A kernel and a split count, caches
+    the choice for the shape (a second context of the same shape gives the
+    same bits), and the tuned application stays within the per-call
+    tolerance of the oracle."""
+    M, N = 189, 6000
+    ens = make_ensemble(M, N, seed=77, rho_sigma=0.1)
+    syms, spaces, bid = oracle.identity_symmetries(M)
+    R1, Y1 = random_R1(M, 78), random_sym(M, 79, scale=1e-3)
+    a = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                    with_mixed=True)
+    one_acc, splits, ms = a.tuning()
+    assert one_acc in (0, 1) and splits >= 1 and ms > 0
+    b = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                    with_mixed=True)
+    assert b.tuning() == (one_acc, splits, ms)
+    fa, da = _mixed_call(a, R1, Y1)
+    fb, db = _mixed_call(b, R1, Y1)
+    assert np.array_equal(fa, fb) and np.array_equal(da, db)
+    f_ref, d_ref = oracle.perturb_averages(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                           ens["T"], 1, syms, spaces, bid, n_threads=8)
+    assert rel(fa, f_ref) <= TOL_CALL and rel(da, d_ref) <= TOL_CALL
+    a.close()
+    b.close()
