@@ -338,6 +338,17 @@ int tdscha_qperturb_averages(tdscha_qctx *ctx, const double *R1, const double *a
 int tdscha_qapply_full_L(tdscha_qctx *ctx, const double *psi_in, double *psi_out, void *stream);
 
 /*
+ * Precision of the q-space averages (no counterpart in the reference, whose
+ * Julia kernel is float64): TDSCHA_PREC_FP64 (default) or TDSCHA_PREC_MIXED,
+ * where the row, force and d2v kernels run in fp32 on the CUDA cores over
+ * float copies of the image rows (made on the first switch; 24-bit operands,
+ * partial sums and finalisation in float64).  Applies to every later
+ * tdscha_qperturb_averages, tdscha_qapply_full_L, tdscha_qlanczos_run and
+ * tdscha_qkpm_run of the context.
+ */
+int tdscha_qctx_set_precision(tdscha_qctx *ctx, int precision);
+
+/*
  * Hermitian Lanczos (run_FT, QSpaceLanczos.py:967-1182): basis_Q, basis_P
  * distinct device buffers of capacity x (2 psi_size) doubles, rows 0..start_step
  * filled (row 0 the start vector normalised in the mask product, P = Q).

@@ -80,13 +80,15 @@ class QSpaceLanczos(Lanczos):
     # ------------------------------------------------------------------ setup
     @classmethod
     def from_arrays(cls, X_q, Y_q, w_q, rho, T, q_points=None, valid_modes_q=None, bg=None,
-                    pols_q=None, m=None, pairing="sum"):
+                    pols_q=None, m=None, pairing="sum", precision="fp64"):
         """Bloch-transformed ensemble: X_q, Y_q (n_q, N, n_bands) complex in the q
         mode basis (the arrays _bloch_transform_ensemble builds, :221-296), w_q
         (n_bands, n_q) in Ry.  q_points (n_q, 3) and bg (reciprocal vectors /
         2 pi, rows) locate partners; without bg, q_points are taken in crystal
-        coordinates."""
-        self = cls()
+        coordinates.  precision "mixed": the averages in fp32 on the CUDA
+        cores (24-bit operands, float64 partial sums), the recurrence in
+        float64."""
+        self = cls(precision=precision)
         X_q = np.ascontiguousarray(X_q, dtype=np.complex128)
         Y_q = np.ascontiguousarray(Y_q, dtype=np.complex128)
         if X_q.ndim != 3 or X_q.shape != Y_q.shape:
@@ -360,6 +362,7 @@ class QSpaceLanczos(Lanczos):
             if P != self.get_psi_size():
                 raise AssertionError("psi layout mismatch")
             self._qpert_key = pkey
+        self._qctx.set_precision(self.precision)
         return self._qctx
 
     def _invalidate(self):

@@ -31,6 +31,7 @@ EXPORTS = [
     "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
     "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
     "tdscha_release_cached_memory", "tdscha_ctx_layout", "tdscha_ctx_tuning",
+    "tdscha_qctx_set_precision",
 ]
 
 
@@ -92,6 +93,7 @@ def load():
     lib.tdscha_ctx_sync.argtypes = [_vp, _vp]
     lib.tdscha_ctx_layout.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_longlong)]
     lib.tdscha_ctx_tuning.argtypes = [_vp, _i, _i, _d]
+    lib.tdscha_qctx_set_precision.argtypes = [_vp, _c_int]
     lib.tdscha_release_cached_memory.argtypes = [_vp]
     lib.tdscha_static_hessian_expand.argtypes = [_vp, _vp, _vp, _vp]
     lib.tdscha_lanczos_run_hostbuf.argtypes = [_vp, _d, _d, _c_int, _c_int, _c_int, _c_int, _c_int,
@@ -295,6 +297,15 @@ class QContext:
         self.handle = h
         self.P = None
         self.n_pairs = None
+
+    def set_precision(self, precision):
+        """"fp64" (default) or "mixed": fp32 averages on the CUDA cores."""
+        code = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(precision)
+        if code is None:
+            raise ValueError("precision must be 'fp64' or 'mixed', got %r" % (precision,))
+        if getattr(self, "_precision", None) != code:
+            check(load().tdscha_qctx_set_precision(self.handle, code))
+            self._precision = code
 
     def set_pert(self, iq_pert, q_pair_map, ignore_harmonic=False, ignore_v3=False,
                  ignore_v4=False):

@@ -167,6 +167,12 @@ struct tdscha_qctx {
     double2 *R1 = nullptr, *alpha = nullptr, *f = nullptr, *d2v = nullptr;
     double2 *rowc = nullptr;                   // 4 per image row
     double2 *fpart = nullptr, *dpart = nullptr;
+    // mixed precision (tdscha_qctx_set_precision): float copies of the image
+    // rows and frequency factors, per-call float perturbation and row weights
+    int precision = 0;
+    float2 *Xr32 = nullptr, *Yr32 = nullptr;
+    float *fY32 = nullptr, *fpsi32 = nullptr;
+    float2 *R1_32 = nullptr, *alpha32 = nullptr, *rowc32 = nullptr;
     int nfchunk = 0, nbchunk = 0;
     // Lanczos scratch (2P doubles each)
     double *Lq = nullptr, *rk = nullptr, *sk = nullptr;

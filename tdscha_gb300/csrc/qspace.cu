@@ -48,6 +48,44 @@ __device__ __forceinline__ double2 cfma_conj(double2 a, double2 b, double2 acc) 
     return acc;
 }
 
+// The same complex helpers on float2: the mixed-precision operator does its
+// arithmetic in fp32 on the CUDA cores (see q_perturb).
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 acc) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+    return acc;
+}
+__device__ __forceinline__ float2 cfma_conj(float2 a, float2 b, float2 acc) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+    return acc;
+}
+template <typename T2> struct CReal;
+template <> struct CReal<double2> { using type = double; };
+template <> struct CReal<float2> { using type = float; };
+template <typename T2> __device__ __forceinline__ T2 czero() { T2 z; z.x = 0; z.y = 0; return z; }
+__device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+
+// float copies for the mixed-precision operator
+__global__ void k_q_to32(const double *__restrict__ a, long n, float *__restrict__ b) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        b[e] = (float)a[e];
+}
+
 // x_rot = S_j x_i for every image row, S_j in CSR (identity when n_syms == 0).
 // bad = 1 if any of the n entries of a or b is not finite
 __global__ void k_q_finite(const double *__restrict__ a, const double *__restrict__ b, long n,
@@ -127,33 +165,39 @@ inline int q_rows_per_block(int L) {
     int lw = std::min(256, ((L + 31) / 32) * 32);
     return 256 / lw;
 }
+// T2 = double2: float64 throughout (the reference's precision); T2 = float2:
+// fp32 products and per-row sums (24 significant bits), the block sums and the
+// row weights in float64, written to rowc as T2.
+template <typename T2>
 __global__ void __launch_bounds__(256, 4) k_q_rows(
-        const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
-        const double *__restrict__ fY, const double *__restrict__ fpsi,
-        const double *__restrict__ rho, const double2 *__restrict__ R1,
-        const double2 *__restrict__ alpha, const int *__restrict__ qpair,
+        const T2 *__restrict__ Xr, const T2 *__restrict__ Yr,
+        const typename CReal<T2>::type *__restrict__ fY,
+        const typename CReal<T2>::type *__restrict__ fpsi,
+        const double *__restrict__ rho, const T2 *__restrict__ R1,
+        const T2 *__restrict__ alpha, const int *__restrict__ qpair,
         const int *__restrict__ qrole, const int *__restrict__ qpartner,
         int n_q, int nb, int S, long R, int iq_pert, int apply_d4, int rpb,
-        double2 *__restrict__ rowc) {
+        T2 *__restrict__ rowc) {
+    using T = typename CReal<T2>::type;
     __shared__ double red[8][8];   // per warp: tot, bfw, wR, wRf (re, im)
     const int lw = blockDim.x / rpb;
     const int g = threadIdx.x / lw, t = threadIdx.x % lw;
     long r = (long)blockIdx.x * rpb + g;
     const bool live = r < R;
     const int L = n_q * nb;
-    double2 tot = make_double2(0, 0), bfw = make_double2(0, 0);
-    double2 wR = make_double2(0, 0), wRf = make_double2(0, 0);
+    T2 tot = czero<T2>(), bfw = czero<T2>();
+    T2 wR = czero<T2>(), wRf = czero<T2>();
     if (live) {
-        const double2 *x = Xr + r * L, *y = Yr + r * L;
+        const T2 *x = Xr + r * L, *y = Yr + r * L;
         for (int a = t; a < L; a += lw) {
             int q = a / nb, nu = a - q * nb;
             int p = qpair[q], role = qrole[q], q2 = qpartner[q];
-            const double2 *blk = alpha + (long)p * nb * nb;
-            const double2 *xp = x + q2 * nb;
-            double2 u = make_double2(0, 0), u2 = make_double2(0, 0);
+            const T2 *blk = alpha + (long)p * nb * nb;
+            const T2 *xp = x + q2 * nb;
+            T2 u = czero<T2>(), u2 = czero<T2>();
             // role 0: alpha[nu][k]; role 1: conj(alpha[k][nu])
             if (role == 0) {
-                const double2 *ar = blk + nu * nb;
+                const T2 *ar = blk + nu * nb;
                 int k = 0;
                 for (; k + 1 < nb; k += 2) {
                     u = cfma(ar[k], xp[k], u);
@@ -178,7 +222,7 @@ __global__ void __launch_bounds__(256, 4) k_q_rows(
             wRf = cadd(wRf, cmulc(y[a], R1[nu]));                   // conj(R1) y
         }
     }
-    double v[8] = {tot.x, tot.y, bfw.x, bfw.y, wR.x, wR.y, wRf.x, wRf.y};
+    T v[8] = {tot.x, tot.y, bfw.x, bfw.y, wR.x, wR.y, wRf.x, wRf.y};
 #pragma unroll
     for (int k = 0; k < 8; ++k)
 #pragma unroll
@@ -196,39 +240,47 @@ __global__ void __launch_bounds__(256, 4) k_q_rows(
             s[k] = 0;
             for (int w = 0; w < nw; ++w) s[k] += red[w0 + w][k];
         }
-        tot = make_double2(s[0], s[1]);
-        bfw = make_double2(s[2], s[3]);
-        wR = make_double2(s[4], s[5]);
-        wRf = make_double2(s[6], s[7]);
+        double2 dtot = make_double2(s[0], s[1]);
+        double2 dbfw = make_double2(s[2], s[3]);
+        double2 dwR = make_double2(s[4], s[5]);
+        double2 dwRf = make_double2(s[6], s[7]);
         double rw = rho[r / S];
         double d4 = apply_d4 ? 1.0 : 0.0;
-        rowc[4 * r + 0] = cscale(tot, -0.5 * rw / 3.0);
-        rowc[4 * r + 1] = cscale(bfw, -rw / 3.0);
-        rowc[4 * r + 2] = cadd(cscale(wR, rw / 3.0), cscale(tot, -d4 * rw / 8.0));
-        rowc[4 * r + 3] = cadd(cscale(wRf, rw / 3.0), cscale(bfw, -d4 * rw / 4.0));
+        double2 w[4] = {cscale(dtot, -0.5 * rw / 3.0), cscale(dbfw, -rw / 3.0),
+                        cadd(cscale(dwR, rw / 3.0), cscale(dtot, -d4 * rw / 8.0)),
+                        cadd(cscale(dwRf, rw / 3.0), cscale(dbfw, -d4 * rw / 4.0))};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            rowc[4 * r + k].x = (T)w[k].x;
+            rowc[4 * r + k].y = (T)w[k].y;
+        }
     }
 }
 
 // f partials: fpart[chunk][nu] = sum_r w1 y[q_pert][nu] + w2 f_Y x[q_pert][nu]
-__global__ void k_q_favg(const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
-                         const double *__restrict__ fY, const double2 *__restrict__ rowc, int L,
-                         int nb, int iq_pert, long R, long chunk, double2 *__restrict__ fpart) {
+template <typename T2>
+__global__ void k_q_favg(const T2 *__restrict__ Xr, const T2 *__restrict__ Yr,
+                         const typename CReal<T2>::type *__restrict__ fY,
+                         const T2 *__restrict__ rowc, int L, int nb, int iq_pert, long R,
+                         long chunk, double2 *__restrict__ fpart) {
+    using T = typename CReal<T2>::type;
     __shared__ double sh[2][32];
     int nu = blockIdx.x;
     long rb = (long)blockIdx.y * chunk, re = min(R, rb + chunk);
     int a = iq_pert * nb + nu;
-    double fy = fY[a];
-    double2 acc = make_double2(0, 0);
+    T fy = fY[a];
+    T2 acc = czero<T2>();
     for (long r = rb + threadIdx.x; r < re; r += blockDim.x) {
         acc = cadd(acc, cmul(rowc[4 * r], Yr[r * L + a]));
         acc = cadd(acc, cmul(rowc[4 * r + 1], cscale(Xr[r * L + a], fy)));
     }
+    double2 dacc = to_d2(acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        dacc.x += __shfl_xor_sync(0xffffffffu, dacc.x, o);
+        dacc.y += __shfl_xor_sync(0xffffffffu, dacc.y, o);
     }
-    if ((threadIdx.x & 31) == 0) { sh[0][threadIdx.x >> 5] = acc.x; sh[1][threadIdx.x >> 5] = acc.y; }
+    if ((threadIdx.x & 31) == 0) { sh[0][threadIdx.x >> 5] = dacc.x; sh[1][threadIdx.x >> 5] = dacc.y; }
     __syncthreads();
     if (threadIdx.x == 0) {
         double2 s = make_double2(0, 0);
@@ -248,11 +300,13 @@ inline int q_d2v_threads(int nb) {
     int nbb = nb * nb;
     return nbb <= 128 ? 256 : ((nbb + 31) / 32) * 32;
 }
-__global__ void k_q_d2v(const double2 *__restrict__ Xr, const double2 *__restrict__ Yr,
-                        const double *__restrict__ fY, const double2 *__restrict__ rowc,
-                        const int *__restrict__ pair_q, int L, int nb, long R, long chunk,
-                        int n_pairs, double2 *__restrict__ dpart) {
-    extern __shared__ double2 sm[];   // kQRows x 4 nb, reused for the phase sum
+template <typename T2>
+__global__ void k_q_d2v(const T2 *__restrict__ Xr, const T2 *__restrict__ Yr,
+                        const typename CReal<T2>::type *__restrict__ fY,
+                        const T2 *__restrict__ rowc, const int *__restrict__ pair_q, int L, int nb,
+                        long R, long chunk, int n_pairs, double2 *__restrict__ dpart) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T2 *sm = reinterpret_cast<T2 *>(sm_raw);   // kQRows x 4 nb, reused for the phase sum
     const int p = blockIdx.x;
     const int q1 = pair_q[2 * p], q2 = pair_q[2 * p + 1];
     const int stride = 4 * nb;
@@ -263,25 +317,25 @@ __global__ void k_q_d2v(const double2 *__restrict__ Xr, const double2 *__restric
     const int i = e / nb, j = e % nb;
     long rb = (long)blockIdx.y * chunk, re = min(R, rb + chunk);
     // two accumulators (the A1 and A2 products) to shorten the FMA chains
-    double2 acc = make_double2(0, 0), acc2 = make_double2(0, 0);
+    T2 acc = czero<T2>(), acc2 = czero<T2>();
     for (long r0 = rb; r0 < re; r0 += kQRows) {
         int nr = (int)min((long)kQRows, re - r0);
         __syncthreads();
         for (int t = threadIdx.x; t < nr * 2 * nb; t += blockDim.x) {
             int rr = t / (2 * nb), c = t % (2 * nb);
             long r = r0 + rr;
-            double2 *s = sm + rr * stride;
+            T2 *s = sm + rr * stride;
             if (c < nb) {
-                double2 x1 = Xr[r * L + q1 * nb + c], f1 = Yr[r * L + q1 * nb + c];
-                double2 u1 = cscale(x1, fY[q1 * nb + c]);
-                double2 wc = rowc[4 * r + 2], wd = rowc[4 * r + 3];
-                double2 a1 = cmul(wc, u1);
-                double2 a2 = cadd(cmul(wc, f1), cmul(wd, u1));
-                s[c] = make_double2(-a1.x, -a1.y);
-                s[nb + c] = make_double2(-a2.x, -a2.y);
+                T2 x1 = Xr[r * L + q1 * nb + c], f1 = Yr[r * L + q1 * nb + c];
+                T2 u1 = cscale(x1, fY[q1 * nb + c]);
+                T2 wc = rowc[4 * r + 2], wd = rowc[4 * r + 3];
+                T2 a1 = cmul(wc, u1);
+                T2 a2 = cadd(cmul(wc, f1), cmul(wd, u1));
+                s[c] = cscale(a1, -1);
+                s[nb + c] = cscale(a2, -1);
             } else {
                 int cc = c - nb;
-                double2 x2 = Xr[r * L + q2 * nb + cc], f2 = Yr[r * L + q2 * nb + cc];
+                T2 x2 = Xr[r * L + q2 * nb + cc], f2 = Yr[r * L + q2 * nb + cc];
                 s[2 * nb + cc] = cconj(f2);
                 s[3 * nb + cc] = cconj(cscale(x2, fY[q2 * nb + cc]));
             }
@@ -289,23 +343,24 @@ __global__ void k_q_d2v(const double2 *__restrict__ Xr, const double2 *__restric
         __syncthreads();
         if (active) {
             for (int rr = ph; rr < nr; rr += nph) {
-                const double2 *s = sm + rr * stride;
-                double2 a1 = s[i], a2 = s[nb + i], cf = s[2 * nb + j], cu = s[3 * nb + j];
+                const T2 *s = sm + rr * stride;
+                T2 a1 = s[i], a2 = s[nb + i], cf = s[2 * nb + j], cu = s[3 * nb + j];
                 acc = cfma(a1, cf, acc);
                 acc2 = cfma(a2, cu, acc2);
             }
         }
     }
-    acc = cadd(acc, acc2);
+    double2 dacc = cadd(to_d2(acc), to_d2(acc2));
     __syncthreads();
+    double2 *smd = reinterpret_cast<double2 *>(sm_raw);
     if (nph > 1) {
-        if (active) sm[threadIdx.x] = acc;
+        if (active) smd[threadIdx.x] = dacc;
         __syncthreads();
         if (ph == 0 && active) {
-            for (int k = 1; k < nph; ++k) acc = cadd(acc, sm[k * nbb + e]);
+            for (int k = 1; k < nph; ++k) dacc = cadd(dacc, smd[k * nbb + e]);
         }
     }
-    if (ph == 0 && active) dpart[((long)blockIdx.y * n_pairs + p) * nbb + e] = acc;
+    if (ph == 0 && active) dpart[((long)blockIdx.y * n_pairs + p) * nbb + e] = dacc;
 }
 
 __global__ void k_q_finalize(const double2 *__restrict__ fpart, int nfchunk,
@@ -453,6 +508,9 @@ static int q_build_layout(tdscha_qctx *c, const int *q_pair_map) {
     for (double2 **b : bufs2)
         if (*b) { cudaFree(*b); *b = nullptr; }
     TDS_CUDA(cudaMalloc(&c->alpha, sizeof(double2) * (size_t)n_pairs * nb * nb));
+    if (c->alpha32) { cudaFree(c->alpha32); c->alpha32 = nullptr; }
+    if (c->precision == TDSCHA_PREC_MIXED)
+        TDS_CUDA(cudaMalloc(&c->alpha32, sizeof(float2) * (size_t)n_pairs * nb * nb));
     TDS_CUDA(cudaMalloc(&c->d2v, sizeof(double2) * (size_t)n_pairs * nb * nb));
     // d2v split over configurations: about four waves of eight blocks per SM
     // over all pairs (a short last wave), at least 64 image rows per block
@@ -472,25 +530,33 @@ static int q_build_layout(tdscha_qctx *c, const int *q_pair_map) {
 
 namespace tdscha {
 
-// perturbation averages into c->f, c->d2v from c->R1, c->alpha
-static int q_perturb(tdscha_qctx *c, int apply_d4, cudaStream_t st) {
+// perturbation averages into c->f, c->d2v from c->R1, c->alpha.  Float64, or
+// with precision mixed the row, force and d2v kernels in fp32 on the CUDA
+// cores over float copies of the image rows (their partial sums and the
+// finalisation stay float64).  The q-pair blocks are n_b x n_b with K = N*S:
+// a 128-row tensor-core tile would compute mostly unused blocks (the row
+// products are block diagonal with K = n_b), while GB300's fp32 pipe runs at
+// about 64 times its float64 rate.
+template <typename T2>
+static int q_perturb_t(tdscha_qctx *c, int apply_d4, const T2 *Xr, const T2 *Yr,
+                       const typename CReal<T2>::type *fY, const typename CReal<T2>::type *fpsi,
+                       const T2 *R1, const T2 *alpha, T2 *rowc, cudaStream_t st) {
     const int nb = c->nb, L = c->L;
     const long R = c->R;
     const int rpb = q_rows_per_block(L);
-    k_q_rows<<<ceil_div(R, rpb), 256, 0, st>>>(c->Xr, c->Yr, c->fY, c->fpsi, c->rho, c->R1,
-                                                c->alpha, c->qpair, c->qrole, c->qpartner, c->n_q,
-                                                nb, c->S, R, c->iq_pert, apply_d4, rpb, c->rowc);
+    k_q_rows<T2><<<ceil_div(R, rpb), 256, 0, st>>>(Xr, Yr, fY, fpsi, c->rho, R1, alpha, c->qpair,
+                                                    c->qrole, c->qpartner, c->n_q, nb, c->S, R,
+                                                    c->iq_pert, apply_d4, rpb, rowc);
     TDS_CHECK_LAUNCH();
     long fchunk = (R + c->nfchunk - 1) / c->nfchunk;
-    k_q_favg<<<dim3(nb, c->nfchunk), 256, 0, st>>>(c->Xr, c->Yr, c->fY, c->rowc, L, nb, c->iq_pert,
-                                                   R, fchunk, c->fpart);
+    k_q_favg<T2><<<dim3(nb, c->nfchunk), 256, 0, st>>>(Xr, Yr, fY, rowc, L, nb, c->iq_pert, R,
+                                                       fchunk, c->fpart);
     TDS_CHECK_LAUNCH();
     long bchunk = (R + c->nbchunk - 1) / c->nbchunk;
     const int dthreads = q_d2v_threads(nb);
     size_t smem = sizeof(double2) * std::max(kQRows * 4 * nb, dthreads);
-    k_q_d2v<<<dim3(c->n_pairs, c->nbchunk), dthreads, smem, st>>>(c->Xr, c->Yr, c->fY, c->rowc,
-                                                              c->pair_q, L, nb, R, bchunk,
-                                                              c->n_pairs, c->dpart);
+    k_q_d2v<T2><<<dim3(c->n_pairs, c->nbchunk), dthreads, smem, st>>>(
+        Xr, Yr, fY, rowc, c->pair_q, L, nb, R, bchunk, c->n_pairs, c->dpart);
     TDS_CHECK_LAUNCH();
     long n = (long)c->n_pairs * nb * nb;
     k_q_finalize<<<std::max(1, std::min(ceil_div(n, 256), 1024)), 256, 0, st>>>(
@@ -498,6 +564,21 @@ static int q_perturb(tdscha_qctx *c, int apply_d4, cudaStream_t st) {
         c->f, c->d2v);
     TDS_CHECK_LAUNCH();
     return TDSCHA_OK;
+}
+
+static int q_perturb(tdscha_qctx *c, int apply_d4, cudaStream_t st) {
+    if (c->precision != TDSCHA_PREC_MIXED)
+        return q_perturb_t<double2>(c, apply_d4, c->Xr, c->Yr, c->fY, c->fpsi, c->R1, c->alpha,
+                                    c->rowc, st);
+    const long na = 2L * c->n_pairs * c->nb * c->nb, nr = 2L * c->nb;
+    k_q_to32<<<std::max(1, std::min(ceil_div(na, 256), 256)), 256, 0, st>>>(
+        reinterpret_cast<const double *>(c->alpha), na, reinterpret_cast<float *>(c->alpha32));
+    TDS_CHECK_LAUNCH();
+    k_q_to32<<<1, 64, 0, st>>>(reinterpret_cast<const double *>(c->R1), nr,
+                               reinterpret_cast<float *>(c->R1_32));
+    TDS_CHECK_LAUNCH();
+    return q_perturb_t<float2>(c, apply_d4, c->Xr32, c->Yr32, c->fY32, c->fpsi32, c->R1_32,
+                               c->alpha32, c->rowc32, st);
 }
 
 int q_apply_full_L_dev(tdscha_qctx *c, const double *psi_in, double *psi_out, cudaStream_t st) {
@@ -524,7 +605,8 @@ static void q_free(tdscha_qctx *c) {
     void *bufs[] = {c->Xr, c->Yr, c->fY, c->fpsi, c->rho, c->qpair, c->qrole, c->qpartner,
                     c->pair_q, c->elem, c->pcoef, c->mask, c->q_off, c->wpert, c->R1, c->alpha,
                     c->f, c->d2v, c->rowc, c->fpart, c->dpart, c->Lq, c->rk, c->sk, c->dots,
-                    c->scal, c->hist_dev, c->stat_dev, c->pqn, c->rcoef};
+                    c->scal, c->hist_dev, c->stat_dev, c->pqn, c->rcoef, c->Xr32, c->Yr32,
+                    c->fY32, c->fpsi32, c->R1_32, c->alpha32, c->rowc32};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (c->stat_host) cudaFreeHost(c->stat_host);
@@ -698,4 +780,36 @@ extern "C" int tdscha_qapply_full_L(tdscha_qctx *ctx, const double *psi_in, doub
     if (!ctx || !psi_in || !psi_out || psi_in == psi_out) { set_error("qapply_full_L: bad pointers"); return TDSCHA_ERR_ARG; }
     if (ctx->n_pairs == 0) { set_error("qapply_full_L: call tdscha_qctx_set_pert first"); return TDSCHA_ERR_STATE; }
     return q_apply_full_L_dev(ctx, psi_in, psi_out, (cudaStream_t)stream);
+}
+
+extern "C" int tdscha_qctx_set_precision(tdscha_qctx *ctx, int precision) {
+    set_error("");
+    if (!ctx) { set_error("qctx_set_precision: null context"); return TDSCHA_ERR_ARG; }
+    if (precision != TDSCHA_PREC_FP64 && precision != TDSCHA_PREC_MIXED) {
+        set_error("qctx_set_precision: unknown precision %d", precision);
+        return TDSCHA_ERR_ARG;
+    }
+    if (precision == TDSCHA_PREC_MIXED && !ctx->Xr32) {
+        const long n = ctx->R * (long)ctx->L * 2, nm = (long)ctx->L;
+        TDS_CUDA(cudaMalloc(&ctx->Xr32, sizeof(float) * n));
+        TDS_CUDA(cudaMalloc(&ctx->Yr32, sizeof(float) * n));
+        TDS_CUDA(cudaMalloc(&ctx->fY32, sizeof(float) * nm));
+        TDS_CUDA(cudaMalloc(&ctx->fpsi32, sizeof(float) * nm));
+        TDS_CUDA(cudaMalloc(&ctx->R1_32, sizeof(float2) * (size_t)ctx->nb));
+        TDS_CUDA(cudaMalloc(&ctx->rowc32, sizeof(float2) * 4 * (size_t)ctx->R));
+        const int g = (int)std::min<long>(ceil_div(n, 256), 152L * 16);
+        k_q_to32<<<g, 256>>>(reinterpret_cast<const double *>(ctx->Xr), n,
+                             reinterpret_cast<float *>(ctx->Xr32));
+        k_q_to32<<<g, 256>>>(reinterpret_cast<const double *>(ctx->Yr), n,
+                             reinterpret_cast<float *>(ctx->Yr32));
+        k_q_to32<<<ceil_div(nm, 256), 256>>>(ctx->fY, nm, ctx->fY32);
+        k_q_to32<<<ceil_div(nm, 256), 256>>>(ctx->fpsi, nm, ctx->fpsi32);
+        TDS_CUDA(cudaGetLastError());
+        TDS_CUDA(cudaDeviceSynchronize());
+    }
+    if (precision == TDSCHA_PREC_MIXED && ctx->n_pairs > 0 && !ctx->alpha32)
+        TDS_CUDA(cudaMalloc(&ctx->alpha32, sizeof(float2) * (size_t)ctx->n_pairs * ctx->nb *
+                                               ctx->nb));
+    ctx->precision = precision;
+    return TDSCHA_OK;
 }

@@ -170,3 +170,50 @@ def test_qspace_errors(gpu_lib):
     ctx = lz._qcontext()
     with pytest.raises(nat.TdschaError):
         ctx.set_pert(0, np.array([1, 2, 0]))   # not an involution
+
+
+# mixed precision: fp32 averages on the CUDA cores (24-bit operands), float64
+# partial sums; the same per-call bar as the tensor-core real-space path
+TOL_MIXED = 2e-5
+
+
+@pytest.mark.parametrize("dims,nb,N,pairing,iq,syms", CASES + [((4, 4, 4), 6, 400, "sum", 5,
+                                                                 False)])
+def test_perturb_averages_q_mixed(gpu_lib, dims, nb, N, pairing, iq, syms):
+    e, lz, o = _setup(dims, nb, N, pairing, iq, syms)
+    lz.precision = "mixed"
+    rng = np.random.default_rng(13)
+    R1 = rng.standard_normal(nb) + 1j * rng.standard_normal(nb)
+    blocks = [rng.standard_normal((nb, nb)) + 1j * rng.standard_normal((nb, nb))
+              for _ in lz.unique_pairs]
+    scale_d = None
+    for d4 in (True, False):
+        f, d2v = lz.get_perturb_averages_q(R1, blocks, d4)
+        fo, do = oq.perturb_averages_qspace(e["X_q"], e["Y_q"], e["w_q"], e["rho"], R1, blocks,
+                                            e["T"], d4, iq, o.pairs, o.symmetries, o.valid)
+        scale_d = max(np.abs(b).max() for b in do)
+        assert np.abs(f - fo).max() / max(np.abs(fo).max(), 1e-300) < TOL_MIXED
+        assert max(np.abs(a - b).max() for a, b in zip(d2v, do)) / scale_d < TOL_MIXED
+        f2, d22 = lz.get_perturb_averages_q(R1, blocks, d4)      # deterministic
+        assert np.array_equal(f, f2) and all(np.array_equal(a, b) for a, b in zip(d2v, d22))
+
+
+def test_qlanczos_mixed_spectral_error(gpu_lib):
+    """Hermitian q-space Lanczos with Gram-Schmidt, 60 steps on a 4x4x4 grid:
+    the fp32 averages against float64 within the spectral bar of the mixed
+    path (1e-4 relative)."""
+    from tdscha_gb300.synthetic import RY_TO_CM
+    e = make_qspace_ensemble((4, 4, 4), 6, 2000, seed=9, T=250.0, dispersion=0.3, rho_sigma=0.2)
+    w = np.linspace(0, 1200, 2000) / RY_TO_CM
+    spec = {}
+    for prec in ("fp64", "mixed"):
+        lz = QSpaceLanczos.from_arrays(e["X_q"], e["Y_q"], e["w_q"], e["rho"], e["T"],
+                                       q_points=e["q"], precision=prec)
+        lz.init(use_symmetries=False)
+        lz.prepare_mode_q(3, 2)
+        lz.run_FT(60, verbose=False)
+        spec[prec] = -lz.get_green_function_continued_fraction(w, smearing=5 / RY_TO_CM).imag
+        lz._invalidate()
+    err = np.abs(spec["mixed"] - spec["fp64"]).max() / np.abs(spec["fp64"]).max()
+    print("q-space mixed spectral error %.2e" % err)
+    assert err <= 1e-4
