@@ -655,8 +655,8 @@ def batch_leg(n_steps=150, seed=31, n_real=36, n_q=28):
     [48, 384], N uniform in [2000, 40000]) from one of 3 IR / 6 Raman start
     vectors in turn, mixed precision with re-orthogonalisation; and n_q
     q-space runs at distinct q-points of a 4x4x4 grid (four 6-band ensembles
-    of 5000 configurations, seven q-points each, float64 Hermitian Lanczos
-    with Gram-Schmidt)."""
+    of 5000 configurations, seven q-points each, Hermitian Lanczos with
+    Gram-Schmidt, fp32 averages)."""
     import torch
     from tdscha_gb300.batch import run_batch
     from tdscha_gb300.DynamicalLanczos import Lanczos
@@ -686,7 +686,7 @@ def batch_leg(n_steps=150, seed=31, n_real=36, n_q=28):
         for k, iq in qpts:
             e = qens[k]
             ql = QSpaceLanczos.from_arrays(e["X_q"], e["Y_q"], e["w_q"], e["rho"], e["T"],
-                                           q_points=e["q"])
+                                           q_points=e["q"], precision="mixed")
             ql.init(use_symmetries=False)
             ql.prepare_mode_q(iq, 2)
             runs.append(ql)
@@ -808,6 +808,31 @@ def qspace_leg(qname, K, W, dev, peaks, with_cpu=True):
                           "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
                           "flops_per_application": flops},
              "ensemble_bytes": 2 * e["X_q"].nbytes}
+    # the same operator with fp32 averages on the CUDA cores (precision mixed)
+    lz.precision = "mixed"
+    ctx = lz._qcontext()
+    for _ in range(3):
+        nat.check(lib.tdscha_qapply_full_L(ctx.handle, psi.data_ptr(), out.data_ptr(), st))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        nat.check(lib.tdscha_qapply_full_L(ctx.handle, psi.data_ptr(), out.data_ptr(), st))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    app32 = e0.elapsed_time(e1) / 1e3 / reps
+    lz.reset_q()
+    lz.prepare_mode_q(0, nb // 2)
+    lz.run_FT(W, verbose=False)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    lz.run_FT(K, verbose=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out_d["mixed"] = {"application_ms": app32 * 1e3,
+                      "lanczos_steps_per_s": K / (e0.elapsed_time(e1) / 1e3),
+                      "achieved_tflops": flops / app32 / 1e12,
+                      "what": "fp32 averages on the CUDA cores, float64 partial sums"}
+    lz.precision = "fp64"
     # kernel polynomial method on the same operator: two moments per application
     from tdscha_gb300.QSpaceKPM import QSpaceKPM
     kpm = QSpaceKPM.from_qspace_lanczos(lz)
