@@ -1688,6 +1688,9 @@ static int autotune(tdscha_ctx *c) {
     cudaEvent_t e0, e1;
     TDS_CUDA(cudaEventCreate(&e0));
     TDS_CUDA(cudaEventCreate(&e1));
+    // the candidates run with the default wait budget whatever the context's own
+    const long long budget = x->budget;
+    x->budget = kDefaultBudget;
     double best = 1e300;
     int best_acc = x->one_acc, best_n = mx.nsplit;
     int rc = TDSCHA_OK;
@@ -1716,6 +1719,7 @@ static int autotune(tdscha_ctx *c) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    x->budget = budget;
     if (rc != TDSCHA_OK) return rc;
     set_stage_a(x, mx, best_acc);
     set_splits(x, mx, best_n);

@@ -295,9 +295,36 @@ def evaluate(term, runs, k, n_total, n_w=2000, w_max_cm=1100.0, smearing_cm=5.0,
             "saved_applications_mean": float(np.mean(saved))}
 
 
+def save_runs(path, **sets):
+    """Coefficient sequences of run sets in one npz: per set, a and b padded
+    with NaN to the longest run, sigma and M."""
+    out = {}
+    for name, runs in sets.items():
+        n = max(len(a) for a, _, _, _ in runs)
+        A = np.full((len(runs), n), np.nan)
+        B = np.full((len(runs), n), np.nan)
+        for i, (a, b, _, _) in enumerate(runs):
+            A[i, :len(a)] = a
+            B[i, :len(b)] = b
+        out[name + "_a"], out[name + "_b"] = A, B
+        out[name + "_sigma"] = np.array([r[2] for r in runs])
+        out[name + "_M"] = np.array([r[3] for r in runs])
+    np.savez_compressed(path, **out)
+
+
+def load_runs(path, name):
+    d = np.load(path)
+    runs = []
+    for a, b, s, m in zip(d[name + "_a"], d[name + "_b"], d[name + "_sigma"], d[name + "_M"]):
+        runs.append((a[~np.isnan(a)], b[~np.isnan(b)], float(s), int(m)))
+    return runs
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("cmd", choices=["train", "generate"])
+    ap.add_argument("--data", default=None,
+                    help="train: read the runs from this file (written by generate)")
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--n-train", type=int, default=200)
     ap.add_argument("--n-test", type=int, default=20)
@@ -317,12 +344,21 @@ def main():
     t0 = time.time()
     gen = dict(m_range=tuple(args.m_range), n_configs=args.n_configs, batch=args.batch,
                reorth=args.reorth)
-    train_runs = generate_runs(args.n_train, args.steps, seed=1, precision=args.train_precision,
-                               verbose=True, **gen)
-    t_tr = time.time()
-    test_runs = generate_runs(args.n_test, args.steps, seed=2, precision=args.test_precision,
-                              verbose=True, **gen)
-    t1 = time.time()
+    if args.data and args.cmd == "train":
+        train_runs, test_runs = load_runs(args.data, "train"), load_runs(args.data, "test")
+        t_tr = t1 = time.time()
+    else:
+        train_runs = generate_runs(args.n_train, args.steps, seed=1,
+                                   precision=args.train_precision, verbose=True, **gen)
+        t_tr = time.time()
+        test_runs = generate_runs(args.n_test, args.steps, seed=2,
+                                  precision=args.test_precision, verbose=True, **gen)
+        t1 = time.time()
+    if args.cmd == "generate":
+        save_runs(args.out, train=train_runs, test=test_runs)
+        print(json.dumps({"saved": args.out, "train": len(train_runs), "test": len(test_runs),
+                          "seconds": t1 - t0}))
+        return
     mlp, hist = train(train_runs, iters=args.iters)
     t2 = time.time()
     term = LearnedTerminator(mlp.get_params())
