@@ -409,9 +409,8 @@ def run_ours(args):
                 roof["tensor_work_incl_split_tflops"] = 3 * 2.0 * R * Mp * Mp / per_launch_s / 1e12
                 roof["frac_incl_split"] = roof["tensor_work_incl_split_tflops"] / peak
                 # DRAM bytes per launch from the ncu captures of the same kernels
-                # at N=20 000 (profiles/k_stageA_tc_m573_n20k.md for stage A,
-                # profiles/k_stageB_tc_m573_n20k.md for stage B), scaled by rows
-                per_row = {0: 147.9e6 / 20000, 3: 96.0e6 / 20000}[kid]
+                # at N=20 000 (profiles/k_stageA_stageB_m573_n20k.md), scaled by rows
+                per_row = {0: 147.2e6 / 20000, 3: 97.4e6 / 20000}[kid]
                 if M == 573 and S == 1:
                     roof["traffic"] = per_row * R
                     roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"
