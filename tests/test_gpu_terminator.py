@@ -53,13 +53,12 @@ def test_training_reduces_loss(gpu_lib):
 
 def test_trained_terminator_gains_over_plain(gpu_lib):
     """The committed network (tdscha_gb300/data), on ten runs it was not
-    trained on, at its training shapes (M in [96, 384], N = 20 000, 1000
-    Wigner steps): extending 100 steps to 1000 is closer to the 1000-step
-    spectrum than the 100-step continued fraction with the standard
-    terminator."""
+    trained on, at its training shapes (M in [48, 160], N = 4000, 320 Wigner
+    steps with full re-orthogonalisation): extending 100 steps to 320 is
+    closer to the 320-step spectrum than the 100-step continued fraction with
+    the standard terminator."""
     from tdscha_gb300.terminator import LearnedTerminator, evaluate, generate_runs
-    runs = generate_runs(10, 1000, seed=7, m_range=(96, 384), n_configs=20000, reorth=False,
-                         precision="mixed")
-    rep = evaluate(LearnedTerminator(), runs, 100, 1000)
+    runs = generate_runs(10, 320, seed=7)
+    rep = evaluate(LearnedTerminator(), runs, 100, 320)
     assert rep["learned_err_median"] < rep["plain_terminator_err_median"]
     assert rep["learned_better_fraction"] >= 0.6
