@@ -70,10 +70,6 @@ __global__ void k_psi_y1(const int *__restrict__ sc_idx, const double *__restric
     }
 }
 
-// hs[j][k][l] = sum_s G_js[k][l] + sum_s G_js[l][k], G_js[k][l] = g[s*ss + j*js + k*lda + l],
-// each sum in float64 in split order, through a 32 x 32 shared-memory tile so
-// that both the direct and the transposed partials are read along rows.
-// Blocks of the first tile row also form fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m].
 // sum_s p[s * stride] in float64, in split order, eight loads in flight
 // (the sums are load-latency bound)
 template <typename T>
@@ -91,30 +87,50 @@ __device__ __forceinline__ double split_sum(const T *__restrict__ p, int n, long
     return acc;
 }
 
+// hs[j][k][l] = hs[j][l][k] = sum_s G_js[k][l] + sum_s G_js[l][k], with
+// G_js[k][l] = g[s*ss + j*js + k*lda + l], each sum in float64 in split order.
+// One block per pair of 32 x 32 tiles (K <= L, upper triangle) and image: the
+// tile (K, L) and its mirror (L, K) are each read once, summed over the splits
+// into shared memory, and both halves of the symmetric result written along
+// rows.  Blocks of the first tile pair row also form
+// fs[j][m] = sum_ch fpart[(j*nfc + ch)*M + m] for their columns.
 template <typename T>
 __global__ void __launch_bounds__(256) k_psi_hsum(const T *__restrict__ g, int nsplit, long ss,
                                                   long js, long lda, const T *__restrict__ fpart,
                                                   int nfc, int M, double *__restrict__ hs,
                                                   double *__restrict__ fs) {
-    __shared__ double tile[32][33];
+    __shared__ double t1[32][33], t2[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;    // 32 x 8
-    const int l0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
-    const long j = blockIdx.z;
-    const T *base = g + j * js;
-    // transposed part: rows l of the tile's column range, columns k
-    for (int r = ty; r < 32; r += 8) {
-        int l = l0 + r, k = k0 + tx;
-        double acc = 0;
-        if (l < M && k < M) acc = split_sum(base + (long)l * lda + k, nsplit, ss);
-        tile[r][tx] = acc;            // tile[l - l0][k - k0]
+    const int nt = (M + 31) / 32;
+    int K = 0, rem = blockIdx.x;
+    while (rem >= nt - K) {
+        rem -= nt - K;
+        ++K;
     }
-    __syncthreads();
+    const int L = K + rem;
+    const int k0 = K * 32, l0 = L * 32;
+    const long j = blockIdx.y;
+    const T *base = g + j * js;
     for (int r = ty; r < 32; r += 8) {
         int k = k0 + r, l = l0 + tx;
-        if (k < M && l < M)
-            hs[(j * M + k) * M + l] = split_sum(base + (long)k * lda + l, nsplit, ss) + tile[tx][r];
+        t1[r][tx] = (k < M && l < M) ? split_sum(base + (long)k * lda + l, nsplit, ss) : 0.0;
+        if (K != L) {
+            int l2 = l0 + r, k2 = k0 + tx;
+            t2[r][tx] = (l2 < M && k2 < M) ? split_sum(base + (long)l2 * lda + k2, nsplit, ss) : 0.0;
+        }
     }
-    if (blockIdx.y == 0 && ty == 0) {
+    __syncthreads();
+    double(*m2)[33] = K != L ? t2 : t1;     // m2[l - l0][k - k0] = sum_s G[l][k]
+    double *H = hs + j * (long)M * M;
+    for (int r = ty; r < 32; r += 8) {
+        int k = k0 + r, l = l0 + tx;        // rows of tile (K, L)
+        if (k < M && l < M) H[(long)k * M + l] = t1[r][tx] + m2[tx][r];
+        if (K != L) {
+            int l2 = l0 + r, k2 = k0 + tx;  // rows of the mirror tile (L, K)
+            if (l2 < M && k2 < M) H[(long)l2 * M + k2] = t1[tx][r] + m2[r][tx];
+        }
+    }
+    if (K == 0 && ty == 0) {
         int m = l0 + tx;
         if (m < M) fs[j * M + m] = split_sum(fpart + j * nfc * M + m, nfc, M);
     }
@@ -251,7 +267,8 @@ static int psi_finalize(tdscha_ctx *c, const T *gpart, int nsplit, long sstride,
     const size_t JMM = (size_t)J * M * M, JM = (size_t)J * M;
     double *hs = c->hs, *tj = hs + JMM, *fs = tj + JMM, *tf = fs + JM;
     ProfScope ps(c, 4, st);
-    dim3 gt(ceil_div(M, 32), ceil_div(M, 32), J);
+    const int nt = ceil_div(M, 32);
+    dim3 gt(nt * (nt + 1) / 2, J);
     k_psi_hsum<T><<<gt, 256, 0, st>>>(gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, M, hs,
                                       fs);
     TDS_CHECK_LAUNCH();
