@@ -110,9 +110,10 @@ int tdscha_apply_full_L(tdscha_ctx *ctx, const double *psi_in, double *psi_out,
  * run_simm == 0 and the symmetric Wigner Lanczos with the double-counting mask
  * (mask_dot_wigner, :5905-5954) when run_simm != 0.
  *
- * basis_Q, basis_P: device buffers of (capacity) x P doubles; rows
- *   0 .. start_step hold the Krylov vectors already computed (row 0 is the
- *   normalised start vector, which the caller writes before the first call).
+ * basis_Q, basis_P: device buffers of (capacity) rows of P doubles, row stride
+ *   P or the one set by tdscha_ctx_set_basis_ld; rows 0 .. start_step hold
+ *   the Krylov vectors already computed (row 0 is the normalised start
+ *   vector, which the caller writes before the first call).
  * hist: host double[4 * capacity] holding a_k, b_k, c_k, s_norm_k in rows of 4
  *   for k < start_step (a, b, c) and k <= start_step (s_norm); the call
  *   appends the new rows.  n_iter steps are attempted; *steps_done receives
@@ -125,6 +126,17 @@ int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int ca
                        int start_step, int n_iter, int run_simm, int precision,
                        int full_reorth, double *hist, int *steps_done, int *converged,
                        void *stream);
+
+/*
+ * Row stride (in doubles) of the basis buffers that tdscha_lanczos_run and
+ * tdscha_lanczos_run_batch receive for this context: row k of basis_Q starts
+ * at basis_Q + k * ld.  0 (the default) means ld = P; otherwise ld >= P.  No
+ * counterpart in the reference, whose basis is a list of vectors.  With an even
+ * ld and 16-byte aligned basis pointers the re-biorthogonalisation reads two
+ * elements per load (the Python layer pads rows to 32 doubles); other layouts
+ * take one element per load.
+ */
+int tdscha_ctx_set_basis_ld(tdscha_ctx *ctx, long long ld);
 
 /*
  * tdscha_lanczos_run with host-memory basis arrays (capacity x P doubles each):
@@ -178,7 +190,8 @@ int tdscha_continued_fraction(const double *a, int n, const double *b, int n_b,
  * 0 stops.  tdscha_ctx_profile_read returns the total device milliseconds and
  * the launch count recorded for kernel_id: 0 stage A (quadratic forms),
  * 1 row scalars, 2 force average, 3 stage B (weighted outer products),
- * 4 finalisation, 5 operand preparation; it synchronises the device.
+ * 4 finalisation, 5 operand preparation, 6 re-biorthogonalisation dots and
+ * coefficients, 7 re-biorthogonalisation update; it synchronises the device.
  */
 int tdscha_ctx_profile(tdscha_ctx *ctx, int enable);
 int tdscha_ctx_profile_read(tdscha_ctx *ctx, int kernel_id, double *total_ms, int *launches);

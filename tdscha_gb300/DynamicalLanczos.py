@@ -620,9 +620,9 @@ class Lanczos(object):
 
     def _sync_basis(self, drop_device=False):
         if getattr(self, "_Qd", None) is not None:
-            n = self._nbasis
-            Q = self._Qd[:n].cpu().numpy()
-            Pm = self._Pd[:n].cpu().numpy()
+            n, P = self._nbasis, self._Plen
+            Q = self._Qd[:n, :P].cpu().numpy()
+            Pm = self._Pd[:n, :P].cpu().numpy()
             self._basis_host = ([q for q in Q], [p for p in Pm])
             if drop_device:
                 self._Qd = self._Pd = None
@@ -703,21 +703,24 @@ class Lanczos(object):
                 raise AssertionError("Something wrong when restoring the Lanczos. len b = {} len c = {}"
                                      .format(len(self.b_coeffs), len(self.c_coeffs)))
         cap = i_step + n_iter + 2
+        # rows padded to 32 doubles; the context is told the stride
+        ld = ctx.basis_ld()
+        ctx.set_basis_ld(ld)
         if i_step == 0 or self._Qd is None or self._Qd.shape[0] < cap:
-            Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
-            Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+            Qd = torch.empty((cap, ld), dtype=torch.float64, device=dev)
+            Pd = torch.empty((cap, ld), dtype=torch.float64, device=dev)
             if i_step == 0:
-                Qd[0].copy_(torch.from_numpy(first))
-                Pd[0].copy_(torch.from_numpy(first))
+                Qd[0, :P].copy_(torch.from_numpy(first))
+                Pd[0, :P].copy_(torch.from_numpy(first))
             elif self._Qd is not None:
                 Qd[: self._nbasis].copy_(self._Qd[: self._nbasis])
                 Pd[: self._nbasis].copy_(self._Pd[: self._nbasis])
             else:
                 Qh = np.asarray(self._basis_host[0], dtype=np.float64)
                 Ph = np.asarray(self._basis_host[1], dtype=np.float64)
-                Qd[: len(Qh)].copy_(torch.from_numpy(Qh))
-                Pd[: len(Ph)].copy_(torch.from_numpy(Ph))
-            self._Qd, self._Pd = Qd, Pd
+                Qd[: len(Qh), :P].copy_(torch.from_numpy(Qh))
+                Pd[: len(Ph), :P].copy_(torch.from_numpy(Ph))
+            self._Qd, self._Pd, self._Plen = Qd, Pd, P
         self._nbasis = i_step + 1
         self._basis_host = None
         hist = np.zeros(4 * cap, dtype=np.float64)

@@ -31,7 +31,7 @@ EXPORTS = [
     "tdscha_mlp_num_params", "tdscha_mlp_set_params", "tdscha_mlp_get_params",
     "tdscha_mlp_forward", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
     "tdscha_release_cached_memory", "tdscha_ctx_layout", "tdscha_ctx_tuning",
-    "tdscha_qctx_set_precision",
+    "tdscha_qctx_set_precision", "tdscha_ctx_set_basis_ld",
 ]
 
 
@@ -72,6 +72,7 @@ def load():
     lib.tdscha_apply_full_L.argtypes = [_vp, _vp, _vp, _c_int, _c_int, _vp]
     lib.tdscha_lanczos_run.argtypes = [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int,
                                        _c_int, _d, _i, _i, _vp]
+    lib.tdscha_ctx_set_basis_ld.argtypes = [_vp, ctypes.c_longlong]
     lib.tdscha_continued_fraction.argtypes = [
         _d, _c_int, _d, _c_int, _d, _c_int, _d, _c_int, _c_int, _c_double, _c_int, _c_double,
         _c_int, _c_int, _c_double, _c_int, _d]
@@ -210,6 +211,14 @@ class Context:
         check(load().tdscha_ctx_tuning(self.handle, ctypes.byref(a), ctypes.byref(n),
                                        ctypes.byref(ms)))
         return a.value, n.value, ms.value
+
+    def basis_ld(self):
+        """Row stride used for Lanczos basis buffers: P rounded up to 32 doubles
+        (256-byte rows, so that the re-biorthogonalisation reads element pairs)."""
+        return (self.P + 31) // 32 * 32
+
+    def set_basis_ld(self, ld):
+        check(load().tdscha_ctx_set_basis_ld(self.handle, int(ld)))
 
     def set_options(self, use_wigner, ignore_harmonic, ignore_v3, ignore_v4, reverse_L, shift):
         opts = (int(bool(use_wigner)), int(bool(ignore_harmonic)), int(bool(ignore_v3)),

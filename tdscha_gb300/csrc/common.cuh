@@ -108,6 +108,7 @@ struct tdscha_ctx {
     int J = 1, maxdeg = 1;
     int *sc_idx = nullptr, *sr_idx = nullptr;
     double *sc_val = nullptr, *sr_val = nullptr;
+    float2 *sr_val2 = nullptr;  // sr_val as double-float pairs (mixed path)
     double *Y1all = nullptr;    // float64 path, J x M x M: S_j^T Y1 S_j
     double *vsv = nullptr;      // J x M: S_j^T (f_Y R1), then J x M: S_j^T R1
     double *hs = nullptr;       // J x M x M: G_j + G_j^T summed over the splits
@@ -133,6 +134,8 @@ struct tdscha_ctx {
     double *pqn = nullptr;      // p_j . q_j of the stored basis (full reorthogonalisation)
     double *rcoef = nullptr;    // projection coefficients (2 per basis vector)
     int pqn_cap = 0;
+    float2 *vsplit = nullptr;   // 2 x ldv: double-float splits of the masked new pair
+    long basis_ld = 0;          // row stride of the Lanczos basis buffers (0: P)
     double *host_pinned = nullptr;
     int nblk_dot = 0;
     tdscha::MixedStore mx;

@@ -196,6 +196,7 @@ static void ctx_free(tdscha_ctx *c) {
     for (double *p : bufs) cached_free(p);
     cached_free(c->tri);
     cached_free(c->lam_static);
+    cached_free(c->vsplit);
     free_translations(c);
     psi_free(c);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);
@@ -362,7 +363,11 @@ images_done:
     TRYC(dev_alloc(&c->rk, c->P)); TRYC(dev_alloc(&c->sk, c->P));
     TRYC(dev_alloc(&c->mask, c->P)); TRYC(dev_alloc(&c->pc, 12 * c->H + 4 * (size_t)M));
     c->nblk_dot = 296;    // block partials of the fused dot kernels (two blocks per SM)
-    TRYC(dev_alloc(&c->dots, 4 * (size_t)std::max(c->nblk_dot, 1216))); TRYC(dev_alloc(&c->scal, 64));
+    // block partials: the fused dot kernels (up to 1216 blocks, three sums) and
+    // the tiled re-biorthogonalisation update (one per 64 elements)
+    TRYC(dev_alloc(&c->dots, std::max<size_t>(4 * (size_t)std::max(c->nblk_dot, 1216),
+                                              (size_t)(c->P + 63) / 64)));
+    TRYC(dev_alloc(&c->scal, 64));
     CUC(cudaMemset(c->scal, 0, sizeof(double) * 64));
     CUC(cudaMallocHost((void **)&c->host_pinned, sizeof(double) * 64));
     TRYC(build_pair_coeffs(c));
@@ -490,6 +495,17 @@ extern "C" int tdscha_get_perturb_average_sym(int M, int N, const double *X, con
     tdscha_ctx_destroy(c);
     if (rc != TDSCHA_OK) set_error("%s", keep.c_str());
     return rc;
+}
+
+extern "C" int tdscha_ctx_set_basis_ld(tdscha_ctx *ctx, long long ld) {
+    set_error("");
+    if (!ctx) { set_error("set_basis_ld: null context"); return TDSCHA_ERR_ARG; }
+    if (ld != 0 && ld < ctx->P) {
+        set_error("set_basis_ld: row stride %lld below the vector length %ld", ld, ctx->P);
+        return TDSCHA_ERR_ARG;
+    }
+    ctx->basis_ld = (long)ld;
+    return TDSCHA_OK;
 }
 
 extern "C" int tdscha_ctx_profile(tdscha_ctx *ctx, int enable) {

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace tdscha {
 
@@ -440,17 +441,41 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
     }
 }
 
+// ---------------------------------------------------------------------------
+// The re-biorthogonalisation below runs in double-float (dfloat.cuh): GB300
+// issues float64 at 2 FMA per clock per SM against 128 float32/int32 lanes,
+// and the classical Gram-Schmidt pass spends two products per element and
+// stored vector in each of its two sweeps.  In float64 both sweeps sat on the
+// float64 pipe (0.8 element-vector per clock per SM) at every step index; with
+// the operands split by integer operations and the products and sums formed
+// error-free in float32, no float64 instruction runs per (element, vector)
+// pair and the sweeps become HBM-bound.
+
+// q_{k+1} = r_k / b, p_{k+1} = s_k / s_raw.  With vs != nullptr (full
+// re-biorthogonalisation) also the double-float splits of the masked new pair
+// the projection dots read: vs[e] = split(q mask), vs[ldv + e] = split(p mask).
 __global__ void k_normalize(const double *__restrict__ rk, const double *__restrict__ sk,
                             const double *__restrict__ scal, long n, double *__restrict__ qn,
-                            double *__restrict__ pn) {
+                            double *__restrict__ pn, const double *__restrict__ mask,
+                            float2 *__restrict__ vs, long ldv) {
     pdl_enter();
     if (scal[SC_HALT] != 0.0) return;
     // the reciprocals come from k_scal_bc: a float64 division per thread here
     // cost more than the whole pass
     const double ib = scal[SC_IB], is = scal[SC_IS];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        qn[e] = rk[e] * ib;
-        pn[e] = sk[e] * is;
+        double q = rk[e] * ib, p = sk[e] * is;
+        qn[e] = q;
+        pn[e] = p;
+        if (vs) {
+            if (mask) {
+                const double m = mask[e];
+                q *= m;
+                p *= m;
+            }
+            vs[e] = split_f64(q);
+            vs[ldv + e] = split_f64(p);
+        }
     }
 }
 
@@ -589,6 +614,275 @@ __global__ void k_proj_apply(const double *__restrict__ Qb, const double *__rest
     }
     if (pq_part) {
         double t = block_sum(pq, sh);
+        if (threadIdx.x == 0) pq_part[blockIdx.x] = t;
+    }
+}
+
+// Real-space re-biorthogonalisation in double-float (see split_f64).  The
+// same classical Gram-Schmidt pass as k_proj_dots / k_proj_scale /
+// k_proj_apply: the dots of every stored vector against the unprojected new
+// pair, then one update q -= sum_j c_j q_j, p -= sum_j d_j p_j in ascending j.
+//
+// Dots: block (j, chunk) sums P_j . split(q mask) and Q_j . split(p mask)
+// over a contiguous element range, four strides' loads in flight per thread;
+// each thread's double-float sums are folded into float64 once and reduced by
+// the float64 block tree.
+__global__ void k_rdots(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                        const float2 *__restrict__ vs, long n, long ldv, long ld,
+                        double *__restrict__ part) {
+    pdl_enter();
+    __shared__ double sh[32];
+    const int j = blockIdx.x;
+    const long nch = gridDim.y;
+    const long e0 = n * blockIdx.y / nch, e1 = n * (blockIdx.y + 1) / nch;
+    const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
+    const float2 *qm = vs, *pm = vs + ldv;
+    float as = 0.f, ac = 0.f, bs = 0.f, bc = 0.f;
+    const long bd = blockDim.x;
+    long e = e0 + threadIdx.x;
+    for (; e + 3 * bd < e1; e += 4 * bd) {
+        double vp[4], vq[4];
+        float2 vqm[4], vpm[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long x = e + u * bd;
+            vp[u] = pj[x];
+            vq[u] = qj[x];
+            vqm[u] = qm[x];
+            vpm[u] = pm[x];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            df_fma_acc(as, ac, split_f64(vp[u]), vqm[u]);
+            df_fma_acc(bs, bc, split_f64(vq[u]), vpm[u]);
+        }
+    }
+    for (; e < e1; e += bd) {
+        df_fma_acc(as, ac, split_f64(pj[e]), qm[e]);
+        df_fma_acc(bs, bc, split_f64(qj[e]), pm[e]);
+    }
+    double t = block_sum((double)as + (double)ac, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2] = t;
+    t = block_sum((double)bs + (double)bc, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2 + 1] = t;
+}
+
+// coef[j] = split(c_j), split(d_j) with c_j, d_j = chunk sums / (p_j . q_j)
+// (float64 sums and division); one warp per j
+__global__ void k_rscale(const double *__restrict__ part, const double *__restrict__ pqn,
+                         int nvec, int nch, float4 *__restrict__ coef) {
+    pdl_enter();
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (j >= nvec) return;   // whole warps
+    double a = warp_chunk_sum(part, j, nch, 2, 0);
+    double b = warp_chunk_sum(part, j, nch, 2, 1);
+    if ((threadIdx.x & 31) == 0) {
+        const double inv = 1.0 / pqn[j];
+        const float2 c = split_f64(a * inv), d = split_f64(b * inv);
+        coef[j] = make_float4(c.x, c.y, d.x, d.y);
+    }
+}
+
+constexpr int kRProjMax = 1024;   // coefficients per apply pass (16 KB of shared memory)
+// q -= sum_j c_j Q_j, p -= sum_j d_j P_j over j0 <= j < j0 + nvec: the sums
+// in double-float (eight vectors' loads in flight, ascending j), subtracted
+// from the float64 vectors once per pass.  With pq_part != nullptr (the last
+// pass) also the block partials of p . q (mask) for the new pair's weight.
+__global__ void __launch_bounds__(256) k_rapply(const double *__restrict__ Qb,
+                                                const double *__restrict__ Pb,
+                                                const float4 *__restrict__ coef, long n, int j0,
+                                                int nvec, long ld, double *__restrict__ qn,
+                                                double *__restrict__ pn,
+                                                const double *__restrict__ mask,
+                                                double *__restrict__ pq_part) {
+    pdl_enter();
+    __shared__ float4 cs[kRProjMax];
+    __shared__ double sh[32];
+    for (int t = threadIdx.x; t < nvec; t += blockDim.x) cs[t] = coef[j0 + t];
+    __syncthreads();
+    const double *Q0 = Qb + (long)j0 * ld, *P0 = Pb + (long)j0 * ld;
+    double pq = 0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        float qs = 0.f, qc = 0.f, ps = 0.f, pc = 0.f;
+        int j = 0;
+        for (; j + 8 <= nvec; j += 8) {
+            double vq[8], vp[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                vq[u] = Q0[(long)(j + u) * ld + e];
+                vp[u] = P0[(long)(j + u) * ld + e];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float4 c = cs[j + u];
+                df_fma_acc(qs, qc, make_float2(c.x, c.y), split_f64(vq[u]));
+                df_fma_acc(ps, pc, make_float2(c.z, c.w), split_f64(vp[u]));
+            }
+        }
+        for (; j < nvec; ++j) {
+            const float4 c = cs[j];
+            df_fma_acc(qs, qc, make_float2(c.x, c.y), split_f64(Q0[(long)j * ld + e]));
+            df_fma_acc(ps, pc, make_float2(c.z, c.w), split_f64(P0[(long)j * ld + e]));
+        }
+        const double q = (qn[e] - (double)qs) - (double)qc;
+        const double p = (pn[e] - (double)ps) - (double)pc;
+        qn[e] = q;
+        pn[e] = p;
+        if (pq_part) pq = fma(p, mask ? q * mask[e] : q, pq);
+    }
+    if (pq_part) {
+        double t = block_sum(pq, sh);
+        if (threadIdx.x == 0) pq_part[blockIdx.x] = t;
+    }
+}
+
+// Vector forms for 16-byte aligned rows (even row stride, aligned bases): two
+// consecutive elements per load.  Measured on the GB300 at 188 stored pairs of
+// 329 476 elements: a plain streaming read of the basis 160 us (6.2 TB/s),
+// these dots 190 us and this update 189 us, against 240 and 305 us for the
+// one-element forms above and 254 and 246 us for the float64 ones.
+
+// split_ld(n): the even stride between the q and p halves of ctx->vsplit
+inline long split_ld(long n) { return (n + 1) & ~1L; }
+
+// k_rdots over element pairs: block (j, chunk) takes pairs [i0, i1) of its
+// chunk, two pair strides' loads in flight; for odd n the last element is
+// added by thread 0 of the last chunk.  vs holds split(q mask) at [0, n) and
+// split(p mask) at [ldv, ldv + n), ldv even.
+__global__ void k_rdots2(const double *__restrict__ Qb, const double *__restrict__ Pb,
+                         const float2 *__restrict__ vs, long n, long ldv, long ld,
+                         double *__restrict__ part) {
+    pdl_enter();
+    __shared__ double sh[32];
+    const int j = blockIdx.x;
+    const long nch = gridDim.y, npair = n >> 1;
+    const long i0 = npair * blockIdx.y / nch, i1 = npair * (blockIdx.y + 1) / nch;
+    const double *pj = Pb + (long)j * ld, *qj = Qb + (long)j * ld;
+    const double2 *p2 = reinterpret_cast<const double2 *>(pj);
+    const double2 *q2 = reinterpret_cast<const double2 *>(qj);
+    const float4 *qm = reinterpret_cast<const float4 *>(vs);
+    const float4 *pm = reinterpret_cast<const float4 *>(vs + ldv);
+    float as = 0.f, ac = 0.f, bs = 0.f, bc = 0.f;
+    const long bd = blockDim.x;
+    long i = i0 + threadIdx.x;
+    for (; i + bd < i1; i += 2 * bd) {
+        double2 vp[2], vq[2];
+        float4 va[2], vb[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const long x = i + u * bd;
+            vp[u] = p2[x];
+            vq[u] = q2[x];
+            va[u] = qm[x];
+            vb[u] = pm[x];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            df_fma_acc(as, ac, split_f64(vp[u].x), make_float2(va[u].x, va[u].y));
+            df_fma_acc(as, ac, split_f64(vp[u].y), make_float2(va[u].z, va[u].w));
+            df_fma_acc(bs, bc, split_f64(vq[u].x), make_float2(vb[u].x, vb[u].y));
+            df_fma_acc(bs, bc, split_f64(vq[u].y), make_float2(vb[u].z, vb[u].w));
+        }
+    }
+    for (; i < i1; i += bd) {
+        const double2 vp = p2[i], vq = q2[i];
+        const float4 va = qm[i], vb = pm[i];
+        df_fma_acc(as, ac, split_f64(vp.x), make_float2(va.x, va.y));
+        df_fma_acc(as, ac, split_f64(vp.y), make_float2(va.z, va.w));
+        df_fma_acc(bs, bc, split_f64(vq.x), make_float2(vb.x, vb.y));
+        df_fma_acc(bs, bc, split_f64(vq.y), make_float2(vb.z, vb.w));
+    }
+    if ((n & 1) && blockIdx.y == nch - 1 && threadIdx.x == 0) {
+        const long e = n - 1;
+        df_fma_acc(as, ac, split_f64(pj[e]), vs[e]);
+        df_fma_acc(bs, bc, split_f64(qj[e]), vs[ldv + e]);
+    }
+    double t = block_sum((double)as + (double)ac, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2] = t;
+    t = block_sum((double)bs + (double)bc, sh);
+    if (threadIdx.x == 0) part[((long)j * nch + blockIdx.y) * 2 + 1] = t;
+}
+
+// k_rapply over tiles of 64 elements, one tile per block: lane l of warp w
+// holds the element pair (2l, 2l + 1) of the tile and sums the stored vectors
+// j = w, w + 8, ... (ascending) in double-float; the eight warps' sums are
+// then added in warp order per element and subtracted from the float64
+// vectors.  Odd n: the last pair's second element is the row padding (read,
+// never written; ld >= n + 1).  pq_part gets one partial per tile.
+constexpr int kTileWarps = 8;
+__global__ void __launch_bounds__(32 * kTileWarps) k_rapply2(
+    const double *__restrict__ Qb, const double *__restrict__ Pb, const float4 *__restrict__ coef,
+    long n, int j0, int nvec, long ld, double *__restrict__ qn, double *__restrict__ pn,
+    const double *__restrict__ mask, double *__restrict__ pq_part) {
+    pdl_enter();
+    __shared__ float4 cs[kRProjMax];
+    __shared__ float4 red[kTileWarps][64];
+    __shared__ double sh[32];
+    for (int t = threadIdx.x; t < nvec; t += blockDim.x) cs[t] = coef[j0 + t];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long ld2 = ld >> 1;
+    const double2 *Q2 = reinterpret_cast<const double2 *>(Qb + (long)j0 * ld);
+    const double2 *P2 = reinterpret_cast<const double2 *>(Pb + (long)j0 * ld);
+    const long npair = (n + 1) >> 1;
+    const long i = blockIdx.x * 32L + lane;
+    const long ic = i < npair ? i : npair - 1;
+    float qs0 = 0.f, qc0 = 0.f, qs1 = 0.f, qc1 = 0.f;
+    float ps0 = 0.f, pc0 = 0.f, ps1 = 0.f, pc1 = 0.f;
+    int j = w;
+    for (; j + kTileWarps < nvec; j += 2 * kTileWarps) {
+        double2 vq[2], vp[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            vq[u] = Q2[(long)(j + u * kTileWarps) * ld2 + ic];
+            vp[u] = P2[(long)(j + u * kTileWarps) * ld2 + ic];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const float4 c = cs[j + u * kTileWarps];
+            const float2 cq = make_float2(c.x, c.y), cp = make_float2(c.z, c.w);
+            df_fma_acc(qs0, qc0, cq, split_f64(vq[u].x));
+            df_fma_acc(qs1, qc1, cq, split_f64(vq[u].y));
+            df_fma_acc(ps0, pc0, cp, split_f64(vp[u].x));
+            df_fma_acc(ps1, pc1, cp, split_f64(vp[u].y));
+        }
+    }
+    for (; j < nvec; j += kTileWarps) {
+        const double2 vq = Q2[(long)j * ld2 + ic], vp = P2[(long)j * ld2 + ic];
+        const float4 c = cs[j];
+        const float2 cq = make_float2(c.x, c.y), cp = make_float2(c.z, c.w);
+        df_fma_acc(qs0, qc0, cq, split_f64(vq.x));
+        df_fma_acc(qs1, qc1, cq, split_f64(vq.y));
+        df_fma_acc(ps0, pc0, cp, split_f64(vp.x));
+        df_fma_acc(ps1, pc1, cp, split_f64(vp.y));
+    }
+    const float2 a0 = df_norm(qs0, qc0), a1 = df_norm(qs1, qc1);
+    const float2 b0 = df_norm(ps0, pc0), b1 = df_norm(ps1, pc1);
+    red[w][2 * lane] = make_float4(a0.x, a0.y, b0.x, b0.y);
+    red[w][2 * lane + 1] = make_float4(a1.x, a1.y, b1.x, b1.y);
+    __syncthreads();
+    double pq = 0;
+    if (w < 2) {
+        const int x = w * 32 + lane;
+        const long e = blockIdx.x * 64L + x;
+        if (e < n) {
+            float4 r = red[0][x];
+            float2 A = make_float2(r.x, r.y), B = make_float2(r.z, r.w);
+#pragma unroll
+            for (int g = 1; g < kTileWarps; ++g) {
+                r = red[g][x];
+                A = df_add(A, make_float2(r.x, r.y));
+                B = df_add(B, make_float2(r.z, r.w));
+            }
+            const double q = (qn[e] - (double)A.x) - (double)A.y;
+            const double p = (pn[e] - (double)B.x) - (double)B.y;
+            qn[e] = q;
+            pn[e] = p;
+            if (pq_part) pq = p * (mask ? q * mask[e] : q);
+        }
+    }
+    if (pq_part) {
+        const double t = block_sum(pq, sh);
         if (threadIdx.x == 0) pq_part[blockIdx.x] = t;
     }
 }
@@ -807,7 +1101,7 @@ namespace tdscha {
 
 // Buffers and start-of-run state of one real-space run (everything before the
 // first step of tdscha_lanczos_run); stream ordered.
-static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, long ld, int capacity,
                     int start_step, int run_simm, int full_reorth, const double *hist,
                     cudaStream_t st) {
     const long P = ctx->P;
@@ -829,10 +1123,11 @@ static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capac
             TDS_CUDA(cudaMalloc(&ctx->rcoef, sizeof(double) * 2 * (capacity + 1) * (kMaxChunks + 1)));
             ctx->pqn_cap = capacity + 1;
         }
+        if (!ctx->vsplit) TDS_CUDA(cudaMalloc(&ctx->vsplit, sizeof(float2) * 2 * split_ld(P)));
         // weights of the vectors already stored
         double *part = ctx->rcoef + 2 * (capacity + 1);
         const int nch = dot_chunks(P, start_step + 1);
-        k_pq_part<<<dim3(start_step + 1, nch), 256, 0, st>>>(basis_Q, basis_P, mask, P, P, 0, part);
+        k_pq_part<<<dim3(start_step + 1, nch), 256, 0, st>>>(basis_Q, basis_P, mask, P, ld, 0, part);
         k_pq_finish<<<ceil_div(start_step + 1, 8), 256, 0, st>>>(part, start_step + 1, 0, nch,
                                                                  ctx->pqn);
         TDS_CHECK_LAUNCH();
@@ -853,14 +1148,14 @@ static int lz_begin(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capac
 
 // The launches of step k (run_FT :6145-6448): operator application(s), the
 // recurrence scalars on the device, the new pair and its re-biorthogonalisation.
-static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity, int k,
-                   int run_simm, int precision, int full_reorth, cudaStream_t st) {
+static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, long ld, int capacity,
+                   int k, int run_simm, int precision, int full_reorth, cudaStream_t st) {
     const long P = ctx->P;
     const double *mask = run_simm ? ctx->mask : nullptr;
     const int nb = std::max(1, std::min(ceil_div(P, kDotThreads), ctx->nblk_dot));
     // elementwise passes over the vectors and the basis: eight blocks per SM
     const int nbw = std::max(1, std::min(ceil_div(P, kDotThreads), 1216));
-    double *q = basis_Q + (long)k * P, *p = basis_P + (long)k * P;
+    double *q = basis_Q + (long)k * ld, *p = basis_P + (long)k * ld;
     TDS_TRY(apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st));
     const double *pL = ctx->Lq;
     if (!run_simm) {
@@ -869,29 +1164,50 @@ static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capaci
     }
     launch_pdl(k_dot1, nb, kDotThreads, 0, st, p, ctx->Lq, mask, P, ctx->dots);
     launch_pdl(k_scal_a, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-    const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * P : nullptr;
-    const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * P : nullptr;
+    const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * ld : nullptr;
+    const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * ld : nullptr;
     launch_pdl(k_resid, nb, kDotThreads, 0, st, ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
                ctx->rk, ctx->sk, ctx->dots, nb);
     launch_pdl(k_scal_bc, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
-    double *qn = basis_Q + (long)(k + 1) * P, *pn = basis_P + (long)(k + 1) * P;
-    launch_pdl(k_normalize, nbw, kDotThreads, 0, st, ctx->rk, ctx->sk, ctx->scal, P, qn, pn);
+    double *qn = basis_Q + (long)(k + 1) * ld, *pn = basis_P + (long)(k + 1) * ld;
+    const long ldv = split_ld(P);
+    launch_pdl(k_normalize, nbw, kDotThreads, 0, st, ctx->rk, ctx->sk, ctx->scal, P, qn, pn, mask,
+               full_reorth ? ctx->vsplit : nullptr, ldv);
     if (full_reorth) {
         int nvec = k + 1;
         double *part = ctx->rcoef + 2 * (capacity + 1);
         const int nch = dot_chunks(P, nvec);
-        launch_pdl(k_proj_dots, dim3(nvec, nch), 256, 0, st, basis_Q, basis_P, qn, pn, mask, P, P,
-                   part);
-        launch_pdl(k_proj_scale, ceil_div(nvec, 8), 256, 0, st, part, ctx->pqn, nvec, nch,
-                   ctx->rcoef);
-        for (int j0 = 0; j0 < nvec; j0 += kProjMax) {
-            bool last = j0 + kProjMax >= nvec;
-            launch_pdl(k_proj_apply, nbw, 256, 0, st, basis_Q, basis_P, ctx->rcoef, P, j0,
-                       std::min(kProjMax, nvec - j0), P, qn, pn, mask,
-                       last ? ctx->dots : nullptr);
+        float4 *coef = reinterpret_cast<float4 *>(ctx->rcoef);
+        const float2 *vs = ctx->vsplit;
+        // two elements per load where every row starts on 16 bytes
+        const bool vec = (ld % 2 == 0) && ((uintptr_t)basis_Q % 16 == 0) &&
+                         ((uintptr_t)basis_P % 16 == 0);
+        {
+            ProfScope ps(ctx, 6, st);
+            if (vec)
+                launch_pdl(k_rdots2, dim3(nvec, nch), 256, 0, st, basis_Q, basis_P, vs, P, ldv, ld,
+                           part);
+            else
+                launch_pdl(k_rdots, dim3(nvec, nch), 256, 0, st, basis_Q, basis_P, vs, P, ldv, ld,
+                           part);
+            launch_pdl(k_rscale, ceil_div(nvec, 8), 256, 0, st, part, ctx->pqn, nvec, nch, coef);
+        }
+        ProfScope ps(ctx, 7, st);
+        const int ntile = (int)ceil_div(P, 64L);
+        const int npq = vec ? ntile : nbw;
+        for (int j0 = 0; j0 < nvec; j0 += kRProjMax) {
+            bool last = j0 + kRProjMax >= nvec;
+            if (vec)
+                launch_pdl(k_rapply2, ntile, 32 * kTileWarps, 0, st, basis_Q, basis_P,
+                           (const float4 *)coef, P, j0, std::min(kRProjMax, nvec - j0), ld, qn,
+                           pn, mask, last ? ctx->dots : nullptr);
+            else
+                launch_pdl(k_rapply, nbw, 256, 0, st, basis_Q, basis_P, (const float4 *)coef, P,
+                           j0, std::min(kRProjMax, nvec - j0), ld, qn, pn, mask,
+                           last ? ctx->dots : nullptr);
         }
         // weight p_{k+1} . q_{k+1} of the new pair from the apply pass's partials
-        launch_pdl(k_pq_reduce, 1, 512, 0, st, ctx->dots, nbw, ctx->pqn, k + 1);
+        launch_pdl(k_pq_reduce, 1, 512, 0, st, ctx->dots, npq, ctx->pqn, k + 1);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { set_error("lanczos_run launch: %s", cudaGetErrorString(e)); return TDSCHA_ERR_CUDA; }
@@ -905,10 +1221,12 @@ constexpr int kSyncEvery = 16;
 
 }  // namespace tdscha
 
-extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
-                                  int start_step, int n_iter, int run_simm, int precision,
-                                  int full_reorth, double *hist, int *steps_done, int *converged,
-                                  void *stream) {
+namespace tdscha {
+
+// tdscha_lanczos_run on basis rows of stride ld
+static int lz_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, long ld, int capacity,
+                  int start_step, int n_iter, int run_simm, int precision, int full_reorth,
+                  double *hist, int *steps_done, int *converged, void *stream) {
     set_error("");
     if (!ctx || !basis_Q || !basis_P || !hist || !steps_done || !converged) {
         set_error("lanczos_run: null pointer");
@@ -925,7 +1243,8 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
     *steps_done = 0;
     *converged = 0;
     cudaStream_t st = (cudaStream_t)stream;
-    TDS_TRY(lz_begin(ctx, basis_Q, basis_P, capacity, start_step, run_simm, full_reorth, hist, st));
+    TDS_TRY(lz_begin(ctx, basis_Q, basis_P, ld, capacity, start_step, run_simm, full_reorth, hist,
+                     st));
     LaggedReadBack rb(ctx->hist_dev, ctx->stat_dev, ctx->stat_host, capacity, st);
     TDS_TRY(rb.init());
     int rc = TDSCHA_OK;
@@ -938,7 +1257,8 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
             rc = TDSCHA_ERR_ARG;
             break;
         }
-        if ((rc = lz_step(ctx, basis_Q, basis_P, capacity, k, run_simm, precision, full_reorth, st)) != TDSCHA_OK)
+        if ((rc = lz_step(ctx, basis_Q, basis_P, ld, capacity, k, run_simm, precision, full_reorth,
+                          st)) != TDSCHA_OK)
             break;
         if ((it + 1) % kSyncEvery != 0 && it + 1 != n_iter) continue;
         rc = rb.boundary(next, k, hist, start_step, steps_done, converged, &stop);
@@ -957,6 +1277,22 @@ extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basi
     int mrc = mixed_check_error(ctx);
     if (mrc != TDSCHA_OK) rc = mrc;
     return rc;
+}
+
+inline long basis_stride(const tdscha_ctx *ctx) { return ctx->basis_ld ? ctx->basis_ld : ctx->P; }
+
+}  // namespace tdscha
+
+extern "C" int tdscha_lanczos_run(tdscha_ctx *ctx, double *basis_Q, double *basis_P, int capacity,
+                                  int start_step, int n_iter, int run_simm, int precision,
+                                  int full_reorth, double *hist, int *steps_done, int *converged,
+                                  void *stream) {
+    if (!ctx) {
+        set_error("lanczos_run: null pointer");
+        return TDSCHA_ERR_ARG;
+    }
+    return lz_run(ctx, basis_Q, basis_P, basis_stride(ctx), capacity, start_step, n_iter, run_simm,
+                  precision, full_reorth, hist, steps_done, converged, stream);
 }
 
 namespace tdscha {
@@ -1117,7 +1453,8 @@ static int qz_step(tdscha_qctx *ctx, double *basis_Q, double *basis_P, int capac
                                          ctx->rk, ctx->sk, ctx->dots, nb);
     k_scal_bc<<<1, 256, 0, st>>>(ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
     double *qn = basis_Q + (long)(k + 1) * n, *pn = basis_P + (long)(k + 1) * n;
-    k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, n, qn, pn);
+    k_normalize<<<nb, kDotThreads, 0, st>>>(ctx->rk, ctx->sk, ctx->scal, n, qn, pn, nullptr, nullptr,
+                                            0L);
     if (reorthogonalize) {
         // one classical Gram-Schmidt pass of q_{k+1} against q_0..q_k with the
         // real mask product (the p side of the shared kernels runs on the
@@ -1234,7 +1571,8 @@ extern "C" int tdscha_lanczos_run_batch(tdscha_run *runs, int n_runs) {
         own.push_back(streams[i]);
         tdscha_run &r = runs[i];
         int b = r.kind == 0
-                    ? lz_begin((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, r.start_step,
+                    ? lz_begin((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P,
+                               basis_stride((tdscha_ctx *)r.ctx), r.capacity, r.start_step,
                                r.run_simm, r.reorth, r.hist, streams[i])
                     : qz_begin((tdscha_qctx *)r.ctx, r.basis_Q, r.capacity, r.start_step, r.reorth,
                                r.hist, streams[i]);
@@ -1252,7 +1590,8 @@ extern "C" int tdscha_lanczos_run_batch(tdscha_run *runs, int n_runs) {
             for (int t = 0; t < todo; ++t) {
                 int k = r.start_step + done[i] + t;
                 int e = r.kind == 0
-                            ? lz_step((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, k,
+                            ? lz_step((tdscha_ctx *)r.ctx, r.basis_Q, r.basis_P,
+                                      basis_stride((tdscha_ctx *)r.ctx), r.capacity, k,
                                       r.run_simm, r.precision, r.reorth, streams[i])
                             : qz_step((tdscha_qctx *)r.ctx, r.basis_Q, r.basis_P, r.capacity, k,
                                       r.reorth, streams[i]);
@@ -1333,27 +1672,31 @@ extern "C" int tdscha_lanczos_run_hostbuf(tdscha_ctx *ctx, double *basis_Q, doub
     }
     const long P = ctx->P;
     const size_t row = sizeof(double) * P;
+    // device rows padded to 32 doubles (256 bytes): the re-biorthogonalisation
+    // then reads two elements per load
+    const long ld = (P + 31) / 32 * 32;
+    const size_t pitch = sizeof(double) * ld;
     double *dQ = nullptr, *dP = nullptr;
     int rc = TDSCHA_OK;
     auto cleanup = [&]() { if (dQ) cudaFree(dQ); if (dP) cudaFree(dP); };
-    if (cudaMalloc(&dQ, row * capacity) != cudaSuccess || cudaMalloc(&dP, row * capacity) != cudaSuccess) {
+    if (cudaMalloc(&dQ, pitch * capacity) != cudaSuccess || cudaMalloc(&dP, pitch * capacity) != cudaSuccess) {
         cleanup();
-        set_error("lanczos_run_hostbuf: cannot allocate %zu bytes for the basis", 2 * row * capacity);
+        set_error("lanczos_run_hostbuf: cannot allocate %zu bytes for the basis", 2 * pitch * capacity);
         return TDSCHA_ERR_CUDA;
     }
-    if (cudaMemcpy(dQ, basis_Q, row * (start_step + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(dP, basis_P, row * (start_step + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpy2D(dQ, pitch, basis_Q, row, row, start_step + 1, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy2D(dP, pitch, basis_P, row, row, start_step + 1, cudaMemcpyHostToDevice) != cudaSuccess) {
         cleanup();
         set_error("lanczos_run_hostbuf: %s", cudaGetErrorString(cudaGetLastError()));
         return TDSCHA_ERR_CUDA;
     }
-    rc = tdscha_lanczos_run(ctx, dQ, dP, capacity, start_step, n_iter, run_simm, precision,
-                            full_reorth, hist, steps_done, converged, 0);
+    rc = lz_run(ctx, dQ, dP, ld, capacity, start_step, n_iter, run_simm, precision, full_reorth,
+                hist, steps_done, converged, 0);
     int nrows = *steps_done - (*converged ? 1 : 0);   // new basis rows written
     if (nrows > 0) {
-        size_t off = (size_t)(start_step + 1) * P;
-        if (cudaMemcpy(basis_Q + off, dQ + off, row * nrows, cudaMemcpyDeviceToHost) != cudaSuccess ||
-            cudaMemcpy(basis_P + off, dP + off, row * nrows, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        const size_t r0 = (size_t)(start_step + 1);
+        if (cudaMemcpy2D(basis_Q + r0 * P, row, dQ + r0 * ld, pitch, row, nrows, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy2D(basis_P + r0 * P, row, dP + r0 * ld, pitch, row, nrows, cudaMemcpyDeviceToHost) != cudaSuccess) {
             if (rc == TDSCHA_OK) {
                 set_error("lanczos_run_hostbuf: %s", cudaGetErrorString(cudaGetLastError()));
                 rc = TDSCHA_ERR_CUDA;

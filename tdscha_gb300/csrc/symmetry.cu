@@ -26,6 +26,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace tdscha {
 
@@ -172,6 +173,139 @@ __global__ void k_psi_jsum(const double *__restrict__ tj, const double *__restri
     }
 }
 
+// ---------------------------------------------------------------------------
+// The mixed path's finalisation in double-float (dfloat.cuh).  The float64
+// forms above spend a float32 -> float64 conversion and a float64 add per
+// split partial (J M^2 nsplit of them: 17 M at M = 189, 48 images, 10 splits),
+// which kept k_psi_hsum on the float64 pipe at about 0.5 operations per clock
+// per SM; here every sum up to d2v itself runs on float32 pairs.
+
+// sum_s p[s * stride] as a normalised double-float pair, split order, eight
+// loads in flight
+__device__ __forceinline__ float2 split_sum_df(const float *__restrict__ p, int n, long stride) {
+    float s = 0.f, c = 0.f;
+    int k = 0;
+    for (; k + 8 <= n; k += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = p[(long)(k + u) * stride];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) df_two_sum_acc(s, c, v[u]);
+    }
+    for (; k < n; ++k) df_two_sum_acc(s, c, p[(long)k * stride]);
+    return df_norm(s, c);
+}
+
+// k_psi_hsum for float partials: the same tile pairs, hs2 and fs2 as
+// double-float pairs
+__global__ void __launch_bounds__(256) k_psi_hsum_df(const float *__restrict__ g, int nsplit,
+                                                     long ss, long js, long lda,
+                                                     const float *__restrict__ fpart, int nfc,
+                                                     int M, float2 *__restrict__ hs,
+                                                     float2 *__restrict__ fs) {
+    __shared__ float2 t1[32][33], t2[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;    // 32 x 8
+    const int nt = (M + 31) / 32;
+    int K = 0, rem = blockIdx.x;
+    while (rem >= nt - K) {
+        rem -= nt - K;
+        ++K;
+    }
+    const int L = K + rem;
+    const int k0 = K * 32, l0 = L * 32;
+    const long j = blockIdx.y;
+    const float *base = g + j * js;
+    const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = ty; r < 32; r += 8) {
+        int k = k0 + r, l = l0 + tx;
+        t1[r][tx] = (k < M && l < M) ? split_sum_df(base + (long)k * lda + l, nsplit, ss) : zero;
+        if (K != L) {
+            int l2 = l0 + r, k2 = k0 + tx;
+            t2[r][tx] = (l2 < M && k2 < M) ? split_sum_df(base + (long)l2 * lda + k2, nsplit, ss) : zero;
+        }
+    }
+    __syncthreads();
+    float2(*m2)[33] = K != L ? t2 : t1;     // m2[l - l0][k - k0] = sum_s G[l][k]
+    float2 *H = hs + j * (long)M * M;
+    for (int r = ty; r < 32; r += 8) {
+        int k = k0 + r, l = l0 + tx;        // rows of tile (K, L)
+        if (k < M && l < M) H[(long)k * M + l] = df_add(t1[r][tx], m2[tx][r]);
+        if (K != L) {
+            int l2 = l0 + r, k2 = k0 + tx;  // rows of the mirror tile (L, K)
+            if (l2 < M && k2 < M) H[(long)l2 * M + k2] = df_add(t1[tx][r], m2[r][tx]);
+        }
+    }
+    if (K == 0 && ty == 0) {
+        int m = l0 + tx;
+        if (m < M) fs[j * M + m] = split_sum_df(fpart + j * nfc * M + m, nfc, M);
+    }
+}
+
+// k_psi_sandwich in double-float: tj[j][a][b] = sum_{k,l} S_j[a][k] hs[j][k][l] S_j[b][l],
+// tf[j][a] = sum_k S_j[a][k] fs[j][k]
+__global__ void k_psi_sandwich_df(const int *__restrict__ sr_idx, const float2 *__restrict__ sr_val,
+                                  const float2 *__restrict__ hs, const float2 *__restrict__ fs,
+                                  int J, int M, int md, float2 *__restrict__ tj,
+                                  float2 *__restrict__ tf) {
+    const long MM = (long)M * M, n = (long)J * MM;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const long j = e / MM;
+        const int a = (int)((e - j * MM) / M), b = (int)(e % M);
+        const int *ia = sr_idx + (j * M + a) * md, *ib = sr_idx + (j * M + b) * md;
+        const float2 *va = sr_val + (j * M + a) * md, *vb = sr_val + (j * M + b) * md;
+        const float2 *H = hs + j * MM;
+        float as = 0.f, ac = 0.f, fs_ = 0.f, fc = 0.f;
+        for (int p = 0; p < md && ia[p] >= 0; ++p) {
+            float is = 0.f, ic = 0.f;
+            const float2 *row = H + (long)ia[p] * M;
+            for (int q = 0; q < md && ib[q] >= 0; ++q) df_fma_acc(is, ic, vb[q], row[ib[q]]);
+            df_fma_acc(as, ac, va[p], df_norm(is, ic));
+            if (b == 0) df_fma_acc(fs_, fc, va[p], fs[j * M + ia[p]]);
+        }
+        tj[e] = df_norm(as, ac);
+        if (b == 0) tf[j * M + a] = df_norm(fs_, fc);
+    }
+}
+
+// d2v[a][b] = -inv sum_j tj[j][a][b], f[a] = inv sum_j tf[j][a]: block (64, 4),
+// thread (x, y) sums the images j = y, y + 4, ... of element blockIdx.x * 64 + x,
+// and the four partial sums are added in y order.
+__global__ void __launch_bounds__(256) k_psi_jsum_df(const float2 *__restrict__ tj,
+                                                     const float2 *__restrict__ tf, int J, int M,
+                                                     double inv, double *__restrict__ f,
+                                                     double *__restrict__ d2v) {
+    __shared__ float2 red[2][4][64];
+    const long MM = (long)M * M;
+    const int x = threadIdx.x, y = threadIdx.y;
+    const long e = blockIdx.x * 64L + x;
+    float s = 0.f, c = 0.f, s2 = 0.f, c2 = 0.f;
+    if (e < MM)
+        for (int j = y; j < J; j += 4) {
+            const float2 v = tj[j * MM + e];
+            df_two_sum_acc(s, c, v.x);
+            c += v.y;
+        }
+    if (e < M)
+        for (int j = y; j < J; j += 4) {
+            const float2 v = tf[(long)j * M + e];
+            df_two_sum_acc(s2, c2, v.x);
+            c2 += v.y;
+        }
+    red[0][y][x] = df_norm(s, c);
+    red[1][y][x] = df_norm(s2, c2);
+    __syncthreads();
+    if (y == 0 && e < MM) {
+        float2 t = red[0][0][x], u = red[1][0][x];
+        for (int k = 1; k < 4; ++k) {
+            t = df_add(t, red[0][k][x]);
+            u = df_add(u, red[1][k][x]);
+        }
+        d2v[e] = -df_to_double(t) * inv;
+        if (e < M) f[e] = df_to_double(u) * inv;
+    }
+}
+
 static int grid_for(long n) { return (int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 16)); }
 
 int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_space,
@@ -228,6 +362,14 @@ int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_spac
     TDS_CUDA(cudaMemcpy(c->sc_idx, ci.data(), sizeof(int) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->sr_val, rv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->sc_val, cv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
+    // double-float copy of the row-sparse values for the mixed path's sandwich
+    std::vector<float2> rv2(cells);
+    for (size_t i = 0; i < cells; ++i) {
+        float hi = (float)rv[i];
+        rv2[i] = make_float2(hi, (float)(rv[i] - (double)hi));
+    }
+    TDS_CUDA(cached_malloc(&c->sr_val2, sizeof(float2) * cells));
+    TDS_CUDA(cudaMemcpy(c->sr_val2, rv2.data(), sizeof(float2) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cached_malloc(&c->vsv, sizeof(double) * 2 * (size_t)S * M));
     // hs and tj (J x M x M each), fs and tf (J x M each)
     TDS_CUDA(cached_malloc(&c->hs, sizeof(double) * 2 * ((size_t)S * M * M + (size_t)S * M)));
@@ -241,6 +383,8 @@ void psi_free(tdscha_ctx *c) {
     cached_free(c->sc_idx);
     cached_free(c->sr_val);
     cached_free(c->sc_val);
+    cached_free(c->sr_val2);
+    c->sr_val2 = nullptr;
     cached_free(c->Y1all);
     cached_free(c->vsv);
     cached_free(c->hs);
@@ -288,7 +432,23 @@ int psi_finalize64(tdscha_ctx *c, const double *gpart, int nsplit, long sstride,
 
 int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, long jstride,
                    long lda, const float *fpart, int nfchunk, cudaStream_t st) {
-    return psi_finalize<float>(c, gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, st);
+    const int M = c->M, J = c->J;
+    const size_t JMM = (size_t)J * M * M, JM = (size_t)J * M;
+    // the float64 layout of hs, tj, fs, tf holds the double-float pairs
+    float2 *hs = reinterpret_cast<float2 *>(c->hs), *tj = hs + JMM, *fs = tj + JMM, *tf = fs + JM;
+    ProfScope ps(c, 4, st);
+    const int nt = ceil_div(M, 32);
+    dim3 gt(nt * (nt + 1) / 2, J);
+    k_psi_hsum_df<<<gt, 256, 0, st>>>(gpart, nsplit, sstride, jstride, lda, fpart, nfchunk, M, hs,
+                                      fs);
+    TDS_CHECK_LAUNCH();
+    k_psi_sandwich_df<<<grid_for((long)JMM), 256, 0, st>>>(c->sr_idx, c->sr_val2, hs, fs, J, M,
+                                                           c->maxdeg, tj, tf);
+    TDS_CHECK_LAUNCH();
+    k_psi_jsum_df<<<std::max(1, ceil_div((long)M * M, 64)), dim3(64, 4), 0, st>>>(
+        tj, tf, J, M, 1.0 / (c->sum_rho * c->S), c->f, c->d2v);
+    TDS_CHECK_LAUNCH();
+    return TDSCHA_OK;
 }
 
 }  // namespace tdscha

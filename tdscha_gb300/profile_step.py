@@ -47,13 +47,15 @@ def main():
     P = ctx.P
     cap = args.warmup + args.steps + 2
     dev = torch.device("cuda")
-    Qd = torch.empty((cap, P), dtype=torch.float64, device=dev)
-    Pd = torch.empty((cap, P), dtype=torch.float64, device=dev)
+    ld = ctx.basis_ld()                  # rows padded to 256 bytes
+    ctx.set_basis_ld(ld)
+    Qd = torch.empty((cap, ld), dtype=torch.float64, device=dev)
+    Pd = torch.empty((cap, ld), dtype=torch.float64, device=dev)
     psi = np.zeros(P)
     psi[:M] = random_R1(M, 11)
     first = torch.from_numpy(psi / np.linalg.norm(psi)).to(dev)
-    Qd[0].copy_(first)
-    Pd[0].copy_(first)
+    Qd[0, :P].copy_(first)
+    Pd[0, :P].copy_(first)
     hist = np.zeros(4 * cap)
     hist[3] = 1.0
     done, conv = ctypes.c_int(0), ctypes.c_int(0)

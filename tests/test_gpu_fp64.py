@@ -243,3 +243,50 @@ def test_full_reorth_keeps_biorthogonality(gpu_lib, golden):
     dg = np.abs(np.diag(G))
     off = np.abs(G - np.diag(np.diag(G))) / np.sqrt(np.outer(dg, dg))
     assert off.max() < 1e-10, off.max()
+
+
+@pytest.mark.parametrize("M", [21, 24])     # P = M (M + 2): 483 (odd) and 624 (even)
+def test_reorth_row_stride_paths_agree(gpu_lib, M):
+    """The re-biorthogonalisation reads element pairs when every basis row
+    starts on 16 bytes (even row stride) and single elements otherwise; the
+    row strides P, P + 1 and P padded to 32 doubles cover both forms for odd
+    and even P.  The runs agree to rounding and the bases stay biorthogonal."""
+    import torch
+    ens = make_ensemble(M, 600, seed=31, n_syms=1, rho_sigma=0.1)
+    ident = ([np.ones((1, 1, 1))] * M, [np.array([i], dtype=np.intc) for i in range(M)],
+             np.arange(M, dtype=np.intc))
+    ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], *ident)
+    ctx.set_options(False, False, False, False, False, 0.0)
+    P, n = ctx.P, 40
+    cap = n + 2
+    lib = nat.load()
+    psi = np.zeros(P)
+    psi[:M] = random_R1(M, 3)
+    first = torch.from_numpy(psi / np.linalg.norm(psi)).cuda()
+    runs = {}
+    for ld in (P, P + 1, ctx.basis_ld()):
+        ctx.set_basis_ld(ld)
+        Qd = torch.zeros((cap, ld), dtype=torch.float64, device="cuda")
+        Pd = torch.zeros((cap, ld), dtype=torch.float64, device="cuda")
+        Qd[0, :P].copy_(first)
+        Pd[0, :P].copy_(first)
+        hist = np.zeros(4 * cap)
+        hist[3] = 1.0
+        done, conv = ctypes.c_int(0), ctypes.c_int(0)
+        nat.check(lib.tdscha_lanczos_run(ctx.handle, Qd.data_ptr(), Pd.data_ptr(), cap, 0, n, 0,
+                                         nat.PREC_FP64, 1, nat.dp(hist), ctypes.byref(done),
+                                         ctypes.byref(conv), None))
+        assert done.value == n and not conv.value
+        Q = Qd[: n + 1, :P].cpu().numpy()
+        Pm = Pd[: n + 1, :P].cpu().numpy()
+        G = Pm @ Q.T
+        dg = np.abs(np.diag(G))
+        off = np.abs(G - np.diag(np.diag(G))) / np.sqrt(np.outer(dg, dg))
+        assert off.max() < 1e-12, (ld, off.max())
+        runs[ld] = hist[: 4 * n].reshape(n, 4)[:, :3]
+    ref = runs[P]
+    for ld, h in runs.items():
+        np.testing.assert_allclose(h, ref, rtol=1e-9, atol=1e-14 * np.abs(ref).max())
+    with pytest.raises(nat.TdschaError):
+        ctx.set_basis_ld(P - 1)
+    ctx.close()
