@@ -556,8 +556,12 @@ constexpr int kRBN = 192;
 constexpr int kRSlots = 4;
 constexpr uint32_t kRLimbA = kBM * kBK * 2;                  // 16 KB
 constexpr uint32_t kRSlotBytes = kRLimbA + kRBN * kBK * 2;   // 40 KB
-constexpr int kRBars = 2 * kRSlots + 7;
-constexpr size_t kRSmem = 1024 + kRSlots * (size_t)kRSlotBytes + 2 * (size_t)kPEpiBytes +
+// epilogue part buffers (d and g parts, one TMA load each from L2).  Three
+// buffers (two parts in flight while one is read) made this kernel slower at
+// M = 189, 48 images: 273 us against 262 us per launch with two
+constexpr int kREpiBufs = 2;
+constexpr int kRBars = 2 * kRSlots + 5 + kREpiBufs;   // full, empty, tfull[2], tempty[2], efull[], done
+constexpr size_t kRSmem = 1024 + kRSlots * (size_t)kRSlotBytes + kREpiBufs * (size_t)kPEpiBytes +
                           3 * kRBN * sizeof(float) + 8 * kRBars + 16;
 static_assert(kRSmem <= 232448, "stage A (one accumulator) shared memory above the limit");
 
@@ -579,13 +583,13 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *epi = smem + kRSlots * kRSlotBytes;
-    float *colv = reinterpret_cast<float *>(epi + 2 * kPEpiBytes);   // [3][kRBN]
+    float *colv = reinterpret_cast<float *>(epi + kREpiBufs * kPEpiBytes);   // [3][kRBN]
     uint64_t *bars = reinterpret_cast<uint64_t *>(colv + 3 * kRBN);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kRBars);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
     const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * kRSlots,
                    tfull0 = empty0 + 8 * kRSlots, tempty0 = tfull0 + 16, efull0 = tempty0 + 16,
-                   done = efull0 + 16;
+                   done = efull0 + 8 * kREpiBufs;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long budget = args.budget;
     const long G = gridDim.x;
@@ -606,8 +610,8 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
         for (int j = 0; j < 2; ++j) {
             mbar_init(tfull0 + 8 * j, 1);
             mbar_init(tempty0 + 8 * j, 128);
-            mbar_init(efull0 + 8 * j, 1);
         }
+        for (int j = 0; j < kREpiBufs; ++j) mbar_init(efull0 + 8 * j, 1);
         mbar_init(done, 1);
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -732,7 +736,7 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
             if (iss_i >= nloc) return;
             long t = t0 + iss_i;
             int arow = (int)(t / jn) * kBM, brow = (int)((t % jn) % nct) * kRBN;
-            int e = (int)(issued & 1);
+            int e = (int)(issued % kREpiBufs);
             uint32_t buf = smem_u32(epi + e * kPEpiBytes), bar = efull0 + 8 * e;
             int x = brow + iss_p * kPEpiCols;
             mbar_expect_tx(bar, kPEpiBytes);
@@ -744,10 +748,8 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
                 ++iss_i;
             }
         };
-        if (leader) {
-            issue_next();
-            issue_next();
-        }
+        if (leader)
+            for (int b = 0; b < kREpiBufs; ++b) issue_next();
         long consumed = 0;
         for (long i = 0; i < nloc; ++i) {
             long t = t0 + i;
@@ -793,9 +795,9 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
                 }
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
-                    const int e = (int)(consumed & 1);
-                    bool landed = mbar_wait_ab(efull0 + 8 * e, (uint32_t)(consumed >> 1) & 1,
-                                               budget, abort);
+                    const int e = (int)(consumed % kREpiBufs);
+                    bool landed = mbar_wait_ab(efull0 + 8 * e,
+                                               (uint32_t)(consumed / kREpiBufs) & 1, budget, abort);
                     __syncwarp();
                     if (epi_sync_or(!landed)) {
                         fail_code = 3;
@@ -848,7 +850,8 @@ __global__ void __launch_bounds__(192, 1) k_stageA_tc1(const __grid_constant__ T
             *abort = 1;
             if (leader)
                 for (long k = consumed; k < issued; ++k)
-                    mbar_wait(efull0 + 8 * (int)(k & 1), (uint32_t)(k >> 1) & 1, kDefaultBudget);
+                    mbar_wait(efull0 + 8 * (int)(k % kREpiBufs), (uint32_t)(k / kREpiBufs) & 1,
+                              kDefaultBudget);
         }
     }
     if (fail_code && lane == 0) *(volatile int *)args.err = fail_code;
