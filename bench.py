@@ -426,11 +426,16 @@ def run_ours(args):
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
+    # the mixed bi-Lanczos step runs L q and L^T p as one two-perturbation call
+    # (one launch of each GEMM stage for both); the profiled run made
+    # 2 n_run applications
+    pair = prec_name == "mixed" and os.environ.get("TDSCHA_PAIR_APPLY", "1") != "0"
+    ppl = 2 if pair else 1                  # perturbations per GEMM-stage launch
     if kid is not None:
         tot_ms, cnt = kern[kid]
         per_launch_s = tot_ms / cnt / 1e3
         if kid in (0, 3):
-            work = 2.0 * R * M * M           # flops per launch of one GEMM stage
+            work = 2.0 * R * M * M * ppl     # flops per launch of one GEMM stage
             achieved = work / per_launch_s / 1e12
             if prec_name == "fp64":
                 peak, src = 1.25, "nominal GB300 FP64 1.25 TFLOP/s (not in MEASURED_PEAKS.json)"
@@ -445,11 +450,13 @@ def run_ours(args):
                 # three tensor products per K step (hi*hi, hi*lo, lo*hi) on the
                 # padded mode count: the tensor-pipe work behind `achieved`
                 Mp = ((M + 63) // 64) * 64
-                roof["tensor_work_incl_split_tflops"] = 3 * 2.0 * R * Mp * Mp / per_launch_s / 1e12
+                roof["tensor_work_incl_split_tflops"] = 3 * 2.0 * R * Mp * Mp * ppl / per_launch_s / 1e12
                 roof["frac_incl_split"] = roof["tensor_work_incl_split_tflops"] / peak
                 # DRAM bytes per launch from the ncu captures of the same kernels
-                # at N=20 000 (profiles/k_stageA_stageB_m573_n20k.md), scaled by rows
-                per_row = {0: 147.2e6 / 20000, 3: 97.4e6 / 20000}[kid]
+                # at N=20 000 (profiles/k_stageA_stageB_m573_n20k.md; one- and
+                # two-perturbation launches), scaled by rows
+                per_row = ({0: 147.2e6 / 20000, 3: 97.4e6 / 20000} if ppl == 1 else
+                           {0: 252.26e6 / 20000, 3: 163.46e6 / 20000})[kid]
                 if M == 573 and S == 1:
                     roof["traffic"] = per_row * R
                     roof["traffic_unit"] = "bytes per launch (ncu, scaled from N=20000)"
@@ -461,20 +468,28 @@ def run_ours(args):
             roof = {"bound": "hbm", "kernel": KERNEL_NAMES[kid], "achieved": achieved, "peak": peak,
                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                     "avg_launch_ms": tot_ms / cnt}
-    kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1]}
+    kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1],
+                                 "perturbations_per_launch": ppl if k != 4 else 1}
                for k, v in kern.items()}
     # kernels launched per Lanczos step.  One application: the averages and
     # the assemble (mixed: Y1 limbs read straight from psi, stage A, row
     # scalars, W build, stage B, finalisation; float64: psi unpack, stage A,
     # row scalars, force average, stage B, finalisation; with images on the
-    # perturbation side the finalisation is two kernels and the float64 path
+    # perturbation side the finalisation is three kernels and the float64 path
     # adds the image vectors and matrices).  Recurrence: dot + a, residuals,
     # b/c, normalisation, and with re-biorthogonalisation the dots,
-    # coefficients, apply and weight (one apply pass per 2048 stored vectors,
+    # coefficients, update and weight (one update pass per 1024 stored pairs,
     # here always one).
-    per_app = 1 + 6 + (1 if n_img > 1 else 0) + (2 if n_img > 1 and prec_name == "fp64" else 0)
+    per_app = 7 + (2 if n_img > 1 else 0) + (2 if n_img > 1 and prec_name == "fp64" else 0)
+    if pair:
+        # one call for both: Y1 preparation and finalisation per perturbation,
+        # stage A, row scalars, W build and stage B once, then two assembles
+        fin = 3 if n_img > 1 else 1
+        per_step_ops = 2 + 4 + 2 * fin + 2
+    else:
+        per_step_ops = 2 * per_app
     per_step_rec = 5 + (4 if not args.no_reorth else 0)
-    gpu_launches = K * n_run * (2 * per_app + per_step_rec)
+    gpu_launches = K * n_run * (per_step_ops + per_step_rec)
 
     # float64 arm of the metric (same GPU, same runs) and the accuracy check
     fp64 = None

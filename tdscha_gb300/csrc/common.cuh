@@ -116,6 +116,7 @@ struct tdscha_ctx {
     double *pc = nullptr;       // 10 arrays of H: see lanczos.cu
     // per-application scratch (device)
     double *R1 = nullptr, *Y1 = nullptr, *f = nullptr, *d2v = nullptr;
+    double *f2 = nullptr, *d2v2 = nullptr;   // second output of a two-perturbation call
     double *qp_part = nullptr;  // fp64 path: nct x 2 x R
     double *alpha = nullptr, *beta = nullptr, *c1 = nullptr, *c2 = nullptr;   // R each
     double *gpart = nullptr;    // fp64 path: nsplit x M x M
@@ -197,6 +198,11 @@ int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st);
 // (plain layout, or the transposed one with its per-pair factors cty / ctra)
 int perturb_mixed_psi(tdscha_ctx *c, int apply_d4, const double *psi, const double *cty,
                       const double *ctra, cudaStream_t st);
+// The two applications of a bi-Lanczos step in one call: perturbation a from
+// psi_a in the plain layout, b from psi_b in the transposed one (per-pair
+// factors cty, ctra); results in (f, d2v) and (f2, d2v2).
+int perturb_mixed_pair(tdscha_ctx *c, int apply_d4, const double *psi_a, const double *psi_b,
+                       const double *cty, const double *ctra, cudaStream_t st);
 int mixed_check_error(tdscha_ctx *c);
 // the autotuner's choice: stage A kernel (1: one accumulator per 128 x 192
 // tile), stage B split count, and the timed application (ms; 0: not tuned)
@@ -226,7 +232,8 @@ int psi_perturbation64(tdscha_ctx *c, cudaStream_t st);
 int psi_finalize64(tdscha_ctx *c, const double *gpart, int nsplit, long sstride, long jstride,
                    long lda, const double *fpart, int nfchunk, cudaStream_t st);
 int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, long jstride,
-                   long lda, const float *fpart, int nfchunk, cudaStream_t st);
+                   long lda, const float *fpart, int nfchunk, double *f_out, double *d2v_out,
+                   cudaStream_t st);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 

@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstring>
 
+#include <list>
 #include <map>
 #include <mutex>
 #include <unordered_map>
@@ -95,12 +96,28 @@ static void prof_clear(tdscha_ctx *c) {
 }
 
 namespace {
+// Freed blocks are kept for reuse by exact size; past the cap the blocks freed
+// longest ago are released first (the block just freed is the one a repeated
+// context of the same shape asks for next).
 struct BlockCache {
+    struct Idle {
+        int dev;
+        size_t bytes;
+        void *p;
+    };
     std::mutex mu;
     std::unordered_map<void *, std::pair<int, size_t>> live;   // block -> (device, bytes)
-    std::multimap<std::pair<int, size_t>, void *> idle;        // (device, bytes) -> block
+    std::list<Idle> order;                                     // idle blocks, oldest first
+    std::multimap<std::pair<int, size_t>, std::list<Idle>::iterator> idle;
     size_t idle_bytes = 0;
 };
+void free_on_device(int dev, void *p) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (dev != cur) cudaSetDevice(dev);
+    cudaFree(p);
+    if (dev != cur) cudaSetDevice(cur);
+}
 BlockCache &block_cache() {
     static BlockCache *bc = new BlockCache();   // never destroyed: no cudaFree at exit
     return *bc;
@@ -126,7 +143,8 @@ cudaError_t tdscha::cached_malloc(void **p, size_t bytes) {
     std::lock_guard<std::mutex> lock(bc.mu);
     auto it = bc.idle.find({dev, bytes});
     if (it != bc.idle.end()) {
-        *p = it->second;
+        *p = it->second->p;
+        bc.order.erase(it->second);
         bc.idle.erase(it);
         bc.idle_bytes -= bytes;
         bc.live[*p] = {dev, bytes};
@@ -135,7 +153,8 @@ cudaError_t tdscha::cached_malloc(void **p, size_t bytes) {
     e = cudaMalloc(p, bytes);
     if (e == cudaErrorMemoryAllocation && !bc.idle.empty()) {
         cudaGetLastError();
-        for (auto &kv : bc.idle) cudaFree(kv.second);
+        for (auto &b : bc.order) free_on_device(b.dev, b.p);
+        bc.order.clear();
         bc.idle.clear();
         bc.idle_bytes = 0;
         e = cudaMalloc(p, bytes);
@@ -155,11 +174,26 @@ void tdscha::cached_free(void *p) {
     }
     auto key = it->second;
     bc.live.erase(it);
-    if (bc.idle_bytes + key.second > cache_cap()) {
-        cudaFree(p);
+    const size_t cap = cache_cap();
+    if (key.second > cap) {
+        free_on_device(key.first, p);
         return;
     }
-    bc.idle.insert({key, p});
+    // release the blocks freed longest ago until this one fits
+    while (!bc.order.empty() && bc.idle_bytes + key.second > cap) {
+        BlockCache::Idle &old = bc.order.front();
+        auto range = bc.idle.equal_range({old.dev, old.bytes});
+        for (auto r = range.first; r != range.second; ++r)
+            if (r->second == bc.order.begin()) {
+                bc.idle.erase(r);
+                break;
+            }
+        bc.idle_bytes -= old.bytes;
+        free_on_device(old.dev, old.p);
+        bc.order.pop_front();
+    }
+    bc.order.push_back({key.first, key.second, p});
+    bc.idle.insert({key, std::prev(bc.order.end())});
     bc.idle_bytes += key.second;
 }
 
@@ -169,15 +203,11 @@ extern "C" int tdscha_release_cached_memory(unsigned long long *bytes) {
     BlockCache &bc = block_cache();
     std::lock_guard<std::mutex> lock(bc.mu);
     unsigned long long freed = 0;
-    int cur = 0;
-    cudaGetDevice(&cur);
-    for (auto &kv : bc.idle) {
-        // each block is freed on the device it was allocated on
-        if (kv.first.first != cur) cudaSetDevice(kv.first.first);
-        cudaFree(kv.second);
-        if (kv.first.first != cur) cudaSetDevice(cur);
-        freed += kv.first.second;
+    for (auto &b : bc.order) {
+        free_on_device(b.dev, b.p);   // on the device it was allocated on
+        freed += b.bytes;
     }
+    bc.order.clear();
     bc.idle.clear();
     bc.idle_bytes = 0;
     if (bytes) *bytes = freed;
@@ -197,6 +227,8 @@ static void ctx_free(tdscha_ctx *c) {
     cached_free(c->tri);
     cached_free(c->lam_static);
     cached_free(c->vsplit);
+    cached_free(c->f2);
+    cached_free(c->d2v2);
     free_translations(c);
     psi_free(c);
     if (c->host_pinned) cudaFreeHost(c->host_pinned);

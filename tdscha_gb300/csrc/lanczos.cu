@@ -10,6 +10,7 @@
 //     deterministic block-partial dot products;
 //   * the continued fraction (:5032-5162), one thread per frequency.
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -277,6 +278,39 @@ int apply_full_L_dev(tdscha_ctx *c, const double *psi_in, double *psi_out, int t
         TDS_CUDA(launch_assemble<ASM_PLAIN>(nb, st, c->reverse_L, psi_in, c->f, c->d2v, c->pc, c->tri, c->w,
                                    c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic, with_anh,
                                    c->shift, psi_out));
+    return TDSCHA_OK;
+}
+
+// L q and L^T p of a bi-Lanczos step.  On the tensor-core path (normal
+// representation, anharmonic part on, no translation projection) both
+// perturbation averages run as one two-perturbation call (perturb_mixed_pair:
+// the ensemble read once, one launch per kernel for both) and give the bits of
+// two separate applications; otherwise, or with TDSCHA_PAIR_APPLY=0 in the
+// environment, two applications.
+static bool pair_apply_enabled() {
+    const char *e = getenv("TDSCHA_PAIR_APPLY");
+    return !(e && atoi(e) == 0);
+}
+
+int apply_full_L_pair_dev(tdscha_ctx *c, const double *q, const double *p, double *Lq,
+                          double *pL, int precision, cudaStream_t st) {
+    const bool pair = pair_apply_enabled() && precision == TDSCHA_PREC_MIXED && c->with_mixed &&
+                      !c->use_wigner && !c->ignore_v3 && c->tr_ntrans == 0 && c->f2;
+    if (!pair) {
+        TDS_TRY(apply_full_L_dev(c, q, Lq, 0, precision, st));
+        return apply_full_L_dev(c, p, pL, 1, precision, st);
+    }
+    const long H = c->H;
+    const int M = c->M;
+    TDS_TRY(perturb_mixed_pair(c, c->ignore_v4 ? 0 : 1, q, p, c->pc + PC_TY * H,
+                               c->pc + PC_TRA * H, st));
+    const int nb = std::max(1, std::min(ceil_div(M + H, 256), 4096));
+    TDS_CUDA(launch_assemble<ASM_PLAIN>(nb, st, c->reverse_L, q, c->f, c->d2v, c->pc, c->tri, c->w,
+                                        c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic, 1,
+                                        c->shift, Lq));
+    TDS_CUDA(launch_assemble<ASM_TRANSPOSE>(nb, st, c->reverse_L, p, c->f2, c->d2v2, c->pc, c->tri,
+                                            c->w, c->Yw, c->Ywinv, c->ReAw, M, H,
+                                            c->ignore_harmonic, 1, c->shift, pL));
     return TDSCHA_OK;
 }
 
@@ -1156,10 +1190,11 @@ static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, long ld, i
     // elementwise passes over the vectors and the basis: eight blocks per SM
     const int nbw = std::max(1, std::min(ceil_div(P, kDotThreads), 1216));
     double *q = basis_Q + (long)k * ld, *p = basis_P + (long)k * ld;
-    TDS_TRY(apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st));
     const double *pL = ctx->Lq;
-    if (!run_simm) {
-        TDS_TRY(apply_full_L_dev(ctx, p, ctx->pL, 1, precision, st));
+    if (run_simm) {
+        TDS_TRY(apply_full_L_dev(ctx, q, ctx->Lq, 0, precision, st));
+    } else {
+        TDS_TRY(apply_full_L_pair_dev(ctx, q, p, ctx->Lq, ctx->pL, precision, st));
         pL = ctx->pL;
     }
     launch_pdl(k_dot1, nb, kDotThreads, 0, st, p, ctx->Lq, mask, P, ctx->dots);

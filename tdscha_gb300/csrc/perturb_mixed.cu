@@ -892,7 +892,7 @@ struct StageBArgs {
     int ldGb;             // columns of a partial tile (ntile_b x 128)
     int JMp;              // J x Mp
     long nitems;          // ntile x ntile_b x nsplit
-    const float *su, *sw; // row scales of U^T and W^T (Mp; W^T row j*Mp + b uses sw[b])
+    const float *su, *sw; // row scales of U^T (Mp) and W^T (J x Mp, per image)
     float *gpart;         // [nsplit][ldG][ldGb]
     int *err;
     long long budget;
@@ -1032,7 +1032,7 @@ __global__ void __launch_bounds__(192, 1) k_stageB_tc(const __grid_constant__ Tm
             float *cv = colv + j * kBNB;
             {
                 int c = brow + row_in;
-                cv[row_in] = c < args.JMp ? args.sw[c % args.Mp] : 0.f;
+                cv[row_in] = c < args.JMp ? args.sw[c] : 0.f;
             }
             const int a = arow + row_in;
             const float sa = a < args.Mp ? args.su[a] : 0.f;
@@ -1330,21 +1330,24 @@ __global__ void k_prep_y1_img(const Src src, const int *__restrict__ sc_idx,
         tcol[row] = n < M ? t : 0.f;
         vs[row] = n < M ? (float)a : 0.f;
         vt[row] = n < M ? (float)(b / fpsi[n]) : 0.f;
-        if (row == 0) { absmax[0] = 0.f; absmax[1] = 0.f; }
+        if (n == 0) { absmax[2 * j] = 0.f; absmax[2 * j + 1] = 0.f; }   // per image
     }
 }
 
 // Row scalars from the stage A partials (sums in float64), and max |alpha|,
-// max |beta| for the W scales.  Row r = j*Nr + i: configuration row i of
-// perturbation image j (J = 1: the image rows themselves, i = r).
-__global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long Nr, int J, int rho_div,
+// max |beta| of each perturbation image for its W scales.  Block
+// (x, image j) takes rows r = j*Nr + i of configuration rows i (J = 1: the
+// image rows themselves, i = r).
+__global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long Nr, int rho_div,
                              const double *__restrict__ rho, int apply_d4,
                              float4 *__restrict__ abcc, float *__restrict__ absmax) {
     pdl_enter();
-    long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long jj = blockIdx.y;
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long r = jj * Nr + i;
+    absmax += 2 * jj;
     float ma = 0.f, mb = 0.f;
-    if (r < (long)J * Nr) {
-        const long jj = r / Nr, i = r - jj * Nr;
+    if (i < Nr) {
         const float *base = qpst + jj * nct * 4 * Nr;
         double q = 0, p = 0, s = 0, t = 0;
         for (int ct = 0; ct < nct; ++ct) {
@@ -1389,12 +1392,12 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long Nr, i
 }
 
 // W^T[b][r] = (alpha_r F^T[b][r] + beta_r/2 U^T[b][r]) / sw_b as fp16 limbs,
-// sw_b = max|alpha| fmax_b + max|beta|/2 su_b; and the force-average partials
+// sw_b = max|alpha| fmax_b + max|beta|/2 su_b (maxima of the image); and the force-average partials
 // fpart[chunk][b] = sum_r c1_r F^T[b][r] + c2_r U^T[b][r].
 constexpr int kWRows = 8;      // b rows per block
 constexpr int kWChunk = 2048;  // r per block (256 threads x 4 r x 2 passes)
-// blockIdx.z = j: row scalars of perturbation image j (at j*R), W^T rows at
-// j*Mp, force partials at j*nchunk*M.
+// blockIdx.z = j: row scalars of perturbation image j (at j*R), its maxima at
+// 2j, W^T rows and scales at j*Mp, force partials at j*nchunk*M.
 __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
                                                 const float *__restrict__ ut32,
                                                 const float4 *__restrict__ abcc,
@@ -1410,6 +1413,8 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
     wt_hi += (long)blockIdx.z * Mp * Rp;
     wt_lo += (long)blockIdx.z * Mp * Rp;
     fpart += (long)blockIdx.z * gridDim.y * M;
+    absmax += 2 * blockIdx.z;
+    sw_out += (long)blockIdx.z * Mp;
     __shared__ float red[kWRows][8];
     int b0 = blockIdx.x * kWRows;
     long r0 = (long)blockIdx.y * kWChunk;
@@ -1422,7 +1427,7 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
         if (!(sw > 0.f)) sw = 1.f;
         inv[k] = 1.f / sw;
         facc[k] = 0.f;
-        if (blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
+        if (blockIdx.y == 0 && threadIdx.x == 0 && b < M) sw_out[b] = sw;
     }
     // Rp is a multiple of 64 and r0 of 2048, so each 4-group is in bounds of
     // the padded rows; rows r >= R carry alpha = beta = c1 = c2 = 0 there.
@@ -1477,7 +1482,8 @@ __global__ void __launch_bounds__(256) k_wbuild(const float *__restrict__ ft32,
 // compensated fp32 sum over the splits in split order, and
 // d2v[a][b] = d2v[b][a] = -(G[a][b] + G[b][a]) / norm is written without a
 // float64 G round trip.  Blocks with A = 0 also finish f for the columns of
-// tile B.
+// tile B.  G_s[a][b] = gpart[s * stride + a * lda + b] (one image's columns of
+// the partial tiles).
 __device__ __forceinline__ double gsum_one(const float *__restrict__ g, int nsplit, long stride) {
     float sum = 0.f, comp = 0.f;
     int s = 0;
@@ -1504,8 +1510,9 @@ __device__ __forceinline__ double gsum_one(const float *__restrict__ g, int nspl
 }
 
 __global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart, int nsplit,
-                                                int ldG, int M, const float *__restrict__ fpart,
-                                                int nfchunk, double norm, double *__restrict__ f,
+                                                long lda, long stride, int M,
+                                                const float *__restrict__ fpart, int nfchunk,
+                                                double norm, double *__restrict__ f,
                                                 double *__restrict__ d2v) {
     pdl_enter();
     __shared__ double tr[32][9];    // G over rows b of tile B, the slab's 8 columns a: [b][a]
@@ -1521,7 +1528,6 @@ __global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart,
     }
     const int B = A + rem;
     const double inv = 1.0 / norm;
-    const long stride = (long)ldG * ldG;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 x 32
     const int a0 = A * 32 + slab * 8, b0 = B * 32;
     {
@@ -1529,13 +1535,13 @@ __global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart,
         // along a, so that a warp reads 4 rows x 8 consecutive floats (4 sectors)
         int ao = threadIdx.x & 7, bo = threadIdx.x >> 3;
         int b = b0 + bo, a = a0 + ao;
-        tr[bo][ao] = (a < M && b < M) ? gsum_one(gpart + (long)b * ldG + a, nsplit, stride) : 0.0;
+        tr[bo][ao] = (a < M && b < M) ? gsum_one(gpart + (long)b * lda + a, nsplit, stride) : 0.0;
     }
     __syncthreads();
     {
         int a = a0 + ty, b = b0 + tx;                         // G[a][b], coalesced in b
         if (a < M && b < M) {
-            double v = -(gsum_one(gpart + (long)a * ldG + b, nsplit, stride) + tr[tx][ty]) * inv;
+            double v = -(gsum_one(gpart + (long)a * lda + b, nsplit, stride) + tr[tx][ty]) * inv;
             d2v[(long)a * M + b] = v;
             if (A != B) d2v[(long)b * M + a] = v;
         }
@@ -1625,6 +1631,7 @@ struct MixedExtra {
     int nfchunk = 0;
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
     int ntBb = 0, ldGb = 0;   // stage B tiles / columns along the J x Mp rows of W^T
+    int jmax = 1;             // images the per-call buffers hold: 2 J (two perturbations)
     int one_acc = 0;          // stage A with one accumulator per 128 x 192 tile
     double tuned_ms = 0;      // autotuner: time of one application with the chosen shape
     int force_acc = -1;       // TDSCHA_STAGEA_ACC: the stage A kernel fixed by the environment
@@ -1806,6 +1813,11 @@ int mixed_prepare(tdscha_ctx *c) {
     x->split_cands = split_cands;
     const int nsplit_max = *std::max_element(split_cands.begin(), split_cands.end());
     x->nfchunk = ceil_div(R, kWChunk);
+    // the per-call buffers hold the images of two perturbations (the L and
+    // L^T applications of a bi-Lanczos step in one call)
+    const int Jm = 2 * J;
+    x->jmax = Jm;
+    const int ldGb_max = ceil_div((long)Jm * Mp, kBNB) * kBNB;
     size_t rowN = (size_t)R * Mp, colN = (size_t)Mp * Rp;
     TDS_CUDA(cached_malloc(&mx.d_hi, 2 * rowN));
     TDS_CUDA(cached_malloc(&mx.d_lo, 2 * rowN));
@@ -1815,24 +1827,26 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cached_malloc(&mx.ut_lo, 2 * colN));
     TDS_CUDA(cached_malloc(&mx.ut32, 4 * colN));
     TDS_CUDA(cached_malloc(&mx.ft32, 4 * colN));
-    TDS_CUDA(cached_malloc(&mx.wt_hi, 2 * (size_t)J * colN));
-    TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * (size_t)J * colN));
-    TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)J * Mp * Mp));
-    TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)J * Mp * Mp));
-    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * nct_max * (size_t)J * R));
-    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)nsplit_max * x->ldG * x->ldGb));
-    float **vecs[] = {&x->sd, &x->fmx, &x->su, &x->sw};
+    TDS_CUDA(cached_malloc(&mx.wt_hi, 2 * (size_t)Jm * colN));
+    TDS_CUDA(cached_malloc(&mx.wt_lo, 2 * (size_t)Jm * colN));
+    TDS_CUDA(cached_malloc(&mx.y1_hi, 2 * (size_t)Jm * Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.y1_lo, 2 * (size_t)Jm * Mp * Mp));
+    TDS_CUDA(cached_malloc(&mx.qp, sizeof(float) * 4 * nct_max * (size_t)Jm * R));
+    TDS_CUDA(cached_malloc(&mx.gpart, sizeof(float) * (size_t)nsplit_max * x->ldG * ldGb_max));
+    float **vecs[] = {&x->sd, &x->fmx, &x->su};
     for (float **v : vecs) TDS_CUDA(cached_malloc(v, sizeof(float) * Mp));
-    float **jvecs[] = {&x->tcol, &x->vs, &x->vt};
-    for (float **v : jvecs) TDS_CUDA(cached_malloc(v, sizeof(float) * (size_t)J * Mp));
-    TDS_CUDA(cached_malloc(&x->absmax, sizeof(float) * 2));
-    TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * (size_t)J * R));
-    TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)J * x->nfchunk * M));
+    float **jvecs[] = {&x->tcol, &x->vs, &x->vt, &x->sw};
+    for (float **v : jvecs) TDS_CUDA(cached_malloc(v, sizeof(float) * (size_t)Jm * Mp));
+    TDS_CUDA(cached_malloc(&x->absmax, sizeof(float) * 2 * Jm));
+    TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * (size_t)Jm * R));
+    TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)Jm * x->nfchunk * M));
+    TDS_CUDA(cached_malloc(&c->f2, sizeof(double) * M));
+    TDS_CUDA(cached_malloc(&c->d2v2, sizeof(double) * (size_t)M * M));
     TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
     *mx.err_flag = 0;
-    TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * (size_t)J * colN));
-    TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * (size_t)J * colN));
-    TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * Mp));
+    TDS_CUDA(cudaMemset(mx.wt_hi, 0, 2 * (size_t)Jm * colN));
+    TDS_CUDA(cudaMemset(mx.wt_lo, 0, 2 * (size_t)Jm * colN));
+    TDS_CUDA(cudaMemset(x->sw, 0, sizeof(float) * (size_t)Jm * Mp));
     {
         float *dmax = nullptr;
         double *rsc = nullptr;   // 1 / sd and 1 / su in float64 (Mp each)
@@ -1862,15 +1876,15 @@ int mixed_prepare(tdscha_ctx *c) {
     }
     TDS_TRY(make_map(&x->tmA.a_hi, mx.d_hi, Mp, R, kBM));
     TDS_TRY(make_map(&x->tmA.a_lo, mx.d_lo, Mp, R, kBM));
-    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, std::min(kPBN, Mp)));
-    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, std::min(kPBN, Mp)));
+    TDS_TRY(make_map(&x->tmA.b_hi, mx.y1_hi, Mp, (uint64_t)Jm * Mp, std::min(kPBN, Mp)));
+    TDS_TRY(make_map(&x->tmA.b_lo, mx.y1_lo, Mp, (uint64_t)Jm * Mp, std::min(kPBN, Mp)));
     x->tmA1 = x->tmA;
-    TDS_TRY(make_map(&x->tmA1.b_hi, mx.y1_hi, Mp, (uint64_t)J * Mp, std::min(kRBN, Mp)));
-    TDS_TRY(make_map(&x->tmA1.b_lo, mx.y1_lo, Mp, (uint64_t)J * Mp, std::min(kRBN, Mp)));
+    TDS_TRY(make_map(&x->tmA1.b_hi, mx.y1_hi, Mp, (uint64_t)Jm * Mp, std::min(kRBN, Mp)));
+    TDS_TRY(make_map(&x->tmA1.b_lo, mx.y1_lo, Mp, (uint64_t)Jm * Mp, std::min(kRBN, Mp)));
     TDS_TRY(make_map(&x->tmB.a_hi, mx.ut_hi, Rp, Mp, kBM));
     TDS_TRY(make_map(&x->tmB.a_lo, mx.ut_lo, Rp, Mp, kBM));
-    TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, (uint64_t)J * Mp, kBNB));
-    TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, (uint64_t)J * Mp, kBNB));
+    TDS_TRY(make_map(&x->tmB.b_hi, mx.wt_hi, Rp, (uint64_t)Jm * Mp, kBNB));
+    TDS_TRY(make_map(&x->tmB.b_lo, mx.wt_lo, Rp, (uint64_t)Jm * Mp, kBNB));
     TDS_TRY(make_map_f32(&x->te.d, x->d32, Mp, R));
     TDS_TRY(make_map_f32(&x->te.g, mx.g32, Mp, R));
     static bool attr_done = false;
@@ -1924,59 +1938,84 @@ int mixed_check_error(tdscha_ctx *c) {
     return TDSCHA_OK;
 }
 
-static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
+static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc, int nsrc,
                              cudaStream_t st);
 
 int perturb_mixed(tdscha_ctx *c, int apply_d4, cudaStream_t st) {
-    return perturb_mixed_src(c, apply_d4, nullptr, st);
+    return perturb_mixed_src(c, apply_d4, nullptr, 1, st);
 }
 
 int perturb_mixed_psi(tdscha_ctx *c, int apply_d4, const double *psi, const double *cty,
                       const double *ctra, cudaStream_t st) {
     Y1FromPsi src{psi, cty, ctra, c->M, c->H, c->ignore_v3};
-    return perturb_mixed_src(c, apply_d4, &src, st);
+    return perturb_mixed_src(c, apply_d4, &src, 1, st);
 }
 
-static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
+int perturb_mixed_pair(tdscha_ctx *c, int apply_d4, const double *psi_a, const double *psi_b,
+                       const double *cty, const double *ctra, cudaStream_t st) {
+    Y1FromPsi src[2] = {{psi_a, nullptr, nullptr, c->M, c->H, c->ignore_v3},
+                        {psi_b, cty, ctra, c->M, c->H, c->ignore_v3}};
+    return perturb_mixed_src(c, apply_d4, src, 2, st);
+}
+
+// One tensor-core call for nsrc perturbations (1, or 2: the L and L^T
+// applications of a bi-Lanczos step) with J symmetry images each: the images
+// of perturbation s are s*J .. s*J + J - 1 in every per-call buffer, so stage A
+// reads the ensemble once for all of them and every other kernel runs once over
+// all images.  Each image has its own W scales, so the results of a
+// two-perturbation call are those of two one-perturbation calls, bit for bit.
+// psrc == nullptr: one perturbation from the Y1 and R1 buffers.
+static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc, int nsrc,
                              cudaStream_t st) {
     MixedStore &mx = c->mx;
     MixedExtra *x = extra(c);
     if (!x) { set_error("mixed store not prepared"); return TDSCHA_ERR_STATE; }
     const int M = c->M, Mp = mx.Mp, J = c->J;
+    const int Jb = nsrc * J;   // images in this call
+    if (Jb > x->jmax || (nsrc > 1 && !psrc)) { set_error("mixed call: bad perturbation count"); return TDSCHA_ERR_ARG; }
     const long R = c->Nrows, Rp = mx.Rp;
+    const int ntBb = (int)ceil_div((long)Jb * Mp, kBNB), ldGb = ntBb * kBNB;
     int *err_dev = nullptr;
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
-    if (J > 1) {
-        // perturbation-side symmetry images: Y1_j = S_j^T Y1 S_j for every j
+    {
         ProfScope ps(c, 5, st);
-        const size_t sm = sizeof(float) * Mp;
-        if (psrc)
-            TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, J * Mp, 256, sm, st, *psrc, c->sc_idx,
-                                c->sc_val, c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi,
-                                mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
-        else
-            TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st,
-                                Y1FromBuffers{c->Y1, c->R1, M}, c->sc_idx, c->sc_val, c->maxdeg,
-                                c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs,
-                                x->vt, x->absmax));
-    } else {
-        ProfScope ps(c, 5, st);
-        if (psrc)
-            TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, *psrc, c->fY, c->fpsi, x->sd,
-                                M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
-        else
-            TDS_CUDA(launch_pdl(k_prep_y1<Y1FromBuffers>, Mp, 256, 0, st,
-                                Y1FromBuffers{c->Y1, c->R1, M}, c->fY, c->fpsi, x->sd, M, Mp,
-                                mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
+        for (int sidx = 0; sidx < nsrc; ++sidx) {
+            // perturbation sidx: Y1 limbs of its J images, the epilogue vectors
+            // and its W-scale maxima at image offset sidx * J
+            const long io = (long)sidx * J;
+            __half *yh = mx.y1_hi + io * Mp * Mp, *yl = mx.y1_lo + io * Mp * Mp;
+            float *tc = x->tcol + io * Mp, *vs = x->vs + io * Mp, *vt = x->vt + io * Mp;
+            float *am = x->absmax + 2 * io;
+            if (J > 1) {
+                const size_t sm = sizeof(float) * Mp;
+                if (psrc)
+                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, J * Mp, 256, sm, st, psrc[sidx],
+                                        c->sc_idx, c->sc_val, c->maxdeg, c->fY, c->fpsi, x->sd, M,
+                                        Mp, yh, yl, tc, vs, vt, am));
+                else
+                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st,
+                                        Y1FromBuffers{c->Y1, c->R1, M}, c->sc_idx, c->sc_val,
+                                        c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, yh, yl, tc, vs,
+                                        vt, am));
+            } else {
+                if (psrc)
+                    TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, psrc[sidx], c->fY,
+                                        c->fpsi, x->sd, M, Mp, yh, yl, tc, vs, vt, am));
+                else
+                    TDS_CUDA(launch_pdl(k_prep_y1<Y1FromBuffers>, Mp, 256, 0, st,
+                                        Y1FromBuffers{c->Y1, c->R1, M}, c->fY, c->fpsi, x->sd, M,
+                                        Mp, yh, yl, tc, vs, vt, am));
+            }
+        }
     }
     StageAArgs ga{};
     ga.R = R;
     ga.Mp = Mp;
     ga.nkb = Mp / kPBK;
     ga.nct = mx.nctile;
-    ga.J = J;
+    ga.J = Jb;
     ga.b_box = x->bnA;
-    ga.ntiles = (long)ceil_div(R, kBM) * J * mx.nctile;
+    ga.ntiles = (long)ceil_div(R, kBM) * Jb * mx.nctile;
     ga.tcol = x->tcol;
     ga.vec_s = x->vs;
     ga.vec_t = x->vt;
@@ -1993,12 +2032,12 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     }
     {
         ProfScope ps(c, 1, st);
-        TDS_CUDA(launch_pdl(k_rows_mixed, ceil_div((long)J * R, 128), 128, 0, st, mx.qp,
-                            mx.nctile, R, J, c->rho_div, c->rho, apply_d4, x->abcc, x->absmax));
+        TDS_CUDA(launch_pdl(k_rows_mixed, dim3(ceil_div(R, 128), Jb), 128, 0, st, mx.qp,
+                            mx.nctile, R, c->rho_div, c->rho, apply_d4, x->abcc, x->absmax));
     }
     {
         ProfScope ps(c, 2, st);
-        dim3 g(ceil_div(M, kWRows), x->nfchunk, J);
+        dim3 g(ceil_div(M, kWRows), x->nfchunk, Jb);
         TDS_CUDA(launch_pdl(k_wbuild, g, 256, 0, st, mx.ft32, mx.ut32, x->abcc, x->absmax, x->fmx,
                             x->su, R, Rp, M, Mp, mx.wt_hi, mx.wt_lo, x->sw, x->fpart));
     }
@@ -2008,10 +2047,10 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     gb.Mp = Mp;
     gb.ldG = x->ldG;
     gb.ntile = x->ntB;
-    gb.ntile_b = x->ntBb;
-    gb.ldGb = x->ldGb;
-    gb.JMp = J * Mp;
-    gb.nitems = (long)x->ntB * x->ntBb * mx.nsplit;
+    gb.ntile_b = ntBb;
+    gb.ldGb = ldGb;
+    gb.JMp = Jb * Mp;
+    gb.nitems = (long)x->ntB * ntBb * mx.nsplit;
     gb.su = x->su;
     gb.sw = x->sw;
     gb.gpart = mx.gpart;
@@ -2022,14 +2061,22 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
         int grid = (int)std::min<long>(gb.nitems, x->nsm);
         TDS_CUDA(launch_pdl(k_stageB_tc, grid, 192, kQSmem, st, x->tmB, gb));
     }
-    if (J > 1)
-        return psi_finalize32(c, mx.gpart, mx.nsplit, (long)x->ldG * x->ldGb, Mp, x->ldGb,
-                              x->fpart, x->nfchunk, st);
-    {
+    const long sstride = (long)x->ldG * ldGb;
+    for (int sidx = 0; sidx < nsrc; ++sidx) {
+        double *f_out = sidx ? c->f2 : c->f, *d2v_out = sidx ? c->d2v2 : c->d2v;
+        const long io = (long)sidx * J;
+        const float *gp = mx.gpart + io * Mp;                  // its images' columns
+        const float *fp = x->fpart + io * x->nfchunk * M;
+        if (J > 1) {
+            TDS_TRY(psi_finalize32(c, gp, mx.nsplit, sstride, Mp, ldGb, fp, x->nfchunk, f_out,
+                                   d2v_out, st));
+            continue;
+        }
         ProfScope ps(c, 4, st);
         const int nt = ceil_div(M, 32);
-        TDS_CUDA(launch_pdl(k_gfinal, 4 * (nt * (nt + 1) / 2), 256, 0, st, mx.gpart, mx.nsplit,
-                            x->ldG, M, x->fpart, x->nfchunk, c->sum_rho * c->S, c->f, c->d2v));
+        TDS_CUDA(launch_pdl(k_gfinal, 4 * (nt * (nt + 1) / 2), 256, 0, st, gp, mx.nsplit,
+                            (long)ldGb, sstride, M, fp, x->nfchunk, c->sum_rho * c->S, f_out,
+                            d2v_out));
     }
     return TDSCHA_OK;
 }

@@ -431,7 +431,8 @@ int psi_finalize64(tdscha_ctx *c, const double *gpart, int nsplit, long sstride,
 }
 
 int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, long jstride,
-                   long lda, const float *fpart, int nfchunk, cudaStream_t st) {
+                   long lda, const float *fpart, int nfchunk, double *f_out, double *d2v_out,
+                   cudaStream_t st) {
     const int M = c->M, J = c->J;
     const size_t JMM = (size_t)J * M * M, JM = (size_t)J * M;
     // the float64 layout of hs, tj, fs, tf holds the double-float pairs
@@ -446,7 +447,7 @@ int psi_finalize32(tdscha_ctx *c, const float *gpart, int nsplit, long sstride, 
                                                            c->maxdeg, tj, tf);
     TDS_CHECK_LAUNCH();
     k_psi_jsum_df<<<std::max(1, ceil_div((long)M * M, 64)), dim3(64, 4), 0, st>>>(
-        tj, tf, J, M, 1.0 / (c->sum_rho * c->S), c->f, c->d2v);
+        tj, tf, J, M, 1.0 / (c->sum_rho * c->S), f_out, d2v_out);
     TDS_CHECK_LAUNCH();
     return TDSCHA_OK;
 }

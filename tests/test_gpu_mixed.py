@@ -188,3 +188,30 @@ def test_autotuner_choice_is_cached_and_accurate(gpu_lib):
     assert rel(fa, f_ref) <= TOL_CALL and rel(da, d_ref) <= TOL_CALL
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("M,N,S", [(96, 3000, 1), (97, 2000, 1), (24, 400, 48)])
+def test_pair_application_bitwise(gpu_lib, monkeypatch, M, N, S):
+    """A mixed bi-Lanczos step runs L q and L^T p as one two-perturbation call
+    (each perturbation with its own W scales, images s*J .. s*J + J - 1 of the
+    per-call buffers); it must give the bits of two one-perturbation calls
+    (TDSCHA_PAIR_APPLY=0), with and without symmetry images."""
+    ens = make_ensemble(M, N, seed=40 + M, n_syms=S, rho_sigma=0.1)
+    R1 = random_R1(M, 9)
+    runs = []
+    for pair in ("1", "0"):
+        monkeypatch.setenv("TDSCHA_PAIR_APPLY", pair)
+        lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
+                                   use_wigner=False, precision="mixed")
+        if S > 1:
+            lanc.init(use_symmetries=True, symmetries=(ens["symmetries"], ens["degenerate_space"]))
+        else:
+            lanc.init(use_symmetries=False)
+        lanc.full_reorth = True
+        lanc.prepare_perturbation(R1, masses_exp=0)
+        lanc.run_FT(30, verbose=False)
+        runs.append((np.array(lanc.a_coeffs), np.array(lanc.b_coeffs), np.array(lanc.c_coeffs),
+                     np.array(lanc.basis_Q)))
+        lanc._invalidate()
+    for x, y in zip(*runs):
+        assert np.array_equal(x, y)
