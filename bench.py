@@ -32,6 +32,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# hardware work queues for the batched leg's concurrent streams (read when the
+# CUDA context is created; the default of 8 made streams share queues)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "Lanczos steps/s, M=576 N=50k: mixed vs FP64 GPU at ≤1e-4 rel spectral error"
 UNIT = "steps/s"
