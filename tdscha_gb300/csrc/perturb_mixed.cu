@@ -1507,7 +1507,7 @@ __global__ void __launch_bounds__(256) k_wbuild_img(const float *__restrict__ ft
     sw_out += (long)blockIdx.z * Mp;
     __shared__ float red[kWRows][8];
     int b0 = blockIdx.x * kWRows;
-    long r0 = (long)blockIdx.y * kWChunk;
+    long r0 = (long)blockIdx.y * kWChunkImg;
     const float amax = absmax[0], bmax = absmax[1];
     float inv[kWRows], facc[kWRows];
 #pragma unroll

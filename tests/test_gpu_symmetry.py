@@ -60,7 +60,9 @@ def _oracle(ens, R1, Y1, d4=1):
                                    n_threads=16)
 
 
-@pytest.mark.parametrize("M,N,S", [(24, 400, 48), (48, 1500, 8), (189, 2000, 48)])
+# N above 2048 rows: several W-build row chunks and force partials per image
+@pytest.mark.parametrize("M,N,S", [(24, 400, 48), (48, 1500, 8), (189, 2000, 48), (189, 3500, 48),
+                                   (48, 2100, 8)])
 def test_image_free_averages_match_oracle(gpu_lib, M, N, S):
     ens = make_ensemble(M, N, seed=300 + M, n_syms=S, rho_sigma=0.1)
     R1, Y1 = random_R1(M, 4), random_sym(M, 5, scale=1e-3)
