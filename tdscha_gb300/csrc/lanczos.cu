@@ -1,5 +1,6 @@
-// The operator around the perturbation averages and the Krylov driver, all in
-// float64 on the GPU:
+// The operator around the perturbation averages and the Krylov driver on the
+// GPU (float64 vectors and recurrence scalars; the re-biorthogonalisation
+// sweeps of the real-space recurrence in double-float, dfloat.cuh):
 //   * psi -> (R1, Y1) unpack: get_Y1 / get_ReA1 / get_alpha1_beta1_wigner
 //     and the transpose rescaling (Modules/DynamicalLanczos.py:2773-2948,
 //     :3009-3053);
@@ -516,6 +517,8 @@ __global__ void k_normalize(const double *__restrict__ rk, const double *__restr
 // Full re-biorthogonalisation of the new pair (q_{k+1}, p_{k+1}) against the
 // stored basis: q -= sum_j (p_j.q / p_j.q_j) q_j and p -= sum_j (q_j.p / p_j.q_j) p_j
 // (one classical Gram-Schmidt pass; the recurrence scalars are not changed).
+// The float64 kernels below serve the q-space recurrence; the real-space one
+// uses the double-float forms further down (k_rdots*, k_rscale, k_rapply*).
 // The dot products run on a (vectors x chunks) grid of block partials: about
 // four blocks per SM over all vectors (a single vector in 24 chunks was
 // latency-bound at 14 us), but at least 24 chunks of at least eight elements
