@@ -109,6 +109,7 @@ struct tdscha_ctx {
     int *sc_idx = nullptr, *sr_idx = nullptr;
     double *sc_val = nullptr, *sr_val = nullptr;
     float2 *sr_val2 = nullptr;  // sr_val as double-float pairs (mixed path)
+    float2 *sc_val2 = nullptr;  // sc_val as double-float pairs (mixed path)
     double *Y1all = nullptr;    // float64 path, J x M x M: S_j^T Y1 S_j
     double *vsv = nullptr;      // J x M: S_j^T (f_Y R1), then J x M: S_j^T R1
     double *hs = nullptr;       // J x M x M: G_j + G_j^T summed over the splits

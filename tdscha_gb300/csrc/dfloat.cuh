@@ -73,6 +73,15 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return df_norm(s, c);
 }
 
+// a * b for double-float a, b (a.lo * b.lo dropped), normalised
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_norm(p, e);
+}
+
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
 }  // namespace tdscha

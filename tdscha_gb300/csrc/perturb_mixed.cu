@@ -44,6 +44,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace tdscha {
 
@@ -1265,13 +1266,27 @@ __global__ void k_prep_y1(const Src src, const double *__restrict__ fY, const do
     }
 }
 
+// Y1 of one perturbation as double-float pairs (M x M), read from psi or the
+// buffers once, so that the image preparation below does not unpack psi for
+// every one of its md^2 products per entry
+template <class Src>
+__global__ void k_y1_df(const Src src, int M, float2 *__restrict__ y1) {
+    pdl_enter();
+    const int n = blockIdx.x;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) y1[(long)n * M + m] = split_f64(src.y(n, m));
+}
+
 // The same for perturbation-side symmetry images (symmetry.cu): block
 // (j, n) forms row n of Y1_j = S_j^T Y1 S_j, and the epilogue vectors of image
-// j, (S_j^T (f_Y R1)) and (S_j^T R1) / f_psi, all at j*Mp + n.  The row is
-// staged in dynamic shared memory (Mp floats) between its max and its limbs.
+// j, (S_j^T (f_Y R1)) and (S_j^T R1) / f_psi, all at j*Mp + n.  The sandwich
+// runs in double-float (k_y1_df's Y1 and sc_val2: GB300's float64 rate made
+// the md^2 products per entry the kernel's cost); the row is staged in dynamic
+// shared memory (Mp floats) between its max and its limbs.
 template <class Src>
-__global__ void k_prep_y1_img(const Src src, const int *__restrict__ sc_idx,
-                              const double *__restrict__ sc_val, int md,
+__global__ void k_prep_y1_img(const Src src, const float2 *__restrict__ y1,
+                              const int *__restrict__ sc_idx,
+                              const double *__restrict__ sc_val,
+                              const float2 *__restrict__ sc_val2, int md,
                               const double *__restrict__ fY, const double *__restrict__ fpsi,
                               const float *__restrict__ sd, int M, int Mp,
                               __half *__restrict__ y_hi, __half *__restrict__ y_lo,
@@ -1283,20 +1298,22 @@ __global__ void k_prep_y1_img(const Src src, const int *__restrict__ sc_idx,
     const int n = blockIdx.x % Mp, j = blockIdx.x / Mp;
     const int *ia = sc_idx + ((long)j * M + (n < M ? n : 0)) * md;
     const double *va = sc_val + ((long)j * M + (n < M ? n : 0)) * md;
+    const float2 *va2 = sc_val2 + ((long)j * M + (n < M ? n : 0)) * md;
     float mx = 0.f;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
-        double y = 0;
+        float ys = 0.f;
         if (n < M && m < M) {
             const int *ib = sc_idx + ((long)j * M + m) * md;
-            const double *vb = sc_val + ((long)j * M + m) * md;
+            const float2 *vb2 = sc_val2 + ((long)j * M + m) * md;
+            float s = 0.f, c = 0.f;
             for (int p = 0; p < md && ia[p] >= 0; ++p) {
-                double inner = 0;
-                for (int q = 0; q < md && ib[q] >= 0; ++q)
-                    inner = fma(vb[q], src.y(ia[p], ib[q]), inner);
-                y = fma(va[p], inner, y);
+                float is = 0.f, ic = 0.f;
+                const float2 *row = y1 + (long)ia[p] * M;
+                for (int q = 0; q < md && ib[q] >= 0; ++q) df_fma_acc(is, ic, vb2[q], row[ib[q]]);
+                df_fma_acc(s, c, va2[p], df_norm(is, ic));
             }
+            ys = (s + c) * sd[m];
         }
-        float ys = (m < M) ? (float)y * sd[m] : 0.f;
         yrow[m] = ys;
         mx = fmaxf(mx, fabsf(ys));
     }
@@ -1334,7 +1351,7 @@ __global__ void k_prep_y1_img(const Src src, const int *__restrict__ sc_idx,
     }
 }
 
-// Row scalars from the stage A partials (sums in float64), and max |alpha|,
+// Row scalars from the stage A partials (sums in double-float), and max |alpha|,
 // max |beta| of each perturbation image for its W scales.  Block
 // (x, image j) takes rows r = j*Nr + i of configuration rows i (J = 1: the
 // image rows themselves, i = r).
@@ -1348,23 +1365,30 @@ __global__ void k_rows_mixed(const float *__restrict__ qpst, int nct, long Nr, i
     absmax += 2 * jj;
     float ma = 0.f, mb = 0.f;
     if (i < Nr) {
+        // the column-tile sums and the combinations in double-float: the
+        // results are rounded to fp32, and float64 here made the kernel
+        // float64-pipe bound at 96 images (0.96 M rows)
         const float *base = qpst + jj * nct * 4 * Nr;
-        double q = 0, p = 0, s = 0, t = 0;
+        float qs = 0.f, qc = 0.f, ps = 0.f, pc = 0.f, ss = 0.f, sc = 0.f, ts = 0.f, tc = 0.f;
         for (int ct = 0; ct < nct; ++ct) {
             const float *o = base + (long)ct * 4 * Nr;
-            q += o[i];
-            p += o[Nr + i];
-            s += o[2 * Nr + i];
-            t += o[3 * Nr + i];
+            df_two_sum_acc(qs, qc, o[i]);
+            df_two_sum_acc(ps, pc, o[Nr + i]);
+            df_two_sum_acc(ss, sc, o[2 * Nr + i]);
+            df_two_sum_acc(ts, tc, o[3 * Nr + i]);
         }
-        double rw = rho[i / rho_div];
-        double d4 = apply_d4 ? 1.0 : 0.0;
-        // constant reciprocals: float64 division is slow on this part and the
-        // results are rounded to fp32 anyway
-        const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
-        float4 v = make_float4((float)(rw * (s * third - d4 * q * 0.125)),
-                               (float)(rw * (t * third - d4 * p * 0.25)), (float)(-rw * q * sixth),
-                               (float)(-rw * p * third));
+        const float2 q = df_norm(qs, qc), p = df_norm(ps, pc), s3 = df_norm(ss, sc),
+                     t3 = df_norm(ts, tc);
+        const float2 rw = split_f64(rho[i / rho_div]);
+        // 1/3 and 1/6 as double-float constants
+        const float2 third = make_float2(0.333333343f, -9.93410776e-09f);
+        const float2 sixth = make_float2(0.166666672f, -4.96705388e-09f);
+        const float d4 = apply_d4 ? 1.f : 0.f;
+        const float2 a = df_add(df_mul(s3, third), make_float2(-d4 * 0.125f * q.x, -d4 * 0.125f * q.y));
+        const float2 b = df_add(df_mul(t3, third), make_float2(-d4 * 0.25f * p.x, -d4 * 0.25f * p.y));
+        const float2 c1 = df_mul(q, sixth), c2 = df_mul(p, third);
+        const float2 ra = df_mul(rw, a), rb = df_mul(rw, b), r1 = df_mul(rw, c1), r2 = df_mul(rw, c2);
+        float4 v = make_float4(ra.x + ra.y, rb.x + rb.y, -(r1.x + r1.y), -(r2.x + r2.y));
         abcc[r] = v;
         ma = fabsf(v.x);
         mb = fabsf(v.y);
@@ -1717,6 +1741,7 @@ struct MixedExtra {
     float *vs = nullptr, *vt = nullptr, *absmax = nullptr;
     float *d32 = nullptr;
     float4 *abcc = nullptr;
+    float2 *y1df = nullptr;   // symmetry images: Y1 of each perturbation (2 x M x M)
     float *fpart = nullptr;
     int nfchunk = 0;
     int ldG = 0, ntB = 0, nkbB = 0, kbps = 0;
@@ -1932,6 +1957,7 @@ int mixed_prepare(tdscha_ctx *c) {
     TDS_CUDA(cached_malloc(&x->absmax, sizeof(float) * 2 * Jm));
     TDS_CUDA(cached_malloc(&x->abcc, sizeof(float4) * (size_t)Jm * R));
     TDS_CUDA(cached_malloc(&x->fpart, sizeof(float) * (size_t)Jm * x->nfchunk * M));
+    if (J > 1) TDS_CUDA(cached_malloc(&x->y1df, sizeof(float2) * 2 * (size_t)M * M));
     TDS_CUDA(cached_malloc(&c->f2, sizeof(double) * M));
     TDS_CUDA(cached_malloc(&c->d2v2, sizeof(double) * (size_t)M * M));
     TDS_CUDA(cudaHostAlloc(&mx.err_flag, sizeof(int), cudaHostAllocMapped));
@@ -2010,7 +2036,7 @@ int mixed_release(tdscha_ctx *c) {
         cached_free(p);
     if (MixedExtra *x = extra(c)) {
         void *xb[] = {x->sd, x->fmx, x->su, x->sw, x->tcol, x->vs, x->vt, x->absmax, x->d32,
-                      x->abcc, x->fpart};
+                      x->abcc, x->fpart, x->y1df};
         for (void *p : xb)
             cached_free(p);
         delete x;
@@ -2080,15 +2106,21 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
             float *am = x->absmax + 2 * io;
             if (J > 1) {
                 const size_t sm = sizeof(float) * Mp;
-                if (psrc)
+                float2 *y1 = x->y1df + (size_t)sidx * M * M;
+                if (psrc) {
+                    TDS_CUDA(launch_pdl(k_y1_df<Y1FromPsi>, M, 256, 0, st, psrc[sidx], M, y1));
                     TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, J * Mp, 256, sm, st, psrc[sidx],
-                                        c->sc_idx, c->sc_val, c->maxdeg, c->fY, c->fpsi, x->sd, M,
-                                        Mp, yh, yl, tc, vs, vt, am));
-                else
-                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st,
-                                        Y1FromBuffers{c->Y1, c->R1, M}, c->sc_idx, c->sc_val,
+                                        (const float2 *)y1, c->sc_idx, c->sc_val, c->sc_val2,
                                         c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, yh, yl, tc, vs,
                                         vt, am));
+                } else {
+                    const Y1FromBuffers src{c->Y1, c->R1, M};
+                    TDS_CUDA(launch_pdl(k_y1_df<Y1FromBuffers>, M, 256, 0, st, src, M, y1));
+                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st, src,
+                                        (const float2 *)y1, c->sc_idx, c->sc_val, c->sc_val2,
+                                        c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, yh, yl, tc, vs,
+                                        vt, am));
+                }
             } else {
                 if (psrc)
                     TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, psrc[sidx], c->fY,

@@ -362,7 +362,8 @@ int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_spac
     TDS_CUDA(cudaMemcpy(c->sc_idx, ci.data(), sizeof(int) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->sr_val, rv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cudaMemcpy(c->sc_val, cv.data(), sizeof(double) * cells, cudaMemcpyHostToDevice));
-    // double-float copy of the row-sparse values for the mixed path's sandwich
+    // double-float copies of the row- and column-sparse values for the mixed
+    // path's finalisation and image preparation
     std::vector<float2> rv2(cells);
     for (size_t i = 0; i < cells; ++i) {
         float hi = (float)rv[i];
@@ -370,6 +371,12 @@ int psi_setup(tdscha_ctx *c, int n_blocks, const int *n_deg, const int *deg_spac
     }
     TDS_CUDA(cached_malloc(&c->sr_val2, sizeof(float2) * cells));
     TDS_CUDA(cudaMemcpy(c->sr_val2, rv2.data(), sizeof(float2) * cells, cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < cells; ++i) {
+        float hi = (float)cv[i];
+        rv2[i] = make_float2(hi, (float)(cv[i] - (double)hi));
+    }
+    TDS_CUDA(cached_malloc(&c->sc_val2, sizeof(float2) * cells));
+    TDS_CUDA(cudaMemcpy(c->sc_val2, rv2.data(), sizeof(float2) * cells, cudaMemcpyHostToDevice));
     TDS_CUDA(cached_malloc(&c->vsv, sizeof(double) * 2 * (size_t)S * M));
     // hs and tj (J x M x M each), fs and tf (J x M each)
     TDS_CUDA(cached_malloc(&c->hs, sizeof(double) * 2 * ((size_t)S * M * M + (size_t)S * M)));
@@ -384,7 +391,8 @@ void psi_free(tdscha_ctx *c) {
     cached_free(c->sr_val);
     cached_free(c->sc_val);
     cached_free(c->sr_val2);
-    c->sr_val2 = nullptr;
+    cached_free(c->sc_val2);
+    c->sr_val2 = c->sc_val2 = nullptr;
     cached_free(c->Y1all);
     cached_free(c->vsv);
     cached_free(c->hs);
