@@ -472,7 +472,7 @@ def run_ours(args):
                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                     "avg_launch_ms": tot_ms / cnt}
     kernels = {KERNEL_NAMES[k]: {"ms_per_launch": v[0] / v[1], "launches": v[1],
-                                 "perturbations_per_launch": ppl if k != 4 else 1}
+                                 "perturbations_per_launch": ppl if (k != 4 or n_img == 1) else 1}
                for k, v in kern.items()}
     # kernels launched per Lanczos step.  One application: the averages and
     # the assemble (mixed: Y1 limbs read straight from psi, stage A, row
@@ -483,12 +483,13 @@ def run_ours(args):
     # b/c, normalisation, and with re-biorthogonalisation the dots,
     # coefficients, update and weight (one update pass per 1024 stored pairs,
     # here always one).
-    per_app = 7 + (2 if n_img > 1 else 0) + (2 if n_img > 1 and prec_name == "fp64" else 0)
+    per_app = 7 + ((3 if prec_name == "mixed" else 4) if n_img > 1 else 0)
     if pair:
-        # one call for both: Y1 preparation and finalisation per perturbation,
-        # stage A, row scalars, W build and stage B once, then two assembles
-        fin = 3 if n_img > 1 else 1
-        per_step_ops = 2 + 4 + 2 * fin + 2
+        # one call for both: the Y1 preparation (with images: the Y1 unpack
+        # and the image limbs), stage A, row scalars, W build, stage B and (no
+        # images) the finalisation once for both perturbations; with images
+        # the three finalisation kernels per perturbation; two assembles
+        per_step_ops = (2 + 4 + 6 + 2) if n_img > 1 else (1 + 4 + 1 + 2)
     else:
         per_step_ops = 2 * per_app
     per_step_rec = 5 + (4 if not args.no_reorth else 0)

@@ -1225,14 +1225,29 @@ struct Y1FromPsi {
     __device__ double r(int n) const { return ignore_v3 ? 0.0 : psi[n]; }
 };
 
+// The perturbations of one call (one, or the two of a bi-Lanczos step):
+// the preparation kernels take perturbation blockIdx.y and write its outputs
+// at its image offset
 template <class Src>
-__global__ void k_prep_y1(const Src src, const double *__restrict__ fY, const double *__restrict__ fpsi,
-                          const float *__restrict__ sd, int M, int Mp, __half *__restrict__ y_hi,
-                          __half *__restrict__ y_lo, float *__restrict__ tcol,
-                          float *__restrict__ vs, float *__restrict__ vt,
-                          float *__restrict__ absmax) {
+struct SrcPair {
+    Src s[2];
+};
+
+template <class Src>
+__global__ void k_prep_y1(const SrcPair<Src> sp, const double *__restrict__ fY,
+                          const double *__restrict__ fpsi, const float *__restrict__ sd, int M,
+                          int Mp, __half *__restrict__ y_hi, __half *__restrict__ y_lo,
+                          float *__restrict__ tcol, float *__restrict__ vs,
+                          float *__restrict__ vt, float *__restrict__ absmax) {
     pdl_enter();
     __shared__ float red[32];
+    const Src &src = sp.s[blockIdx.y];
+    y_hi += blockIdx.y * (long)Mp * Mp;
+    y_lo += blockIdx.y * (long)Mp * Mp;
+    tcol += blockIdx.y * Mp;
+    vs += blockIdx.y * Mp;
+    vt += blockIdx.y * Mp;
+    absmax += 2 * blockIdx.y;
     int n = blockIdx.x;
     float mx = 0.f;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x)
@@ -1270,8 +1285,10 @@ __global__ void k_prep_y1(const Src src, const double *__restrict__ fY, const do
 // buffers once, so that the image preparation below does not unpack psi for
 // every one of its md^2 products per entry
 template <class Src>
-__global__ void k_y1_df(const Src src, int M, float2 *__restrict__ y1) {
+__global__ void k_y1_df(const SrcPair<Src> sp, int M, float2 *__restrict__ y1) {
     pdl_enter();
+    const Src &src = sp.s[blockIdx.y];
+    y1 += blockIdx.y * (long)M * M;
     const int n = blockIdx.x;
     for (int m = threadIdx.x; m < M; m += blockDim.x) y1[(long)n * M + m] = split_f64(src.y(n, m));
 }
@@ -1283,7 +1300,7 @@ __global__ void k_y1_df(const Src src, int M, float2 *__restrict__ y1) {
 // the md^2 products per entry the kernel's cost); the row is staged in dynamic
 // shared memory (Mp floats) between its max and its limbs.
 template <class Src>
-__global__ void k_prep_y1_img(const Src src, const float2 *__restrict__ y1,
+__global__ void k_prep_y1_img(const SrcPair<Src> sp, const float2 *__restrict__ y1,
                               const int *__restrict__ sc_idx,
                               const double *__restrict__ sc_val,
                               const float2 *__restrict__ sc_val2, int md,
@@ -1295,6 +1312,16 @@ __global__ void k_prep_y1_img(const Src src, const float2 *__restrict__ y1,
     pdl_enter();
     extern __shared__ float yrow[];
     __shared__ float red[32];
+    // perturbation blockIdx.y: its J images at image offset blockIdx.y * J
+    const Src &src = sp.s[blockIdx.y];
+    const long J = gridDim.x / Mp, io = blockIdx.y * J;
+    y1 += blockIdx.y * (long)M * M;
+    y_hi += io * Mp * Mp;
+    y_lo += io * Mp * Mp;
+    tcol += io * Mp;
+    vs += io * Mp;
+    vt += io * Mp;
+    absmax += 2 * io;
     const int n = blockIdx.x % Mp, j = blockIdx.x / Mp;
     const int *ia = sc_idx + ((long)j * M + (n < M ? n : 0)) * md;
     const double *va = sc_val + ((long)j * M + (n < M ? n : 0)) * md;
@@ -1624,11 +1651,20 @@ __device__ __forceinline__ double gsum_one(const float *__restrict__ g, int nspl
 }
 
 __global__ void __launch_bounds__(256) k_gfinal(const float *__restrict__ gpart, int nsplit,
-                                                long lda, long stride, int M,
+                                                long lda, long stride, int M, int Mp,
                                                 const float *__restrict__ fpart, int nfchunk,
                                                 double norm, double *__restrict__ f,
-                                                double *__restrict__ d2v) {
+                                                double *__restrict__ d2v, double *__restrict__ f2,
+                                                double *__restrict__ d2v2) {
     pdl_enter();
+    // perturbation blockIdx.y of the call: its G columns and force partials,
+    // its outputs
+    if (blockIdx.y) {
+        gpart += Mp;
+        fpart += (long)nfchunk * M;
+        f = f2;
+        d2v = d2v2;
+    }
     __shared__ double tr[32][9];    // G over rows b of tile B, the slab's 8 columns a: [b][a]
     __shared__ double red[8][33];
     // (pair, slab): pair index -> (A, B), A <= B, row-major over the upper
@@ -2096,39 +2132,40 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
     int *err_dev = nullptr;
     TDS_CUDA(cudaHostGetDevicePointer((void **)&err_dev, mx.err_flag, 0));
     {
+        // the Y1 limbs, epilogue vectors and W-scale maxima of every
+        // perturbation of the call, perturbation s at image offset s * J
         ProfScope ps(c, 5, st);
-        for (int sidx = 0; sidx < nsrc; ++sidx) {
-            // perturbation sidx: Y1 limbs of its J images, the epilogue vectors
-            // and its W-scale maxima at image offset sidx * J
-            const long io = (long)sidx * J;
-            __half *yh = mx.y1_hi + io * Mp * Mp, *yl = mx.y1_lo + io * Mp * Mp;
-            float *tc = x->tcol + io * Mp, *vs = x->vs + io * Mp, *vt = x->vt + io * Mp;
-            float *am = x->absmax + 2 * io;
-            if (J > 1) {
-                const size_t sm = sizeof(float) * Mp;
-                float2 *y1 = x->y1df + (size_t)sidx * M * M;
-                if (psrc) {
-                    TDS_CUDA(launch_pdl(k_y1_df<Y1FromPsi>, M, 256, 0, st, psrc[sidx], M, y1));
-                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, J * Mp, 256, sm, st, psrc[sidx],
-                                        (const float2 *)y1, c->sc_idx, c->sc_val, c->sc_val2,
-                                        c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, yh, yl, tc, vs,
-                                        vt, am));
-                } else {
-                    const Y1FromBuffers src{c->Y1, c->R1, M};
-                    TDS_CUDA(launch_pdl(k_y1_df<Y1FromBuffers>, M, 256, 0, st, src, M, y1));
-                    TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, J * Mp, 256, sm, st, src,
-                                        (const float2 *)y1, c->sc_idx, c->sc_val, c->sc_val2,
-                                        c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, yh, yl, tc, vs,
-                                        vt, am));
-                }
+        if (J > 1) {
+            const size_t sm = sizeof(float) * Mp;
+            const dim3 gy(M, nsrc), gi(J * Mp, nsrc);
+            if (psrc) {
+                const SrcPair<Y1FromPsi> sp{{psrc[0], psrc[nsrc - 1]}};
+                TDS_CUDA(launch_pdl(k_y1_df<Y1FromPsi>, gy, 256, 0, st, sp, M, x->y1df));
+                TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromPsi>, gi, 256, sm, st, sp,
+                                    (const float2 *)x->y1df, c->sc_idx, c->sc_val, c->sc_val2,
+                                    c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi, mx.y1_lo,
+                                    x->tcol, x->vs, x->vt, x->absmax));
             } else {
-                if (psrc)
-                    TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, Mp, 256, 0, st, psrc[sidx], c->fY,
-                                        c->fpsi, x->sd, M, Mp, yh, yl, tc, vs, vt, am));
-                else
-                    TDS_CUDA(launch_pdl(k_prep_y1<Y1FromBuffers>, Mp, 256, 0, st,
-                                        Y1FromBuffers{c->Y1, c->R1, M}, c->fY, c->fpsi, x->sd, M,
-                                        Mp, yh, yl, tc, vs, vt, am));
+                const Y1FromBuffers b1{c->Y1, c->R1, M};
+                const SrcPair<Y1FromBuffers> sp{{b1, b1}};
+                TDS_CUDA(launch_pdl(k_y1_df<Y1FromBuffers>, gy, 256, 0, st, sp, M, x->y1df));
+                TDS_CUDA(launch_pdl(k_prep_y1_img<Y1FromBuffers>, gi, 256, sm, st, sp,
+                                    (const float2 *)x->y1df, c->sc_idx, c->sc_val, c->sc_val2,
+                                    c->maxdeg, c->fY, c->fpsi, x->sd, M, Mp, mx.y1_hi, mx.y1_lo,
+                                    x->tcol, x->vs, x->vt, x->absmax));
+            }
+        } else {
+            const dim3 g(Mp, nsrc);
+            if (psrc) {
+                const SrcPair<Y1FromPsi> sp{{psrc[0], psrc[nsrc - 1]}};
+                TDS_CUDA(launch_pdl(k_prep_y1<Y1FromPsi>, g, 256, 0, st, sp, c->fY, c->fpsi, x->sd,
+                                    M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt, x->absmax));
+            } else {
+                const Y1FromBuffers b1{c->Y1, c->R1, M};
+                const SrcPair<Y1FromBuffers> sp{{b1, b1}};
+                TDS_CUDA(launch_pdl(k_prep_y1<Y1FromBuffers>, g, 256, 0, st, sp, c->fY, c->fpsi,
+                                    x->sd, M, Mp, mx.y1_hi, mx.y1_lo, x->tcol, x->vs, x->vt,
+                                    x->absmax));
             }
         }
     }
@@ -2194,21 +2231,20 @@ static int perturb_mixed_src(tdscha_ctx *c, int apply_d4, const Y1FromPsi *psrc,
         TDS_CUDA(launch_pdl(k_stageB_tc, grid, 192, kQSmem, st, x->tmB, gb));
     }
     const long sstride = (long)x->ldG * ldGb;
-    for (int sidx = 0; sidx < nsrc; ++sidx) {
-        double *f_out = sidx ? c->f2 : c->f, *d2v_out = sidx ? c->d2v2 : c->d2v;
-        const long io = (long)sidx * J;
-        const float *gp = mx.gpart + io * Mp;                  // its images' columns
-        const float *fp = x->fpart + io * x->nfchunk * M;
-        if (J > 1) {
-            TDS_TRY(psi_finalize32(c, gp, mx.nsplit, sstride, Mp, ldGb, fp, x->nfchunk, f_out,
-                                   d2v_out, st));
-            continue;
+    if (J > 1) {
+        for (int sidx = 0; sidx < nsrc; ++sidx) {
+            const long io = (long)sidx * J;
+            TDS_TRY(psi_finalize32(c, mx.gpart + io * Mp, mx.nsplit, sstride, Mp, ldGb,
+                                   x->fpart + io * x->nfchunk * M, x->nfchunk,
+                                   sidx ? c->f2 : c->f, sidx ? c->d2v2 : c->d2v, st));
         }
+    } else {
+        // both perturbations' split-K sums and (f, d2v) in one launch
         ProfScope ps(c, 4, st);
         const int nt = ceil_div(M, 32);
-        TDS_CUDA(launch_pdl(k_gfinal, 4 * (nt * (nt + 1) / 2), 256, 0, st, gp, mx.nsplit,
-                            (long)ldGb, sstride, M, fp, x->nfchunk, c->sum_rho * c->S, f_out,
-                            d2v_out));
+        TDS_CUDA(launch_pdl(k_gfinal, dim3(4 * (nt * (nt + 1) / 2), nsrc), 256, 0, st, mx.gpart,
+                            mx.nsplit, (long)ldGb, sstride, M, Mp, x->fpart, x->nfchunk,
+                            c->sum_rho * c->S, c->f, c->d2v, c->f2, c->d2v2));
     }
     return TDSCHA_OK;
 }
