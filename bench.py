@@ -479,20 +479,21 @@ def run_ours(args):
     # scalars, W build, stage B, finalisation; float64: psi unpack, stage A,
     # row scalars, force average, stage B, finalisation; with images on the
     # perturbation side the finalisation is three kernels and the float64 path
-    # adds the image vectors and matrices).  Recurrence: dot + a, residuals,
-    # b/c, normalisation, and with re-biorthogonalisation the dots,
-    # coefficients, update and weight (one update pass per 1024 stored pairs,
-    # here always one).
+    # adds the image vectors and matrices).  One update pass per 1024 stored
+    # pairs, here always one.
     per_app = 7 + ((3 if prec_name == "mixed" else 4) if n_img > 1 else 0)
     if pair:
         # one call for both: the Y1 preparation (with images: the Y1 unpack
-        # and the image limbs), stage A, row scalars, W build, stage B and (no
-        # images) the finalisation once for both perturbations; with images
-        # the three finalisation kernels per perturbation; two assembles
-        per_step_ops = (2 + 4 + 6 + 2) if n_img > 1 else (1 + 4 + 1 + 2)
+        # and the image limbs), stage A, row scalars, W build, stage B, (no
+        # images) the finalisation and the assemble once for both
+        # perturbations; with images the three finalisation kernels per
+        # perturbation
+        per_step_ops = (2 + 4 + 6 + 1) if n_img > 1 else (1 + 4 + 1 + 1)
     else:
         per_step_ops = 2 * per_app
-    per_step_rec = 5 + (4 if not args.no_reorth else 0)
+    # recurrence: dot + a, residuals + b/c, normalisation; re-biorthogonalisation:
+    # dots, coefficients, update, weight
+    per_step_rec = 3 + (4 if not args.no_reorth else 0)
     gpu_launches = K * n_run * (per_step_ops + per_step_rec)
 
     # float64 arm of the metric (same GPU, same runs) and the accuracy check

@@ -127,6 +127,7 @@ struct tdscha_ctx {
     double *Lq = nullptr, *pL = nullptr, *rk = nullptr, *sk = nullptr;
     double *mask = nullptr;     // Wigner double-counting mask (P)
     double *dots = nullptr;     // block partials of the fused dot kernels
+    unsigned *ctr = nullptr;    // last-block counters of the fused dot kernels (zero between launches)
     double *scal = nullptr;     // device scalars of the recurrence
     double *hist_dev = nullptr; // device copy of the coefficient history
     int hist_cap = 0;

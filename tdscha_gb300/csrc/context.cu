@@ -227,6 +227,7 @@ static void ctx_free(tdscha_ctx *c) {
     cached_free(c->tri);
     cached_free(c->lam_static);
     cached_free(c->vsplit);
+    cached_free(c->ctr);
     cached_free(c->f2);
     cached_free(c->d2v2);
     free_translations(c);
@@ -400,6 +401,8 @@ images_done:
     TRYC(dev_alloc(&c->dots, std::max<size_t>(4 * (size_t)std::max(c->nblk_dot, 1216),
                                               (size_t)(c->P + 63) / 64)));
     TRYC(dev_alloc(&c->scal, 64));
+    TRYC(dev_alloc(&c->ctr, 4));
+    CUC(cudaMemset(c->ctr, 0, sizeof(unsigned) * 4));
     CUC(cudaMemset(c->scal, 0, sizeof(double) * 64));
     CUC(cudaMallocHost((void **)&c->host_pinned, sizeof(double) * 64));
     TRYC(build_pair_coeffs(c));

@@ -169,13 +169,12 @@ __device__ __forceinline__ double asm_out(double l1, double an_pos, bool minus_a
 }
 
 template <int kMode, bool kRev>
-__global__ void k_assemble(const double *__restrict__ psi, const double *__restrict__ f,
+__device__ __forceinline__ void assemble_body(const double *__restrict__ psi, const double *__restrict__ f,
                            const double *__restrict__ d2v, const double *__restrict__ pc,
                            const int *__restrict__ tri, const double *__restrict__ w,
                            const double *__restrict__ Yw, const double *__restrict__ Ywinv,
                            const double *__restrict__ ReAw, int M, long H, int ignore_harmonic,
                            int with_anh, double shift, double *__restrict__ out) {
-    pdl_enter();
     constexpr bool kW = kMode == ASM_WIGNER;
     const bool harm = !ignore_harmonic, anh = with_anh != 0, sh = shift != 0.0;
     const long n = M + H;
@@ -229,6 +228,38 @@ __global__ void k_assemble(const double *__restrict__ psi, const double *__restr
         out[M + k] = oY;
         out[M + H + k] = oA;
     }
+}
+
+template <int kMode, bool kRev>
+__global__ void k_assemble(const double *__restrict__ psi, const double *__restrict__ f,
+                           const double *__restrict__ d2v, const double *__restrict__ pc,
+                           const int *__restrict__ tri, const double *__restrict__ w,
+                           const double *__restrict__ Yw, const double *__restrict__ Ywinv,
+                           const double *__restrict__ ReAw, int M, long H, int ignore_harmonic,
+                           int with_anh, double shift, double *__restrict__ out) {
+    pdl_enter();
+    assemble_body<kMode, kRev>(psi, f, d2v, pc, tri, w, Yw, Ywinv, ReAw, M, H, ignore_harmonic,
+                               with_anh, shift, out);
+}
+
+// Both outputs of a two-perturbation call in one launch: blockIdx.y = 0
+// assembles L q (plain layout), blockIdx.y = 1 L^T p (transposed layout)
+template <bool kRev>
+__global__ void k_assemble_pair(const double *__restrict__ q, const double *__restrict__ f,
+                                const double *__restrict__ d2v, double *__restrict__ Lq,
+                                const double *__restrict__ p, const double *__restrict__ f2,
+                                const double *__restrict__ d2v2, double *__restrict__ pL,
+                                const double *__restrict__ pc, const int *__restrict__ tri,
+                                const double *__restrict__ w, const double *__restrict__ Yw,
+                                const double *__restrict__ Ywinv, const double *__restrict__ ReAw,
+                                int M, long H, int ignore_harmonic, double shift) {
+    pdl_enter();
+    if (blockIdx.y == 0)
+        assemble_body<ASM_PLAIN, kRev>(q, f, d2v, pc, tri, w, Yw, Ywinv, ReAw, M, H,
+                                       ignore_harmonic, 1, shift, Lq);
+    else
+        assemble_body<ASM_TRANSPOSE, kRev>(p, f2, d2v2, pc, tri, w, Yw, Ywinv, ReAw, M, H,
+                                           ignore_harmonic, 1, shift, pL);
 }
 
 template <int kMode>
@@ -306,12 +337,15 @@ int apply_full_L_pair_dev(tdscha_ctx *c, const double *q, const double *p, doubl
     TDS_TRY(perturb_mixed_pair(c, c->ignore_v4 ? 0 : 1, q, p, c->pc + PC_TY * H,
                                c->pc + PC_TRA * H, st));
     const int nb = std::max(1, std::min(ceil_div(M + H, 256), 4096));
-    TDS_CUDA(launch_assemble<ASM_PLAIN>(nb, st, c->reverse_L, q, c->f, c->d2v, c->pc, c->tri, c->w,
-                                        c->Yw, c->Ywinv, c->ReAw, M, H, c->ignore_harmonic, 1,
-                                        c->shift, Lq));
-    TDS_CUDA(launch_assemble<ASM_TRANSPOSE>(nb, st, c->reverse_L, p, c->f2, c->d2v2, c->pc, c->tri,
-                                            c->w, c->Yw, c->Ywinv, c->ReAw, M, H,
-                                            c->ignore_harmonic, 1, c->shift, pL));
+    const dim3 g(nb, 2);
+    if (c->reverse_L)
+        TDS_CUDA(launch_pdl(k_assemble_pair<true>, g, 256, 0, st, q, c->f, c->d2v, Lq, p, c->f2,
+                            c->d2v2, pL, c->pc, c->tri, c->w, c->Yw, c->Ywinv, c->ReAw, M, H,
+                            c->ignore_harmonic, c->shift));
+    else
+        TDS_CUDA(launch_pdl(k_assemble_pair<false>, g, 256, 0, st, q, c->f, c->d2v, Lq, p, c->f2,
+                            c->d2v2, pL, c->pc, c->tri, c->w, c->Yw, c->Ywinv, c->ReAw, M, H,
+                            c->ignore_harmonic, c->shift));
     return TDSCHA_OK;
 }
 
@@ -377,12 +411,12 @@ __device__ __forceinline__ double reduce_parts(const double *__restrict__ part, 
 }
 
 // a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232)
-__global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
-                         int k, double *__restrict__ scal, double *__restrict__ status) {
-    pdl_enter();
-    __shared__ double sh[32];
-    double d = reduce_parts(part, nblk, sh);
-    if (threadIdx.x != 0 || scal[SC_HALT] != 0.0) return;
+// a = dot * p_norm and the axpy factors of the residuals (run_FT :6167-6232);
+// thread 0
+__device__ __forceinline__ void scal_a_body(double d, const double *__restrict__ hist, int k,
+                                            double *__restrict__ scal,
+                                            double *__restrict__ status) {
+    if (scal[SC_HALT] != 0.0) return;
     double c_old = k >= 1 ? hist[4 * (k - 1) + 2] : 1.0;
     double p_norm = hist[4 * k + 3] / c_old;
     double a = d * p_norm;
@@ -399,6 +433,56 @@ __global__ void k_scal_a(const double *__restrict__ part, int nblk, const double
     }
     scal[SC_CQ] = cq;
     scal[SC_CP] = cp;
+}
+
+__global__ void k_scal_a(const double *__restrict__ part, int nblk, const double *__restrict__ hist,
+                         int k, double *__restrict__ scal, double *__restrict__ status) {
+    pdl_enter();
+    __shared__ double sh[32];
+    double d = reduce_parts(part, nblk, sh);
+    if (threadIdx.x == 0) scal_a_body(d, hist, k, scal, status);
+}
+
+// Sum of nblk block partials written by other blocks of the same kernel:
+// loads from L2 (this SM's L1 may hold the buffer from an earlier step)
+__device__ __forceinline__ double reduce_parts_cg(const double *__restrict__ part, int nblk,
+                                                  double *sh) {
+    double v = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += __ldcg(part + b);
+    return block_sum(v, sh);
+}
+
+// Whether this block is the last of the grid to have written its partials
+// (thread 0 wrote them): the last block then reduces them in the fixed order
+// of the separate reduction kernel and resets the counter for the next launch.
+// No block waits for another.
+__device__ __forceinline__ bool last_block(unsigned *__restrict__ ctr, bool *flag) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *flag = atomicAdd(ctr, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (*flag) __threadfence();
+    return *flag;
+}
+
+// k_dot1 and k_scal_a in one launch (the real-space recurrence)
+__global__ void k_dot1_a(const double *__restrict__ x, const double *__restrict__ y,
+                         const double *__restrict__ mask, long n, double *__restrict__ part,
+                         const double *__restrict__ hist, int k, double *__restrict__ scal,
+                         double *__restrict__ status, unsigned *__restrict__ ctr) {
+    pdl_enter();
+    __shared__ double sh[32];
+    __shared__ bool flag;
+    double acc = mask ? dot1_range<true>(x, y, mask, n) : dot1_range<false>(x, y, mask, n);
+    double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (!last_block(ctr, &flag)) return;
+    const double d = reduce_parts_cg(part, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+        *ctr = 0u;
+        scal_a_body(d, hist, k, scal, status);
+    }
 }
 
 template <bool kMasked>
@@ -444,14 +528,12 @@ __global__ void k_resid(const double *__restrict__ Lq, const double *__restrict_
     t = block_sum(sr, sh); if (threadIdx.x == 0) part[2 * nblk + blockIdx.x] = t;
 }
 
-__global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
-                          int k, double *__restrict__ scal, double *__restrict__ status) {
-    pdl_enter();
-    __shared__ double sh[32];
-    double ss = reduce_parts(part, nblk, sh);
-    double rr = reduce_parts(part + nblk, nblk, sh);
-    double sr = reduce_parts(part + 2 * nblk, nblk, sh);
-    if (threadIdx.x != 0 || scal[SC_HALT] != 0.0) return;
+// b, c, the new s_norm and the stop test (run_FT :6233-6306); thread 0
+__device__ __forceinline__ void scal_bc_body(double ss, double rr, double sr,
+                                             double *__restrict__ hist, int k,
+                                             double *__restrict__ scal,
+                                             double *__restrict__ status) {
+    if (scal[SC_HALT] != 0.0) return;
     double s_raw = sqrt(ss);
     double s_norm = s_raw * scal[SC_PNORM];
     double b = sqrt(rr);
@@ -473,6 +555,47 @@ __global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__r
         hist[4 * k + 1] = b;
         hist[4 * k + 2] = c;
         hist[4 * (k + 1) + 3] = s_norm;
+    }
+}
+
+__global__ void k_scal_bc(const double *__restrict__ part, int nblk, double *__restrict__ hist,
+                          int k, double *__restrict__ scal, double *__restrict__ status) {
+    pdl_enter();
+    __shared__ double sh[32];
+    double ss = reduce_parts(part, nblk, sh);
+    double rr = reduce_parts(part + nblk, nblk, sh);
+    double sr = reduce_parts(part + 2 * nblk, nblk, sh);
+    if (threadIdx.x == 0) scal_bc_body(ss, rr, sr, hist, k, scal, status);
+}
+
+// k_resid and k_scal_bc in one launch (the real-space recurrence)
+__global__ void k_resid_bc(const double *__restrict__ Lq, const double *__restrict__ pL,
+                           const double *__restrict__ q, const double *__restrict__ p,
+                           const double *__restrict__ qprev, const double *__restrict__ pprev,
+                           const double *__restrict__ mask, double *__restrict__ scal, long n,
+                           double *__restrict__ rk, double *__restrict__ sk,
+                           double *__restrict__ part, double *__restrict__ hist, int k,
+                           double *__restrict__ status, unsigned *__restrict__ ctr) {
+    pdl_enter();
+    __shared__ double sh[32];
+    __shared__ bool flag;
+    const int nblk = gridDim.x;
+    double ss = 0, rr = 0, sr = 0;
+    if (mask)
+        resid_range<true>(Lq, pL, q, p, qprev, pprev, mask, scal, n, rk, sk, ss, rr, sr);
+    else
+        resid_range<false>(Lq, pL, q, p, qprev, pprev, mask, scal, n, rk, sk, ss, rr, sr);
+    double t;
+    t = block_sum(ss, sh); if (threadIdx.x == 0) part[blockIdx.x] = t;
+    t = block_sum(rr, sh); if (threadIdx.x == 0) part[nblk + blockIdx.x] = t;
+    t = block_sum(sr, sh); if (threadIdx.x == 0) part[2 * nblk + blockIdx.x] = t;
+    if (!last_block(ctr, &flag)) return;
+    const double a = reduce_parts_cg(part, nblk, sh);
+    const double b = reduce_parts_cg(part + nblk, nblk, sh);
+    const double c = reduce_parts_cg(part + 2 * nblk, nblk, sh);
+    if (threadIdx.x == 0) {
+        *ctr = 0u;
+        scal_bc_body(a, b, c, hist, k, scal, status);
     }
 }
 
@@ -1200,13 +1323,14 @@ static int lz_step(tdscha_ctx *ctx, double *basis_Q, double *basis_P, long ld, i
         TDS_TRY(apply_full_L_pair_dev(ctx, q, p, ctx->Lq, ctx->pL, precision, st));
         pL = ctx->pL;
     }
-    launch_pdl(k_dot1, nb, kDotThreads, 0, st, p, ctx->Lq, mask, P, ctx->dots);
-    launch_pdl(k_scal_a, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    // the dot products with their scalar tails in one launch each (the last
+    // block reduces the partials, counters ctx->ctr[0] and [1])
+    launch_pdl(k_dot1_a, nb, kDotThreads, 0, st, p, ctx->Lq, mask, P, ctx->dots, ctx->hist_dev, k,
+               ctx->scal, ctx->stat_dev, ctx->ctr);
     const double *qprev = k >= 1 ? basis_Q + (long)(k - 1) * ld : nullptr;
     const double *pprev = k >= 1 ? basis_P + (long)(k - 1) * ld : nullptr;
-    launch_pdl(k_resid, nb, kDotThreads, 0, st, ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal, P,
-               ctx->rk, ctx->sk, ctx->dots, nb);
-    launch_pdl(k_scal_bc, 1, 256, 0, st, ctx->dots, nb, ctx->hist_dev, k, ctx->scal, ctx->stat_dev);
+    launch_pdl(k_resid_bc, nb, kDotThreads, 0, st, ctx->Lq, pL, q, p, qprev, pprev, mask, ctx->scal,
+               P, ctx->rk, ctx->sk, ctx->dots, ctx->hist_dev, k, ctx->stat_dev, ctx->ctr + 1);
     double *qn = basis_Q + (long)(k + 1) * ld, *pn = basis_P + (long)(k + 1) * ld;
     const long ldv = split_ld(P);
     launch_pdl(k_normalize, nbw, kDotThreads, 0, st, ctx->rk, ctx->sk, ctx->scal, P, qn, pn, mask,
