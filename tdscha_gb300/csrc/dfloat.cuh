@@ -5,10 +5,10 @@
 // Reductions and projections that would spend one or two float64 operations
 // per loaded element run here on pairs of float32 values (hi, lo) instead:
 // float64 operands are split into hi + lo with integer operations only,
-// products are formed to ~2^-48 relative (hi*hi with its FMA rounding error,
-// plus the two cross terms) and sums are error-free (TwoSum, Knuth, The Art of
-// Computer Programming vol. 2, 4.2.2), so a sum carries about 48 significant
-// bits and is folded into float64 once, at the end.
+// products are formed to about 2^-45.5 relative (hi*hi with its FMA rounding
+// error, plus the two cross terms; the dropped lo*lo is at most 2^-46 of the
+// product) and sums are error-free (TwoSum, Knuth, The Art of Computer
+// Programming vol. 2, 4.2.2); a sum is folded into float64 once, at the end.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -48,9 +48,9 @@ __device__ __forceinline__ void df_two_sum_acc(float &s, float &c, float v) {
     s = t;
 }
 
-// (s, c) += a * b for double-float a, b: the product to ~2^-48 relative
-// (a.lo * b.lo dropped), its hi part added to s by TwoSum, every rounding
-// error collected in c.
+// (s, c) += a * b for double-float a, b: the product to about 2^-45.5
+// relative (a.lo * b.lo dropped), its hi part added to s by TwoSum, every
+// rounding error collected in c.
 __device__ __forceinline__ void df_fma_acc(float &s, float &c, float2 a, float2 b) {
     const float p = a.x * b.x;
     float e = fmaf(a.x, b.x, -p);
