@@ -316,8 +316,10 @@ def run_ours(args):
     prec_name = args.precision or "mixed"
     prec = nat.PREC_MIXED if prec_name == "mixed" else nat.PREC_FP64
     syms, spaces, bid = sym_tables(ens)
+    # mixed: the ensemble held in 4-byte storage only (fp32 rows and fp16 limbs;
+    # the float64 rows are released once the operands are built)
     ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
-                      with_mixed=(prec_name == "mixed"))
+                      with_mixed="fp32" if prec_name == "mixed" else False)
     ctx.set_options(False, False, False, False, False, 0.0)     # bi-Lanczos (normal repr.)
     n_img, rows = ctx.layout()
     tuning = None
@@ -418,7 +420,9 @@ def run_ours(args):
             sweeps[name + "_frac_of_measured_hbm"] = sweeps[name + "_gbs"] / hbm
     static = None
     if not args.no_rows and prec_name == "mixed":
-        static = static_leg(lib, nat, ctx, M, S * N, dev)
+        static = static_leg(lib, nat, ctx, M, S * N, dev,
+                            lambda: nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"],
+                                                ens["T"], syms, spaces, bid, with_mixed=False))
     ctx.close()
     R = N * S
     flops_app = 4.0 * R * M * M          # two GEMM stages of 2 R M^2 each
@@ -531,6 +535,10 @@ def run_ours(args):
                            "symmetry_images": ("applied to the perturbation (%d), ensemble rows "
                                                "resident: %d" % (n_img, rows)) if S > 1 else "none",
                            "tuning": tuning,
+                           "storage": ("ensemble resident in 4-byte storage only: fp32 rows "
+                                       "and two-limb fp16 operands (float64 rows released "
+                                       "after operand preparation)") if prec_name == "mixed"
+                                      else "float64 rows",
                            "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": ("inputs larger than L2 (ensemble %.0f MB)" % (ens_bytes / 1e6))
                                  if flush is None else
@@ -673,10 +681,11 @@ def fp64_arm_and_check(args, ens, spec, syms, spaces, bid, dev, local, rank=0):
     return out, check
 
 
-def static_leg(lib, nat, ctx, M, R, dev):
+def static_leg(lib, nat, ctx, M, R, dev, make_ctx64=None):
     """Static (Hessian) operator L1_static + anharmonic_static through
     tdscha_static_L: one StaticHessian / run_hessian_calculation matvec is M
-    such applications.  Device time per application, mixed and float64."""
+    such applications.  Device time per application, mixed and float64 (on a
+    float64 context from make_ctx64 when ctx holds 4-byte storage only)."""
     import torch
     Ps = M + M * (M + 1) // 2
     stream = torch.cuda.current_stream()
@@ -684,6 +693,10 @@ def static_leg(lib, nat, ctx, M, R, dev):
     g = torch.Generator(device=dev).manual_seed(5)
     out = {"what": "static operator (harmonic + anharmonic), batched rows of M + M(M+1)/2"}
     for name, prec, nvec in (("mixed", nat.PREC_MIXED, min(M, 96)), ("fp64", nat.PREC_FP64, 2)):
+        own = prec == nat.PREC_FP64 and not ctx.fp64_storage
+        if own:
+            ctx = make_ctx64()
+            ctx.set_options(False, False, False, False, False, 0.0)
         X = torch.randn((nvec, Ps), dtype=torch.float64, device=dev, generator=g)
         Y = torch.empty_like(X)
         nat.check(lib.tdscha_static_L(ctx.handle, 1, X.data_ptr(), Y.data_ptr(), 3, 1.0, prec, st))
@@ -699,6 +712,8 @@ def static_leg(lib, nat, ctx, M, R, dev):
         out[name] = {"ms_per_application": ms, "applications_per_s": 1e3 / ms,
                      "rows_timed": nvec, "matvec_s_at_M_rows": ms * M / 1e3,
                      "achieved_tflops": 4.0 * R * M * M / (ms / 1e3) / 1e12}
+        if own:
+            ctx.close()
     return out
 
 

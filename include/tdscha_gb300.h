@@ -65,10 +65,14 @@ int tdscha_get_perturb_average_sym(int M, int N, const double *X, const double *
 
 /*
  * Context: the ensemble uploaded once and kept resident in HBM, with the
- * symmetry images, the per-mode Bose factors and (with_mixed != 0) the
- * split-bf16 copies used by TDSCHA_PREC_MIXED.  Replaces the state the
- * reference keeps in `Lanczos` (Modules/DynamicalLanczos.py:183-505, :694-871)
- * and re-sends to the C module on every call.  Host pointers.
+ * symmetry images, the per-mode Bose factors and (with_mixed != 0) the fp32
+ * rows and two-limb fp16 operands used by TDSCHA_PREC_MIXED.  with_mixed = 0:
+ * float64 storage only; 1: both; 2: the mixed operands only (4-byte storage),
+ * the float64 image rows released once the operands are built, so that
+ * TDSCHA_PREC_FP64 calls on this context return TDSCHA_ERR_STATE.  Replaces
+ * the state the reference keeps in `Lanczos`
+ * (Modules/DynamicalLanczos.py:183-505, :694-871) and re-sends to the C
+ * module on every call.  Host pointers.
  */
 int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X, const double *Y,
                       const double *w, const double *rho, double T, int N_syms,

@@ -102,6 +102,9 @@ class Lanczos(object):
         self.ignore_small_w = False
         self.unwrapped = False
         self.precision = precision
+        # mixed precision with the ensemble held in 4-byte storage only (the
+        # float64 rows are released on the device once the operands are built)
+        self.fp32_storage = False
         self.full_reorth = False
         self.trans_projector = None
         self.trans_cart_perms = None
@@ -383,15 +386,19 @@ class Lanczos(object):
             raise ValueError("Error, this class must be initialized before lunching the "
                              "computation:\n Use the .init()")
         want_mixed = self.precision == "mixed"
+        only32 = want_mixed and bool(self.fp32_storage)
         key = (id(self.X), id(self.Y), id(self.rho), self.T, id(self.symmetries),
                bool(self.gamma_only), id(self.trans_cart_perms))
-        if self._ctx is not None and (self._ctx_key != key or (want_mixed and not self._ctx.with_mixed)):
+        if self._ctx is not None and (self._ctx_key != key or
+                                      (want_mixed and not self._ctx.with_mixed) or
+                                      (not want_mixed and not self._ctx.fp64_storage) or
+                                      (only32 and self._ctx.fp64_storage)):
             self._invalidate()
         if self._ctx is None:
             _torch()
             self._ctx = nat.Context(self.X, self.Y, self.w, self.rho, self.T, self.symmetries,
                                     self.degenerate_space, self.sym_block_id,
-                                    with_mixed=want_mixed)
+                                    with_mixed="fp32" if only32 else want_mixed)
             self._ctx_key = key
             if self.gamma_only and self.trans_cart_perms is not None:
                 perms = np.ascontiguousarray(np.array(self.trans_cart_perms), dtype=np.intc)

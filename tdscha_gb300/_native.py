@@ -178,6 +178,11 @@ class Context:
 
     def __init__(self, X, Y, w, rho, T, symmetries, degenerate_space, blocks_ids,
                  with_mixed=False):
+        # with_mixed: False (float64 only), True (float64 and mixed operands) or
+        # "fp32" (mixed operands only, the float64 rows released after building them)
+        if with_mixed not in (False, True, 0, 1, "fp32"):
+            raise ValueError("with_mixed must be False, True or 'fp32', got %r" % (with_mixed,))
+        code = 2 if with_mixed == "fp32" else (1 if with_mixed else 0)
         lib = load()
         X, Y, w, rho = f64(X), f64(Y), f64(w), f64(rho)
         if X.ndim != 2 or Y.shape != X.shape:
@@ -191,11 +196,12 @@ class Context:
         bid = i32(blocks_ids)
         self.M, self.N, self.S = M, N, n_syms
         self.P = M + M * (M + 1)
-        self.with_mixed = bool(with_mixed)
+        self.with_mixed = code != 0
+        self.fp64_storage = code != 2
         h = _vp()
         check(lib.tdscha_ctx_create(ctypes.byref(h), M, N, dp(X), dp(Y), dp(w), dp(rho), float(T),
                                     n_syms, len(n_deg), ip(n_deg), ip(deg), dp(sym), ip(bid),
-                                    1 if with_mixed else 0))
+                                    code))
         self.handle = h
         self._opts = None
 

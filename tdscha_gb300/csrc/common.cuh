@@ -78,7 +78,7 @@ struct tdscha_ctx {
     long P = 0;                 // psi length M + M(M+1)
     long H = 0;                 // M(M+1)/2
     double T = 0, sum_rho = 0;  // sum_rho accumulated in config order
-    int with_mixed = 0;
+    int with_mixed = 0;     // 0 float64 only, 1 float64 + mixed, 2 mixed with 4-byte storage only
     // operator options
     int use_wigner = 1, ignore_harmonic = 0, ignore_v3 = 0, ignore_v4 = 0, reverse_L = 0;
     int pc_wigner = -1;          // representation the pair coefficients were built for
@@ -251,6 +251,8 @@ inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 // callers free after synchronising.
 cudaError_t cached_malloc(void **p, size_t bytes);
 void cached_free(void *p);
+// frees a block at once (cudaFree), whether it came from cached_malloc or not
+void release_block(void *p);
 template <typename T>
 inline cudaError_t cached_malloc(T **p, size_t bytes) {
     return cached_malloc(reinterpret_cast<void **>(p), bytes);

@@ -197,6 +197,21 @@ void tdscha::cached_free(void *p) {
     bc.idle_bytes += key.second;
 }
 
+// returns a block to the device at once, bypassing the idle cache
+void tdscha::release_block(void *p) {
+    if (!p) return;
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    auto it = bc.live.find(p);
+    if (it == bc.live.end()) {
+        cudaFree(p);
+        return;
+    }
+    const int dev = it->second.first;
+    bc.live.erase(it);
+    free_on_device(dev, p);
+}
+
 extern "C" int tdscha_release_cached_memory(unsigned long long *bytes) {
     set_error("");
     cudaDeviceSynchronize();
@@ -260,6 +275,7 @@ extern "C" int tdscha_ctx_create(tdscha_ctx **out, int M, int N, const double *X
         return TDSCHA_ERR_ARG;
     }
     if (!(T >= 0) || !std::isfinite(T)) { set_error("ctx_create: bad temperature %g", T); return TDSCHA_ERR_ARG; }
+    if (with_mixed < 0 || with_mixed > 2) { set_error("ctx_create: with_mixed=%d (0, 1 or 2)", with_mixed); return TDSCHA_ERR_ARG; }
     // validate the symmetry tables so that no device access can leave them
     std::vector<int> deg_off(n_blocks);
     std::vector<long> sym_off(n_blocks);
@@ -408,6 +424,12 @@ images_done:
     TRYC(build_pair_coeffs(c));
     if (with_mixed) TRYC(mixed_prepare(c));
     CUC(cudaDeviceSynchronize());
+    if (with_mixed == 2) {
+        // 4-byte storage only: the float64 image rows served the preparation of
+        // the fp32 rows and fp16 limbs above and are not read again
+        release_block(c->D); c->D = nullptr;
+        release_block(c->F); c->F = nullptr;
+    }
     *out = c;
     return TDSCHA_OK;
 fail:
@@ -463,7 +485,13 @@ __global__ void k_symmetrize(double *Y1, int M) {
 
 // Perturbation averages for a Y1 already symmetric in ctx->Y1.
 int run_perturb_sym(tdscha_ctx *c, int apply_d4, int precision, cudaStream_t st) {
-    if (precision == TDSCHA_PREC_FP64) return perturb_fp64(c, apply_d4, st);
+    if (precision == TDSCHA_PREC_FP64) {
+        if (!c->D) {
+            set_error("float64 averages requested but the context keeps the ensemble in 4-byte storage only (with_mixed=2)");
+            return TDSCHA_ERR_STATE;
+        }
+        return perturb_fp64(c, apply_d4, st);
+    }
     if (precision == TDSCHA_PREC_MIXED) {
         if (!c->with_mixed) { set_error("mixed precision requested but the context was created without it"); return TDSCHA_ERR_STATE; }
         return perturb_mixed(c, apply_d4, st);

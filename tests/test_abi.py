@@ -49,13 +49,14 @@ def _create(lib, M=4, N=3, **over):
     X = np.zeros((N, M)); Y = np.zeros((N, M)); w = np.full(M, 1e-3); rho = np.ones(N)
     n_deg, deg, sym, bid = _tables(M)
     args = dict(M=M, N=N, X=X, Y=Y, w=w, rho=rho, T=300.0, S=1, nb=M, n_deg=n_deg, deg=deg,
-                sym=sym, bid=bid)
+                sym=sym, bid=bid, mixed=0)
     args.update(over)
     h = ctypes.c_void_p()
     rc = lib.tdscha_ctx_create(ctypes.byref(h), args["M"], args["N"], nat.dp(args["X"]),
                                nat.dp(args["Y"]), nat.dp(args["w"]), nat.dp(args["rho"]),
                                args["T"], args["S"], args["nb"], nat.ip(args["n_deg"]),
-                               nat.ip(args["deg"]), nat.dp(args["sym"]), nat.ip(args["bid"]), 0)
+                               nat.ip(args["deg"]), nat.dp(args["sym"]), nat.ip(args["bid"]),
+                               args["mixed"])
     return rc, h
 
 
@@ -76,6 +77,15 @@ def test_create_rejects_nan_input(gpu_lib):
     Y = np.zeros((3, 4)); Y[2, 0] = np.inf
     rc, h = _create(gpu_lib, Y=Y)
     assert rc == nat.ERR_NAN and b"at 8" in gpu_lib.tdscha_last_error()
+
+
+def test_create_rejects_bad_storage_mode(lib):
+    for mode in (-1, 3):
+        rc, h = _create(lib, mixed=mode)
+        assert rc == nat.ERR_ARG and not h.value and b"with_mixed" in lib.tdscha_last_error()
+    with pytest.raises(ValueError):
+        nat.Context(np.zeros((3, 4)), np.zeros((3, 4)), np.full(4, 1e-3), np.ones(3), 300.0,
+                    None, None, None, with_mixed="fp16")
 
 
 def test_create_rejects_bad_blocks(lib):

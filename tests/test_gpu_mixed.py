@@ -215,3 +215,58 @@ def test_pair_application_bitwise(gpu_lib, monkeypatch, M, N, S):
         lanc._invalidate()
     for x, y in zip(*runs):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("M,N,S", [(96, 30000, 1), (24, 400, 48)])
+def test_fp32_storage_context(gpu_lib, M, N, S):
+    """with_mixed='fp32' keeps only the 4-byte operands: the float64 image rows
+    (2 x N S x M doubles) go back to the device once the operands are built.
+    Mixed calls and runs give the bits of a context that keeps both storages,
+    and a float64 call is refused with TDSCHA_ERR_STATE."""
+    import torch
+    ens = make_ensemble(M, N, seed=60 + M, n_syms=S, rho_sigma=0.1)
+    if S == 1:
+        syms, spaces, bid = oracle.identity_symmetries(M)
+    else:
+        syms, spaces, bid = ens["symmetries"], ens["degenerate_space"], ens["sym_block_id"]
+    R1, Y1 = random_R1(M, 3), random_sym(M, 4, scale=1e-3)
+    lib = nat.load()
+    outs, free = [], []
+    for mode in (True, "fp32"):
+        nat.check(lib.tdscha_release_cached_memory(None))
+        torch.cuda.synchronize()
+        ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
+                          with_mixed=mode)
+        outs.append(_mixed_call(ctx, R1, Y1))
+        f = np.zeros(M)
+        d2v = np.zeros((M, M))
+        rc = lib.tdscha_perturb_averages(ctx.handle, R1.ctypes.data, Y1.ctypes.data, 1,
+                                         nat.PREC_FP64, f.ctypes.data, d2v.ctypes.data, 0, None)
+        assert (rc == nat.OK) == (mode is True)
+        if mode == "fp32":
+            assert rc == nat.ERR_STATE and not ctx.fp64_storage
+        # after both calls: every kernel module the two contexts use is loaded
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
+        ctx.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    assert free[1] - free[0] >= 2 * N * S * M * 8 // 2
+    nat.check(lib.tdscha_release_cached_memory(None))
+    # the Lanczos class: fp32_storage with precision 'mixed', same coefficients
+    runs = []
+    for only32 in (False, True):
+        lanc = Lanczos.from_arrays(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"],
+                                   use_wigner=False, precision="mixed")
+        lanc.fp32_storage = only32
+        if S > 1:
+            lanc.init(use_symmetries=True, symmetries=(ens["symmetries"], ens["degenerate_space"]))
+        else:
+            lanc.init(use_symmetries=False)
+        lanc.prepare_perturbation(random_R1(M, 9), masses_exp=0)
+        lanc.run_FT(8, verbose=False)
+        runs.append((np.array(lanc.a_coeffs), np.array(lanc.b_coeffs), np.array(lanc.c_coeffs)))
+        assert lanc._ctx.fp64_storage == (not only32)
+        lanc._invalidate()
+    for x, y in zip(*runs):
+        assert np.array_equal(x, y)
