@@ -220,7 +220,7 @@ def test_pair_application_bitwise(gpu_lib, monkeypatch, M, N, S):
 @pytest.mark.parametrize("M,N,S", [(96, 30000, 1), (24, 400, 48)])
 def test_fp32_storage_context(gpu_lib, M, N, S):
     """with_mixed='fp32' keeps only the 4-byte operands: the float64 image rows
-    (2 x N S x M doubles) go back to the device once the operands are built.
+    (2 x rows x M doubles) go back to the device once the operands are built.
     Mixed calls and runs give the bits of a context that keeps both storages,
     and a float64 call is refused with TDSCHA_ERR_STATE."""
     import torch
@@ -238,6 +238,7 @@ def test_fp32_storage_context(gpu_lib, M, N, S):
         ctx = nat.Context(ens["X"], ens["Y"], ens["w"], ens["rho"], ens["T"], syms, spaces, bid,
                           with_mixed=mode)
         outs.append(_mixed_call(ctx, R1, Y1))
+        rows = ctx.layout()[1]      # resident ensemble rows (N when images act on Y1)
         f = np.zeros(M)
         d2v = np.zeros((M, M))
         rc = lib.tdscha_perturb_averages(ctx.handle, R1.ctypes.data, Y1.ctypes.data, 1,
@@ -251,7 +252,9 @@ def test_fp32_storage_context(gpu_lib, M, N, S):
         ctx.close()
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
-    assert free[1] - free[0] >= 2 * N * S * M * 8 // 2
+    released = 2 * rows * M * 8     # float64 D and F rows
+    if released >= 1 << 24:         # well above the device's allocation granularity
+        assert free[1] - free[0] >= released // 2
     nat.check(lib.tdscha_release_cached_memory(None))
     # the Lanczos class: fp32_storage with precision 'mixed', same coefficients
     runs = []
