@@ -2,8 +2,11 @@
 
 The public surface keeps the reference's names, argument meanings and error
 behaviour: ensemble/perturbation setup, `init`, `prepare_perturbation`,
-`prepare_mode`, `prepare_two_ph`, `apply_full_L`, `run_FT`,
-`get_green_function_continued_fraction`, `save_status` / `load_status`,
+`prepare_mode`, `prepare_two_ph`, `prepare_ir`, `prepare_raman`,
+`prepare_unpolarized_raman`, `apply_full_L`, `run_FT`,
+`get_green_function_continued_fraction`, `get_static_frequency`,
+`build_lanczos_matrix_from_coeffs`, `get_alpha1_beta1_wigner`,
+`get_a1_b1_wigner`, `save_status` / `load_status`,
 `save_abc` / `load_abc`, and the attributes `a_coeffs`, `b_coeffs`,
 `c_coeffs`, `basis_Q`, `basis_P`, `s_norm`, `psi`, `use_wigner`,
 `ignore_v3`, `ignore_v4`, `ignore_harmonic`, `reverse_L`, `shift_value`,
@@ -108,6 +111,7 @@ class Lanczos(object):
         self.full_reorth = False
         self.trans_projector = None
         self.trans_cart_perms = None
+        self.dyn = None             # cellconstructor Phonons of the ensemble, when built from one
         self._ctx = None
         self._ctx_key = None
         self._Qd = None
@@ -329,6 +333,138 @@ class Lanczos(object):
         self.psi[M + h:] = pert_b[iu]
         self.perturbation_modulus = self.psi.dot(self.psi * self.mask_dot_wigner())
 
+    # ------------------------------------------ IR / Raman perturbations
+    def _supercell_size(self, n_uc_coords, n_supercell):
+        if self.dyn is not None:
+            return int(np.prod(self.dyn.GetSupercell()))
+        if n_supercell is not None:
+            return int(n_supercell)
+        n_coords = np.shape(self.pols)[0]
+        if n_uc_coords <= 0 or n_coords % n_uc_coords:
+            raise ValueError("cannot infer the supercell: %d Cartesian coordinates, %d per unit cell"
+                             % (n_coords, n_uc_coords))
+        return n_coords // n_uc_coords
+
+    def prepare_ir(self, effective_charges=None, pol_vec=np.array([1, 0, 0]), n_supercell=None):
+        """IR perturbation (:1705-1751): the effective charges (n_atoms_uc, 3, 3; atom,
+        field component, coordinate) contracted with the light polarisation, tiled over
+        the supercell, as a Cartesian vector with masses_exp = -1.  Without a dynamical
+        matrix (self.dyn) the charges must be given; the supercell size is then
+        n_supercell or (Cartesian coordinates of pols) / (3 n_atoms_uc)."""
+        ec = effective_charges
+        if ec is None and self.dyn is not None:
+            ec = self.dyn.effective_charges
+        if ec is None:
+            raise AssertionError("Error, no effective charge found. Cannot initialize IR responce")
+        ec = np.asarray(ec, dtype=np.double)
+        if ec.ndim != 3:
+            raise AssertionError("Error, effective charges of the wrong shape: {}".format(ec.shape))
+        n_sc = self._supercell_size(3 * ec.shape[0], n_supercell)
+        msg = ("Error, effective charges of the wrong shape: {}\nNumber of modes : {}\n"
+               "Dimension of the supercell : {}".format(ec.shape, self.n_modes, n_sc))
+        if not self.ignore_small_w and ec.shape[0] * ec.shape[2] * n_sc != self.n_modes + 3:
+            raise AssertionError(msg)
+        if not ec.shape[1] == ec.shape[2] == 3:
+            raise AssertionError(msg)
+        z_eff = np.einsum("abc, b", ec, pol_vec)
+        self.prepare_perturbation(np.tile(z_eff.ravel(), n_sc), masses_exp=-1)
+
+    def _raman_vector_fn(self, raman_tensor):
+        """Raman vector for two polarisations: the dynamical matrix's GetRamanVector, or
+        sum_ab p_in[a] p_out[b] R[a, b, :] of a given tensor R (3, 3, 3 n_atoms_uc) that
+        already obeys the acoustic sum rule."""
+        if raman_tensor is not None:
+            R = np.asarray(raman_tensor, dtype=np.double)
+            if R.ndim != 3 or R.shape[:2] != (3, 3):
+                raise ValueError("raman_tensor must have shape (3, 3, 3 n_atoms), got %s"
+                                 % (R.shape,))
+            return (lambda p_in, p_out: np.einsum("abc,a,b->c", R, np.asarray(p_in, np.double),
+                                                  np.asarray(p_out, np.double))), R.shape[2]
+        if self.dyn is None or getattr(self.dyn, "raman_tensor", None) is None:
+            raise AssertionError("Error, no Raman tensor found. Cannot initialize the Raman responce")
+        return self.dyn.GetRamanVector, np.shape(self.dyn.raman_tensor)[-1]
+
+    # unpolarised components: (pol_in, pol_out) pairs with their factors, for
+    # alpha^2 = (xx+yy+zz)^2/9, beta_1..3 = (xx-yy)^2/2, (xx-zz)^2/2, (yy-zz)^2/2,
+    # beta_4..6 = 3 xy^2, 3 yz^2, 3 xz^2 (:1115-1175)
+    _THIRD = staticmethod(lambda v: v / 3)
+    _HALF = staticmethod(lambda v: v / np.sqrt(2))
+    _MHALF = staticmethod(lambda v: -v / np.sqrt(2))
+    _SQRT3 = staticmethod(lambda v: v * np.sqrt(3))
+    _UNPOL = {0: ((0, 0, _THIRD), (1, 1, _THIRD), (2, 2, _THIRD)),
+              1: ((0, 0, _HALF), (1, 1, _MHALF)),
+              2: ((0, 0, _HALF), (2, 2, _MHALF)),
+              3: ((1, 1, _HALF), (2, 2, _MHALF)),
+              4: ((0, 1, _SQRT3),),
+              5: ((1, 2, _SQRT3),),
+              6: ((0, 2, _SQRT3),)}
+
+    def prepare_raman(self, pol_vec_in=np.array([1, 0, 0]), pol_vec_out=np.array([1, 0, 0]),
+                      mixed=False, pol_in_2=None, pol_out_2=None, unpolarized=None,
+                      raman_tensor=None, n_supercell=None, sum_components=False):
+        """Raman perturbation (:1061-1182) from the Raman vector of the two polarisations
+        (or of one unpolarised component, 0..6), tiled over the supercell, masses_exp = -1.
+
+        The reference ends with a plain prepare_perturbation of the last vector it built,
+        so `mixed` has no effect and the unpolarised components 0-3 keep only their last
+        term; that result is reproduced by default.  sum_components=True keeps every term
+        (the mixed polarisation pair added, the unpolarised terms summed)."""
+        vec_fn, n_uc_coords = self._raman_vector_fn(raman_tensor)
+        n_sc = self._supercell_size(n_uc_coords, n_supercell)
+        e = np.eye(3)
+        if unpolarized is None:
+            terms = [(pol_vec_in, pol_vec_out, None)]
+            if mixed and sum_components:
+                terms.append((pol_in_2, pol_out_2, None))
+        elif unpolarized in self._UNPOL:
+            terms = [(e[i], e[j], f) for i, j, f in self._UNPOL[unpolarized]]
+        else:
+            raise ValueError("Error, unpolarized must be between [0, ... ,6] got invalid {}."
+                             .format(unpolarized))
+        vecs = []
+        for p_in, p_out, scale in terms:
+            v = np.tile(np.asarray(vec_fn(p_in, p_out)).ravel(), n_sc)
+            vecs.append(v if scale is None else scale(v))
+        if not sum_components:
+            self.prepare_perturbation(vecs[-1], masses_exp=-1)
+            return
+        self.prepare_perturbation(vecs[0], masses_exp=-1)
+        for v in vecs[1:]:
+            self.prepare_perturbation(v, masses_exp=-1, add=True)
+        self.perturbation_modulus = self.psi[:self.n_modes].dot(self.psi[:self.n_modes])
+
+    def get_prefactors_unpolarized_raman(self, index):
+        """Weight of unpolarised component `index` in 45/9 (xx+yy+zz)^2 +
+        7/2 [(xx-yy)^2 + (xx-zz)^2 + (yy-zz)^2] + 21 [xy^2 + xz^2 + yz^2] (:1184-1208)."""
+        labels = list(range(7))
+        if index not in labels:
+            raise ValueError('{} should be in {}'.format(index, labels))
+        return (45 / 9, 7 / 2, 7 / 2, 7 / 2, 7 * 3, 7 * 3, 7 * 3)[index]
+
+    # components of prepare_unpolarized_raman: xx+yy+zz, xx-yy, xx-zz, yy-zz, xy, xz, yz
+    _UNPOL_SUM = {0: ((0, 0, 1), (1, 1, 1), (2, 2, 1)), 1: ((0, 0, 1), (1, 1, -1)),
+                  2: ((0, 0, 1), (2, 2, -1)), 3: ((1, 1, 1), (2, 2, -1)),
+                  4: ((0, 1, 1),), 5: ((0, 2, 1),), 6: ((1, 2, 1),)}
+
+    def prepare_unpolarized_raman(self, index=0, debug=False, raman_tensor=None,
+                                  n_supercell=None):
+        """Perturbation of unpolarised Raman component `index` (:1210-1278): the summed
+        (or differenced) Raman vectors of the component, tiled over the supercell,
+        masses_exp = -1.  debug saves the unit-cell vector as raman_v_<index>.npy."""
+        vec_fn, n_uc_coords = self._raman_vector_fn(raman_tensor)
+        labels = list(range(7))
+        if index not in labels:
+            raise ValueError('{} should be in {}'.format(index, labels))
+        e = np.eye(3)
+        raman_v = None
+        for i, j, sgn in self._UNPOL_SUM[index]:
+            v = np.asarray(vec_fn(e[i], e[j]), dtype=np.double)
+            raman_v = v.copy() if raman_v is None else (raman_v + v if sgn > 0 else raman_v - v)
+        if debug:
+            np.save('raman_v_{}'.format(index), raman_v)
+        n_sc = self._supercell_size(n_uc_coords, n_supercell)
+        self.prepare_perturbation(np.tile(raman_v.ravel(), n_sc), masses_exp=-1)
+
     def set_max_frequency(self, freq):
         """Reverse-and-shift setup (:2227-2253)."""
         self.shift_value = 4 * freq * freq
@@ -379,6 +515,52 @@ class Lanczos(object):
     def get_ReA1(self, half_off_diagonal=False):
         return self._sym_from_sector(self.n_modes + self.n_modes * (self.n_modes + 1) // 2,
                                      half_off_diagonal)
+
+    def _wigner_pair_factors(self):
+        """Per mode pair (i <= j, row-major like the psi sectors): X = (1+2n_i)(1+2n_j)/8,
+        w_i w_j, chi^- and chi^+ (:2816-2836, :2732-2752)."""
+        iu = np.triu_indices(self.n_modes)
+        w_i, w_j = self.w[iu[0]], self.w[iu[1]]
+        n_i = n_j = 0
+        if self.T > 0:
+            kT = np.double(self.T / __RyToK__)
+            n_i = 1 / (np.exp(w_i / kT) - 1)
+            n_j = 1 / (np.exp(w_j / kT) - 1)
+        X = (1 + 2 * n_i) * (1 + 2 * n_j) / 8
+        ww = w_i * w_j
+        chi_m = (w_j - w_i) * (n_j - n_i) / (2 * ww)
+        chi_p = (w_j + w_i) * (1 + n_j + n_i) / (2 * ww)
+        return iu, X, ww, chi_m, chi_p
+
+    def get_alpha1_beta1_wigner(self, get_alpha=True):
+        """Upsilon^(1) = alpha^(1) (get_alpha) or beta^(1) as (n_modes, n_modes) matrices
+        from the Wigner sectors a'^(1), b'^(1) of psi (:2773-2882):
+        alpha = w_i w_j / X (sqrt(-chi^-/2) a' - sqrt(chi^+/2) b'),
+        beta = (sqrt(-chi^-/2) a' + sqrt(chi^+/2) b') / X."""
+        M = self.n_modes
+        h = M * (M + 1) // 2
+        iu, X, ww, chi_m, chi_p = self._wigner_pair_factors()
+        a_sec = np.asarray(self.psi[M:M + h])
+        b_sec = np.asarray(self.psi[M + h:])
+        if get_alpha:
+            packed = (ww / X) * np.sqrt(-0.5 * chi_m) * a_sec - (ww / X) * np.sqrt(0.5 * chi_p) * b_sec
+        else:
+            packed = (np.sqrt(-0.5 * chi_m) / X) * a_sec + (np.sqrt(0.5 * chi_p) / X) * b_sec
+        out = np.zeros((M, M), dtype=np.double)
+        out[iu] = packed
+        out.T[iu] = packed
+        return out
+
+    def get_a1_b1_wigner(self, get_a1=True):
+        """The inverse change of variables (:2690-2771): sqrt(-chi^-/2) a' (get_a1) or b'
+        as upper-triangle vectors of length n_modes (n_modes + 1) / 2, from the
+        alpha^(1) and beta^(1) of get_alpha1_beta1_wigner."""
+        iu, X, ww, chi_m, chi_p = self._wigner_pair_factors()
+        alpha1 = self.get_alpha1_beta1_wigner(get_alpha=True)[iu]
+        beta1 = self.get_alpha1_beta1_wigner(get_alpha=False)[iu]
+        if get_a1:
+            return 0.5 * X * (alpha1 / ww + beta1)
+        return -0.5 * X * (alpha1 / ww - beta1) / np.sqrt(0.5 * chi_p)
 
     # ------------------------------------------------------------ device side
     def _context(self):
@@ -767,6 +949,40 @@ class Lanczos(object):
             float(self.shift_value), 1 if use_terminator else 0, int(last_average),
             float(smearing), int(smooth_ramp), nat.dp(out)))
         return (out[0::2] + 1j * out[1::2]).reshape(w_array.shape)
+
+    def get_static_frequency(self, smearing=0):
+        """sign(w2) sqrt(|w2|) with w2 = 1 / Re G(w = 0 + i smearing), G the continued
+        fraction without terminator (:5424-5461): the free-energy curvature along the
+        perturbation, negative when it is unstable.  Returned in the reference's form
+        (a one-element float64 array)."""
+        gf = self.get_green_function_continued_fraction(np.array([0]), False, smearing=smearing)
+        w2 = 1 / np.real(gf)
+        return np.float64(np.sqrt(np.abs(w2)) * np.sign(w2))
+
+    def build_lanczos_matrix_from_coeffs(self, use_arnoldi=False):
+        """The tridiagonal Lanczos matrix (a on the diagonal, b below, c above, b above
+        when no c were produced), or the symmetric matrix of the stored Arnoldi rows;
+        reversed and shifted as the operator was (:4652-4693)."""
+        n = len(self.a_coeffs)
+        if use_arnoldi:
+            if not len(self.b_coeffs) > len(self.c_coeffs):
+                raise AssertionError("Error, cannot Arnoldi with non-symmetric Lanczos not implemented")
+            matrix = np.zeros((n, n), dtype=TYPE_DP)
+            for i in range(n):
+                matrix[:i + 1, i] = self.arnoldi_matrix[i]
+                matrix[i, :i + 1] = self.arnoldi_matrix[i]
+        else:
+            a = np.asarray(self.a_coeffs, dtype=TYPE_DP)
+            b = np.asarray(self.b_coeffs, dtype=TYPE_DP)[:max(n - 1, 0)]
+            up = b if len(self.c_coeffs) != len(self.b_coeffs) else \
+                np.asarray(self.c_coeffs, dtype=TYPE_DP)[:max(n - 1, 0)]
+            matrix = np.diag(a) + np.diag(b, -1) + np.diag(up, 1)
+        sign = -1 if self.reverse_L else 1
+        return sign * matrix - sign * np.eye(n) * self.shift_value
+
+    def run(self, n_iter, save_dir=".", verbose=True):
+        """Deprecated in the reference (:4497-4517): use run_FT."""
+        raise ValueError("Error, this run funciton has been deprecated, use run_FT instead.")
 
     # ------------------------------------------- input files of the executable
     def prepare_input_files(self, root_name="tdscha", n_steps=100, start_from_scratch=True,

@@ -180,6 +180,98 @@ def input_files_case(fname, M, N, S, seed):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+class _DynStub:
+    """The three members of a cellconstructor Phonons object that the
+    reference's IR / Raman perturbation builders read: effective charges,
+    the supercell, and the Raman vector (here the plain contraction of a
+    given Raman tensor with the two polarisations)."""
+
+    def __init__(self, ec, raman, supercell):
+        self.effective_charges = ec
+        self.raman_tensor = raman
+        self._sc = supercell
+
+    def GetSupercell(self):
+        return self._sc
+
+    def GetRamanVector(self, p_in, p_out):
+        return np.einsum("abc,a,b->c", self.raman_tensor, p_in, p_out)
+
+
+def host_helpers_case(fname, seed):
+    """Host-side Lanczos helpers: Wigner change of variables, the Lanczos
+    matrix, the static frequency and the IR / Raman perturbation builders."""
+    nat_uc, supercell = 2, (2, 1, 1)
+    nat_sc = nat_uc * int(np.prod(supercell))
+    M = 3 * nat_sc - 3
+    ens = make_ensemble(M, 6, seed=seed, n_syms=1, rho_sigma=0.0)
+    rng = np.random.default_rng(seed + 1)
+    q, _ = np.linalg.qr(rng.standard_normal((3 * nat_sc, 3 * nat_sc)))
+    pols = np.ascontiguousarray(q[:, :M])
+    m = np.repeat(rng.uniform(1e3, 1e5, nat_sc), 3)
+    ec = rng.standard_normal((nat_uc, 3, 3))
+    raman = rng.standard_normal((3, 3, 3 * nat_uc))
+    out = dict(w=ens["w"], T=ens["T"], X=ens["X"], Y=ens["Y"], rho=ens["rho"], pols=pols, m=m,
+               ec=ec, raman=raman, supercell=np.array(supercell))
+    lanc = make_reference_lanczos(ens, use_wigner=True)
+    lanc.pols, lanc.m = pols, m
+    lanc.dyn = _DynStub(ec, raman, supercell)
+    psi = rng.standard_normal(M + M * (M + 1))
+    out["psi"] = psi
+    for tag, T in (("T", float(ens["T"])), ("T0", 0.0)):
+        lanc.T = T
+        lanc.psi = psi.copy()
+        out["alpha1/" + tag] = lanc.get_alpha1_beta1_wigner(get_alpha=True)
+        out["beta1/" + tag] = lanc.get_alpha1_beta1_wigner(get_alpha=False)
+        out["a1/" + tag] = lanc.get_a1_b1_wigner(get_a1=True)
+        out["b1/" + tag] = lanc.get_a1_b1_wigner(get_a1=False)
+    lanc.T = float(ens["T"])
+
+    def pert(key, fn, *a, **k):
+        with contextlib.redirect_stdout(io.StringIO()):
+            fn(*a, **k)
+        out["psi/" + key] = lanc.psi[:M].copy()
+        out["mod/" + key] = np.float64(lanc.perturbation_modulus)
+
+    e = np.eye(3)
+    pert("ir_x", lanc.prepare_ir, pol_vec=e[0])
+    pert("ir_mix", lanc.prepare_ir, effective_charges=2 * ec, pol_vec=np.array([0.3, -0.5, 0.8]))
+    pert("raman_xy", lanc.prepare_raman, pol_vec_in=e[0], pol_vec_out=e[1])
+    pert("raman_mixed", lanc.prepare_raman, pol_vec_in=e[0], pol_vec_out=e[2], mixed=True,
+         pol_in_2=e[1], pol_out_2=e[1])
+    for k in range(7):
+        pert("raman_unpol%d" % k, lanc.prepare_raman, unpolarized=k)
+        pert("unpol%d" % k, lanc.prepare_unpolarized_raman, index=k)
+        out["prefactor%d" % k] = np.float64(lanc.get_prefactors_unpolarized_raman(k))
+
+    # the Lanczos matrix from given coefficients, both kinds, with and without reversal
+    n = 6
+    a, b, c = rng.standard_normal(n), rng.standard_normal(n - 1), rng.standard_normal(n - 1)
+    out.update(coef_a=a, coef_b=b, coef_c=c)
+    for tag, cc, rev, shift in (("bi", c, False, 0.0), ("sym", [], False, 0.0),
+                                ("bi_rev", c, True, 0.7)):
+        lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs = list(a), list(b), list(cc)
+        lanc.reverse_L, lanc.shift_value = rev, shift
+        out["matrix/" + tag] = lanc.build_lanczos_matrix_from_coeffs()
+    lanc.reverse_L, lanc.shift_value = False, 0.0
+
+    # static frequency from the coefficients of the 50-step reference runs
+    run = np.load(os.path.join(HERE, "runft_m21_n1000.npz"))
+    R1 = run["R1"]
+    for tag, wig in (("bilanczos", False), ("wigner", True)):
+        lanc.use_wigner = wig
+        lanc.a_coeffs = list(run[tag + "/a"])
+        lanc.b_coeffs = list(run[tag + "/b"])
+        lanc.c_coeffs = list(run[tag + "/c"])
+        lanc.perturbation_modulus = float(R1.dot(R1))
+        for k, sm in enumerate((0.0, 1e-5)):
+            with contextlib.redirect_stdout(io.StringIO()):
+                out["wstatic/%s/%d" % (tag, k)] = np.asarray(lanc.get_static_frequency(sm))
+    out["wstatic_smearing"] = np.array([0.0, 1e-5])
+    out["wstatic_modulus"] = np.float64(R1.dot(R1))
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -191,6 +283,7 @@ def main():
              [("bilanczos", False, True), ("wigner", True, True)])
     static_case("static_m12_n800.npz", 12, 800, 41, 25)
     input_files_case("input_files_m6_n5_s48.npz", 6, 5, 48, 51)
+    host_helpers_case("host_helpers_m9.npz", 61)
     print("fixtures written to", HERE)
 
 

@@ -1,0 +1,148 @@
+"""Host-side Lanczos helpers against the reference's own outputs
+(tests/golden/host_helpers_m9.npz, written by make_golden.py from
+Modules/DynamicalLanczos.py): the Wigner change of variables
+(get_alpha1_beta1_wigner / get_a1_b1_wigner), the IR and Raman perturbation
+builders, the Lanczos matrix and the static frequency.  No GPU: the static
+frequency's continued fraction comes from the oracle here (the product
+evaluates it on the GPU; tests/test_gpu_fp64.py covers that path)."""
+import numpy as np
+import pytest
+
+import oracle
+from tdscha_gb300.DynamicalLanczos import Lanczos
+
+
+class _Dyn:
+    """The members of a dynamical matrix the IR / Raman builders read."""
+
+    def __init__(self, ec, raman, supercell):
+        self.effective_charges = ec
+        self.raman_tensor = raman
+        self._sc = tuple(supercell)
+
+    def GetSupercell(self):
+        return self._sc
+
+    def GetRamanVector(self, p_in, p_out):
+        return np.einsum("abc,a,b->c", self.raman_tensor, p_in, p_out)
+
+
+@pytest.fixture
+def case(golden):
+    d = golden("host_helpers_m9.npz")
+    lanc = Lanczos.from_arrays(d["X"], d["Y"], d["w"], d["rho"], float(d["T"]), pols=d["pols"],
+                               m=d["m"])
+    return d, lanc
+
+
+@pytest.mark.parametrize("tag", ["T", "T0"])
+def test_wigner_change_of_variables(case, tag):
+    d, lanc = case
+    lanc.T = float(d["T"]) if tag == "T" else 0.0
+    lanc.psi = d["psi"].copy()
+    np.testing.assert_array_equal(lanc.get_alpha1_beta1_wigner(True), d["alpha1/" + tag])
+    np.testing.assert_array_equal(lanc.get_alpha1_beta1_wigner(False), d["beta1/" + tag])
+    np.testing.assert_array_equal(lanc.get_a1_b1_wigner(True), d["a1/" + tag])
+    np.testing.assert_array_equal(lanc.get_a1_b1_wigner(False), d["b1/" + tag])
+
+
+def _check(lanc, d, key):
+    M = lanc.n_modes
+    np.testing.assert_allclose(lanc.psi[:M], d["psi/" + key], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(lanc.perturbation_modulus, d["mod/" + key], rtol=1e-13)
+
+
+@pytest.mark.parametrize("with_dyn", [True, False])
+def test_ir_and_raman_builders(case, with_dyn):
+    d, lanc = case
+    ec, raman = d["ec"], d["raman"]
+    e = np.eye(3)
+    if with_dyn:
+        lanc.dyn = _Dyn(ec, raman, d["supercell"])
+        kw_ir, kw_r = {}, {}
+    else:
+        # no dynamical matrix: arrays, supercell size inferred from pols
+        kw_ir, kw_r = {"effective_charges": ec}, {"raman_tensor": raman}
+    lanc.prepare_ir(pol_vec=e[0], **kw_ir)
+    _check(lanc, d, "ir_x")
+    lanc.prepare_ir(effective_charges=2 * ec, pol_vec=np.array([0.3, -0.5, 0.8]))
+    _check(lanc, d, "ir_mix")
+    lanc.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[1], **kw_r)
+    _check(lanc, d, "raman_xy")
+    lanc.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[2], mixed=True, pol_in_2=e[1],
+                       pol_out_2=e[1], **kw_r)
+    _check(lanc, d, "raman_mixed")
+    for k in range(7):
+        lanc.prepare_raman(unpolarized=k, **kw_r)
+        _check(lanc, d, "raman_unpol%d" % k)
+        lanc.prepare_unpolarized_raman(index=k, **kw_r)
+        _check(lanc, d, "unpol%d" % k)
+        assert lanc.get_prefactors_unpolarized_raman(k) == d["prefactor%d" % k]
+
+
+def test_raman_sum_components(case):
+    """sum_components keeps every term the reference drops (its final
+    prepare_perturbation overwrites the accumulated vector)."""
+    d, lanc = case
+    raman = d["raman"]
+    e = np.eye(3)
+    lanc.prepare_raman(unpolarized=0, raman_tensor=raman, sum_components=True)
+    summed = lanc.psi[:lanc.n_modes].copy()
+    # (xx + yy + zz) / 3 = the unpolarised component 0 of prepare_unpolarized_raman / 3
+    lanc.prepare_unpolarized_raman(index=0, raman_tensor=raman)
+    np.testing.assert_allclose(summed, lanc.psi[:lanc.n_modes] / 3, rtol=1e-12, atol=1e-300)
+    lanc.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[2], mixed=True, pol_in_2=e[1],
+                       pol_out_2=e[1], raman_tensor=raman, sum_components=True)
+    both = lanc.psi[:lanc.n_modes].copy()
+    lanc.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[2], raman_tensor=raman)
+    xz = lanc.psi[:lanc.n_modes].copy()
+    lanc.prepare_raman(pol_vec_in=e[1], pol_vec_out=e[1], raman_tensor=raman)
+    np.testing.assert_allclose(both, xz + lanc.psi[:lanc.n_modes], rtol=1e-12, atol=1e-300)
+
+
+def test_builder_errors(case):
+    d, lanc = case
+    with pytest.raises(AssertionError):
+        lanc.prepare_ir()                       # no charges, no dynamical matrix
+    with pytest.raises(AssertionError):
+        lanc.prepare_raman()                    # no Raman tensor
+    with pytest.raises(AssertionError):       # 2 atoms x 3 x 3 cells != n_modes + 3
+        lanc.prepare_ir(effective_charges=np.zeros((2, 3, 3)), n_supercell=3)
+    with pytest.raises(ValueError):           # 12 coordinates are not whole cells of 9
+        lanc.prepare_ir(effective_charges=np.zeros((3, 3, 3)))
+    with pytest.raises(ValueError):
+        lanc.prepare_raman(unpolarized=7, raman_tensor=d["raman"])
+    with pytest.raises(ValueError):
+        lanc.get_prefactors_unpolarized_raman(9)
+    with pytest.raises(ValueError):
+        lanc.run(3)
+
+
+@pytest.mark.parametrize("tag", ["bi", "sym", "bi_rev"])
+def test_lanczos_matrix(case, tag):
+    d, lanc = case
+    lanc.a_coeffs = list(d["coef_a"])
+    lanc.b_coeffs = list(d["coef_b"])
+    lanc.c_coeffs = [] if tag == "sym" else list(d["coef_c"])
+    lanc.reverse_L, lanc.shift_value = (True, 0.7) if tag == "bi_rev" else (False, 0.0)
+    np.testing.assert_array_equal(lanc.build_lanczos_matrix_from_coeffs(), d["matrix/" + tag])
+
+
+@pytest.mark.parametrize("tag,wig", [("bilanczos", False), ("wigner", True)])
+def test_static_frequency(case, golden, monkeypatch, tag, wig):
+    d, lanc = case
+    run = golden("runft_m21_n1000.npz")
+    lanc.use_wigner = wig
+    lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs = (list(run[tag + "/a"]), list(run[tag + "/b"]),
+                                                   list(run[tag + "/c"]))
+    lanc.perturbation_modulus = float(d["wstatic_modulus"])
+
+    def cf(w, use_terminator=True, smearing=0.0):
+        return oracle.continued_fraction(lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs, w,
+                                         lanc.use_wigner, lanc.perturbation_modulus,
+                                         use_terminator=use_terminator, smearing=smearing)
+
+    monkeypatch.setattr(lanc, "get_green_function_continued_fraction", cf)
+    for k, sm in enumerate(d["wstatic_smearing"]):
+        got = lanc.get_static_frequency(float(sm))
+        np.testing.assert_allclose(got, d["wstatic/%s/%d" % (tag, k)], rtol=1e-12)
