@@ -469,6 +469,66 @@ class QSpaceLanczos(Lanczos):
         self.psi[:self.n_bands] += R1
         self.perturbation_modulus = float(np.real(np.conj(R1) @ R1))
 
+    # ------------------------------------------ IR / Raman perturbations (at Gamma)
+    def _gamma_cells(self, n_supercell):
+        """Cells of the supercell: the dynamical matrix's, n_supercell, or the q grid size."""
+        if self.dyn is not None:
+            return int(np.prod(self.dyn.GetSupercell()))
+        if n_supercell is not None:
+            return int(n_supercell)
+        return int(self.n_q)
+
+    def prepare_ir(self, effective_charges=None, pol_vec=np.array([1.0, 0.0, 0.0]),
+                   n_supercell=None):
+        """IR perturbation at Gamma (QSpaceLanczos.py:1205-1237): the effective charges
+        contracted with the light polarisation, times sqrt(cells), projected on the
+        q = 0 modes by prepare_perturbation_q."""
+        ec = effective_charges
+        if ec is None and self.dyn is not None:
+            ec = self.dyn.effective_charges
+        if ec is None:
+            raise AssertionError("Error, no effective charge found. Cannot initialize IR responce")
+        z_eff = np.einsum("abc, b", np.asarray(ec, dtype=np.double), pol_vec)
+        self.prepare_perturbation_q(0, z_eff.ravel() * np.sqrt(self._gamma_cells(n_supercell)))
+
+    def prepare_raman(self, pol_vec_in=np.array([1.0, 0.0, 0.0]),
+                      pol_vec_out=np.array([1.0, 0.0, 0.0]), mixed=False, pol_in_2=None,
+                      pol_out_2=None, unpolarized=None, raman_tensor=None, n_supercell=None):
+        """Raman perturbation at Gamma (QSpaceLanczos.py:1239-1355): the Raman vector of
+        the two polarisations (plus the second pair when mixed), or the terms of
+        unpolarised component 0..6 summed, each times sqrt(cells)."""
+        vec_fn, _ = self._raman_vector_fn(raman_tensor)
+        root = np.sqrt(self._gamma_cells(n_supercell))
+        if unpolarized is None:
+            raman_v = np.array(vec_fn(pol_vec_in, pol_vec_out), dtype=np.double)
+            if mixed:
+                raman_v += vec_fn(pol_in_2, pol_out_2)
+            self.prepare_perturbation_q(0, raman_v.ravel() * root)
+            return
+        if unpolarized not in self._UNPOL:
+            raise ValueError("Error, unpolarized must be between [0, ..., 6] got invalid {}."
+                             .format(unpolarized))
+        e = np.eye(3)
+        for k, (i, j, scale) in enumerate(self._UNPOL[unpolarized]):
+            v = np.asarray(vec_fn(e[i], e[j]), dtype=np.double).ravel() * root
+            self.prepare_perturbation_q(0, scale(v), add=k > 0)
+
+    def prepare_unpolarized_raman(self, index=0, debug=False, raman_tensor=None,
+                                  n_supercell=None):
+        """Unpolarised Raman component `index` at Gamma (QSpaceLanczos.py:1357-1426),
+        without the prefactor of get_prefactors_unpolarized_raman."""
+        vec_fn, _ = self._raman_vector_fn(raman_tensor)
+        if index not in range(7):
+            raise ValueError('{} should be in {}'.format(index, list(range(7))))
+        e = np.eye(3)
+        raman_v = None
+        for i, j, sgn in self._UNPOL_SUM[index]:
+            v = np.asarray(vec_fn(e[i], e[j]), dtype=np.double)
+            raman_v = v.copy() if raman_v is None else (raman_v + v if sgn > 0 else raman_v - v)
+        if debug:
+            np.save('raman_v_{}'.format(index), raman_v)
+        self.prepare_perturbation_q(0, raman_v.ravel() * np.sqrt(self._gamma_cells(n_supercell)))
+
     def prepare_symmetrization(self, no_sym=False, verbose=True, symmetries=None):
         """q-space symmetry matrices (:1472-1531).  symmetries: list of (n_q n_bands)^2
         complex matrices (dense or scipy.sparse) acting on vectors indexed

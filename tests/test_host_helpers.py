@@ -146,3 +146,45 @@ def test_static_frequency(case, golden, monkeypatch, tag, wig):
     for k, sm in enumerate(d["wstatic_smearing"]):
         got = lanc.get_static_frequency(float(sm))
         np.testing.assert_allclose(got, d["wstatic/%s/%d" % (tag, k)], rtol=1e-12)
+
+
+def _qspace(seed=3):
+    from tdscha_gb300.QSpaceLanczos import QSpaceLanczos
+    rng = np.random.default_rng(seed)
+    n_q, N, nb = 2, 4, 6
+    X = rng.standard_normal((n_q, N, nb)) + 1j * rng.standard_normal((n_q, N, nb))
+    w_q = rng.uniform(1e-3, 3e-3, (nb, n_q))
+    q, _ = np.linalg.qr(rng.standard_normal((nb, nb)) + 1j * rng.standard_normal((nb, nb)))
+    pols_q = np.stack([q, np.conj(q)], axis=2)
+    m = np.repeat(rng.uniform(1e3, 1e5, nb // 3), 3)
+    ql = QSpaceLanczos.from_arrays(X, X.copy(), w_q, np.ones(N), 100.0,
+                                   q_points=np.array([[0, 0, 0], [0.5, 0, 0]]), pols_q=pols_q, m=m)
+    return ql, pols_q, m, rng
+
+
+def test_qspace_ir_and_raman_at_gamma():
+    """The q-space builders project on the q = 0 modes (QSpaceLanczos.py:1205-1451):
+    R1 = conj(pols_q[:, :, 0])^T (v sqrt(cells) / sqrt(m)), the unpolarised terms
+    summed (the q-space reference keeps every term), cells = the q grid size."""
+    ql, pols_q, m, rng = _qspace()
+    ec = rng.standard_normal((2, 3, 3))
+    raman = rng.standard_normal((3, 3, 6))
+    e = np.eye(3)
+    proj = lambda v: np.conj(pols_q[:, :, 0]).T @ (v * np.sqrt(2) / np.sqrt(m))
+    pol = np.array([0.2, 0.9, -0.4])
+    ql.prepare_ir(effective_charges=ec, pol_vec=pol)
+    np.testing.assert_allclose(ql.psi[:6], proj(np.einsum("abc,b", ec, pol).ravel()),
+                               rtol=1e-13)
+    rv = lambda a, b: np.einsum("abc,a,b->c", raman, e[a], e[b])
+    ql.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[2], mixed=True, pol_in_2=e[1],
+                     pol_out_2=e[1], raman_tensor=raman)
+    np.testing.assert_allclose(ql.psi[:6], proj(rv(0, 2) + rv(1, 1)), rtol=1e-13)
+    for k, want in ((0, (rv(0, 0) + rv(1, 1) + rv(2, 2)) / 3),
+                    (1, (rv(0, 0) - rv(1, 1)) / np.sqrt(2)),
+                    (5, rv(1, 2) * np.sqrt(3))):
+        ql.prepare_raman(unpolarized=k, raman_tensor=raman)
+        np.testing.assert_allclose(ql.psi[:6], proj(want), rtol=1e-12, atol=1e-300)
+    ql.prepare_unpolarized_raman(index=3, raman_tensor=raman)
+    np.testing.assert_allclose(ql.psi[:6], proj(rv(1, 1) - rv(2, 2)), rtol=1e-12, atol=1e-300)
+    # the rest of psi stays zero: a Gamma perturbation of the R sector only
+    assert not np.any(ql.psi[6:])
