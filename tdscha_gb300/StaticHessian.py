@@ -174,6 +174,67 @@ class StaticHessian(object):
             print("Total time to converge: {:.2f} s".format(t2 - t1))
             print()
 
+    def run_no_mode_mixing(self, nsteps, save_dir=None, restart_from_file=False, noq=False):
+        """Hessian without mode mixing (:403-496): one Lanczos run per mode of the
+        auxiliary force constants (prepare_mode, run_FT on the GPU), G_ii = Re G(0) of
+        its continued fraction without terminator, W = 0.  A mode degenerate with the
+        one before it (|w_i - w_{i-1}| < 1e-10) is not run again and takes that run's
+        G(0).  save_dir keeps each run's steps and final status
+        (<prefix>_M<i>_conv), from which restart_from_file resumes.  Returns
+        retrieve_hessian(noq)."""
+        lanc = self.lanczos
+        M = lanc.n_modes
+        Gw = np.zeros((M, M), dtype=np.double)
+        if save_dir is not None and not os.path.exists(save_dir):
+            os.makedirs(save_dir)
+        for i in range(M):
+            if i > 0 and np.abs(lanc.w[i - 1] - lanc.w[i]) < 1e-10:
+                if self.verbose:
+                    print("SKIPPING MODE {} (Degeneracy)".format(i + 1))
+            else:
+                lanc.prepare_mode(i)
+                if self.verbose:
+                    head = "RUNNING MODE {} out of {}".format(i + 1, M)
+                    print("\n" + head + "\n" + "-" * len(head) + "\n")
+                todo = nsteps
+                tag = self.prefix + "_M{:d}".format(i + 1)
+                final = None if save_dir is None else os.path.join(save_dir, tag + "_conv")
+                if save_dir is not None and restart_from_file:
+                    self._resume_mode(final, save_dir, tag)
+                    if len(lanc.a_coeffs):
+                        todo = nsteps - len(lanc.a_coeffs)
+                if todo > 0:
+                    lanc.run_FT(todo, save_dir=save_dir, verbose=self.verbose, prefix=tag)
+                if final is not None:
+                    lanc.save_status(final)
+            gf0 = lanc.get_green_function_continued_fraction(np.array([0]), use_terminator=False,
+                                                             smearing=0)[0]
+            Gw[i, i] = np.real(gf0)
+        W = np.zeros((M, M, M), dtype=np.double)
+        self.preconitioned = False
+        self.vector = self.get_vector(Gw, W)
+        return self.retrieve_hessian(noq=noq)
+
+    def _resume_mode(self, final, save_dir, tag):
+        """Load a mode's final status, else its latest <tag>_STEP<n>.npz (:463-480).
+        The final status is looked up with its .npz suffix and the step files by
+        "<tag>_STEP", so that mode 1 does not pick up the files of modes 10-19."""
+        lanc = self.lanczos
+        for name in (final, final + ".npz"):
+            if os.path.exists(name):
+                if self.verbose:
+                    print("Loading from {}...".format(name))
+                lanc.load_status(name)
+                return
+        steps = [x for x in os.listdir(save_dir)
+                 if x.startswith(tag + "_STEP") and x.endswith(".npz")]
+        if steps:
+            count = [int(x.split(".")[-2].split("STEP")[-1]) for x in steps]
+            name = os.path.join(save_dir, steps[int(np.argmax(count))])
+            if self.verbose:
+                print("Loading from {}...".format(name))
+            lanc.load_status(name)
+
     # ------------------------------------------------------------- layout
     def get_G_W(self, vector, ignore_W=False):
         """G (symmetric) and W (fully symmetric) from the vector (:625-658)."""

@@ -272,6 +272,54 @@ def host_helpers_case(fname, seed):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def fake_lanczos_run(lanc, A, B, C, calls):
+    """A run_FT stand-in for the host logic of StaticHessian.run_no_mode_mixing:
+    the coefficients of the prepared mode (psi[index] = 1) from the tables A, B, C
+    (n_modes x steps); every call is recorded."""
+    M = A.shape[0]
+
+    def run_FT(n_iter, save_dir=None, verbose=True, prefix="LANCZOS", **kw):
+        i = int(np.argmax(np.abs(np.asarray(lanc.psi[:M]))))
+        calls.append((i, int(n_iter), prefix))
+        lanc.a_coeffs = list(A[i, :n_iter])
+        lanc.b_coeffs = list(B[i, :n_iter])
+        lanc.c_coeffs = list(C[i, :n_iter])
+    return run_FT
+
+
+def no_mode_mixing_case(fname, M, seed, n_steps):
+    """The reference's StaticHessian.run_no_mode_mixing with run_FT replaced by
+    fake_lanczos_run (the host logic: modes, degeneracy skips, G(0) of the
+    continued fraction without terminator, the Hessian from the diagonal G)."""
+    import importlib
+    load_reference()
+    SH = importlib.import_module("tdscha.StaticHessian")
+    ens = make_ensemble(M, 8, seed=seed, n_syms=1, rho_sigma=0.0)
+    w = np.sort(ens["w"].copy())
+    w[2] = w[1]                              # a degenerate pair: the second is skipped
+    ens = dict(ens, w=w)
+    lanc = make_reference_lanczos(ens, use_wigner=True)
+    rng = np.random.default_rng(seed + 1)
+    A = (w ** 2)[:, None] * rng.uniform(0.8, 1.2, (M, n_steps))
+    B = (w ** 2)[:, None] * rng.uniform(0.05, 0.2, (M, n_steps))
+    C = (w ** 2)[:, None] * rng.uniform(0.05, 0.2, (M, n_steps))
+    calls = []
+    # past the reference's attribute guard: an instance attribute shadows the method
+    object.__setattr__(lanc, "run_FT", fake_lanczos_run(lanc, A, B, C, calls))
+    sh = SH.StaticHessian()
+    sh.lanczos = lanc
+    sh.verbose = False
+    with contextlib.redirect_stdout(io.StringIO()):
+        try:
+            sh.run_no_mode_mixing(n_steps)
+        except AttributeError:
+            pass    # the final retrieve_hessian() builds a cellconstructor Phonons object
+    out = dict(w=w, X=ens["X"], Y=ens["Y"], rho=ens["rho"], T=ens["T"], A=A, B=B, C=C,
+               n_steps=n_steps, vector=np.asarray(sh.vector),
+               hessian=sh.retrieve_hessian(noq=True), calls=np.array([c[:2] for c in calls]))
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -284,6 +332,7 @@ def main():
     static_case("static_m12_n800.npz", 12, 800, 41, 25)
     input_files_case("input_files_m6_n5_s48.npz", 6, 5, 48, 51)
     host_helpers_case("host_helpers_m9.npz", 61)
+    no_mode_mixing_case("no_mode_mixing_m5.npz", 5, 71, 12)
     print("fixtures written to", HERE)
 
 

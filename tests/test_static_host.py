@@ -77,3 +77,53 @@ def test_batched_minimum_residual_equals_sequential():
         x, it, c = oracle.minimum_residual(lambda v: A @ v, B[r], B[r].copy(), 100, 1e-10)
         np.testing.assert_allclose(X[r].numpy(), x, rtol=1e-10, atol=1e-12)
         assert iters[r] == it and conv[r] == c
+
+
+def _fake_run(lanc, A, B, C, calls):
+    """run_FT stand-in: the prepared mode's coefficients from the tables (the
+    generator of tests/golden/no_mode_mixing_m5.npz uses the same rule)."""
+    M = A.shape[0]
+
+    def run_FT(n_iter, save_dir=None, verbose=True, prefix="LANCZOS", **kw):
+        i = int(np.argmax(np.abs(np.asarray(lanc.psi[:M]))))
+        calls.append((i, int(n_iter)))
+        lanc.a_coeffs = list(A[i, :n_iter])
+        lanc.b_coeffs = list(B[i, :n_iter])
+        lanc.c_coeffs = list(C[i, :n_iter])
+    return run_FT
+
+
+def test_run_no_mode_mixing_matches_reference(golden, tmp_path):
+    """StaticHessian.run_no_mode_mixing's host logic against the reference's, both
+    driven by the same stand-in run: modes run and skipped (a degenerate pair),
+    G(0) of the continued fraction without terminator, vector and Hessian."""
+    import oracle
+    from tdscha_gb300.DynamicalLanczos import Lanczos
+    d = golden("no_mode_mixing_m5.npz")
+    lanc = Lanczos.from_arrays(d["X"], d["Y"], d["w"], d["rho"], float(d["T"]), use_wigner=True)
+    calls = []
+    lanc.run_FT = _fake_run(lanc, d["A"], d["B"], d["C"], calls)
+
+    def cf(w, use_terminator=True, smearing=0.0):
+        return oracle.continued_fraction(lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs, w,
+                                         lanc.use_wigner, lanc.perturbation_modulus,
+                                         use_terminator=use_terminator, smearing=smearing)
+
+    lanc.get_green_function_continued_fraction = cf
+    sh = StaticHessian()
+    sh.lanczos = lanc
+    hess = sh.run_no_mode_mixing(int(d["n_steps"]), noq=True)
+    assert [c[0] for c in calls] == list(d["calls"][:, 0])
+    np.testing.assert_allclose(sh.vector, d["vector"], rtol=1e-12)
+    np.testing.assert_allclose(hess, d["hessian"], rtol=1e-11)
+    assert sh.preconitioned is False
+    # save_dir: each mode's final status; a second pass resumes from them and runs nothing
+    calls.clear()
+    sh.run_no_mode_mixing(int(d["n_steps"]), save_dir=str(tmp_path), noq=True)
+    assert sorted(p.name for p in tmp_path.glob("*_conv.npz")) == \
+        ["hessian_calculation_M%d_conv.npz" % (i + 1) for i in (0, 1, 3, 4)]
+    calls.clear()
+    sh.run_no_mode_mixing(int(d["n_steps"]), save_dir=str(tmp_path), restart_from_file=True,
+                          noq=True)
+    assert calls == []
+    np.testing.assert_allclose(sh.vector, d["vector"], rtol=1e-12)
