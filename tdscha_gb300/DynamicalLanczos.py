@@ -6,7 +6,8 @@ behaviour: ensemble/perturbation setup, `init`, `prepare_perturbation`,
 `prepare_unpolarized_raman`, `apply_full_L`, `run_FT`,
 `get_green_function_continued_fraction`, `get_static_frequency`,
 `build_lanczos_matrix_from_coeffs`, `get_alpha1_beta1_wigner`,
-`get_a1_b1_wigner`, `save_status` / `load_status`,
+`get_a1_b1_wigner`, `apply_L1_inverse_FT`, `L_linop` / `M_linop`,
+`run_biconjugate_gradient`, `save_status` / `load_status`,
 `save_abc` / `load_abc`, and the attributes `a_coeffs`, `b_coeffs`,
 `c_coeffs`, `basis_Q`, `basis_P`, `s_norm`, `psi`, `use_wigner`,
 `ignore_v3`, `ignore_v4`, `ignore_harmonic`, `reverse_L`, `shift_value`,
@@ -613,6 +614,157 @@ class Lanczos(object):
                                                  1 if transpose else 0, self._prec(), st))
         out = y.cpu().numpy()
         return out
+
+    # ------------------------------------------- harmonic inverse and solvers
+    def _free_pair_propagator(self):
+        """Per mode pair (upper triangle rows, w_a the column mode, w_b the row mode):
+        the 2 x 2 block (X, Y; X1, Y1) of the non-interacting two-phonon propagator
+        and the occupations used for it (:2478-2513).  Occupations are zeroed
+        where 0.01 w_a > k_B T, for both modes of the pair, as the reference does."""
+        iu = np.triu_indices(self.n_modes)
+        w_a, w_b = self.w[iu[1]], self.w[iu[0]]
+        n_a = np.zeros(np.shape(w_a), dtype=TYPE_DP)
+        n_b = np.zeros(np.shape(w_a), dtype=TYPE_DP)
+        cold = 0.01 * w_a * __RyToK__ > self.T
+        if self.T > 0:
+            kT = np.double(self.T / __RyToK__)
+            n_a = 1 / (np.exp(w_a / kT) - 1)
+            n_b = 1 / (np.exp(w_b / kT) - 1)
+            n_a[cold] = 0
+            n_b[cold] = 0
+        occ = (2 * n_a + 1) * (2 * n_b + 1)
+        cross = 2 * w_a * w_b
+        s = 2 * n_a * n_b + n_a + n_b
+        X = -w_a ** 2 - w_b ** 2 - cross / occ
+        Y = -(8 * w_a * w_b) / occ
+        X1 = -s * (s + 1) * cross / occ
+        Y1 = -w_a ** 2 - w_b ** 2 + cross / occ
+        return w_a, w_b, n_a, X, Y, X1, Y1
+
+    def apply_L1_inverse_FT(self, psi, transpose=False):
+        """Inverse of the harmonic operator (:2451-2560), the preconditioner of
+        run_biconjugate_gradient: 1/w^2 on the R sector and the inverse of each
+        pair's 2 x 2 block on the (Y, ReA) sectors.  A block with determinant below
+        1e-12 keeps only -1/X on its Y entry; at T > 0 a diagonal pair of populated
+        modes also inverts its ReA entry alone."""
+        out = np.zeros(np.shape(self.psi), dtype=TYPE_DP)
+        if self.ignore_harmonic:
+            return out
+        M = self.n_modes
+        psi = np.asarray(psi)
+        out[:M] = (psi[:M] / self.w) / self.w
+        w_a, w_b, n_a, X, Y, X1, Y1 = self._free_pair_propagator()
+        h = len(w_a)
+        if len(psi) != M + 2 * h:
+            raise AssertionError("\nERROR,\nThe initial vector for the Lanczos algorithm has a "
+                                 "wrong dimension. \nThis may be caused by the Lanczos "
+                                 "initialized at the wrong temperature.\n")
+        det = X * Y1 - X1 * Y
+        singular = det < __EPSILON__
+        det[singular] = np.inf
+        iX, iY, iX1, iY1 = -Y1 / det, Y / det, X1 / det, -X / det
+        iX[singular] = -1 / X[singular]
+        if self.T > __EPSILON__:
+            lone = (w_a == w_b) & (n_a > __EPSILON__)
+            iY1[lone] = -1 / Y1[lone]
+        pY, pA = psi[M:M + h], psi[M + h:]
+        oY, oA = out[M:M + h], out[M + h:]
+        oY[:] = iX * pY
+        if transpose:
+            oA += iY * pY
+            oY += iX1 * pA
+        else:
+            oY += iY * pA
+            oA += iX1 * pY
+        oA += iY1 * pA
+        return out
+
+    @property
+    def L_linop(self):
+        """scipy LinearOperator of the full L on the GPU; like the reference's
+        (:478-483), matvec is apply_full_L (which overwrites self.psi) and rmatvec
+        its transpose."""
+        import scipy.sparse.linalg
+        n = len(self.psi)
+        return scipy.sparse.linalg.LinearOperator(
+            shape=(n, n), matvec=self.apply_full_L,
+            rmatvec=lambda v: self.apply_full_L(v, transpose=True), dtype=TYPE_DP)
+
+    @property
+    def M_linop(self):
+        """scipy LinearOperator of apply_L1_inverse_FT (:485-489)."""
+        import scipy.sparse.linalg
+        n = len(self.psi)
+        return scipy.sparse.linalg.LinearOperator(
+            shape=(n, n), matvec=self.apply_L1_inverse_FT,
+            rmatvec=lambda v: self.apply_L1_inverse_FT(v, transpose=True), dtype=TYPE_DP)
+
+    def run_biconjugate_gradient(self, verbose=True, tol=5e-4, maxiter=1000, save_g=None,
+                                 save_each=1, use_preconditioning=True, algorithm="bicgstab"):
+        """Static response by solving L x_i = e_i for every mode (:3842-4052) with
+        scipy's bicgstab / bicg (tol as their relative tolerance) or a BFGS
+        minimisation of (Lx - b) H^-1 (Lx - b) / 2 ('cg-minimize'), every
+        application of L on the GPU.  Returns the inverse of the symmetrised
+        one-phonon block of G (the mass-rescaled free-energy Hessian)."""
+        import inspect
+        import scipy.optimize
+        import scipy.sparse.linalg as sla
+        algo = algorithm.lower()
+        if algo not in ("bicgstab", "bicg", "cg-minimize"):
+            raise ValueError("\nError, algorithm type '{}' in subroutine run_biconjugate_gradient "
+                             "not implemented.\n       the only supported algorithms are "
+                             "['bicgstab', 'bicg']\n".format(algorithm))
+        if not self.initialized:
+            self.prepare_symmetrization()
+        M = self.n_modes
+        G = np.zeros((M, M), dtype=np.double)
+        L, Minv = self.L_linop, self.M_linop
+        for i in range(M):
+            self.psi = np.zeros(self.psi.shape, dtype=TYPE_DP)
+            self.psi[i] = 1
+            b = self.psi
+            x0 = Minv.matvec(b)
+            last = [b.copy(), 0]
+
+            def callback(xk):
+                if np.isnan(np.sum(xk)):
+                    raise ValueError("Error, NaN value found during the Biconjugate Gradient.")
+                if verbose:
+                    print("BCG STEP {} | solution changed by {} (tol = {})".format(
+                        last[1], np.sum((xk - last[0]) ** 2), tol))
+                last[0], last[1] = xk.copy(), last[1] + 1
+
+            t1 = time.time()
+            if algo == "cg-minimize":
+                def func(x, rhs):
+                    r = L.matvec(x) - rhs
+                    h_r = Minv.matvec(Minv.rmatvec(r)) if use_preconditioning else r
+                    return 0.5 * np.sum(r * h_r), L.rmatvec(h_r)
+                res = scipy.optimize.minimize(func, x0, args=(b.copy(),), method="bfgs", jac=True,
+                                              options={"gtol": tol, "maxiter": maxiter,
+                                                       "disp": verbose, "norm": 2})
+                info, x = (0 if res.success else 1), res.x.copy()
+            else:
+                solver = sla.bicgstab if algo == "bicgstab" else sla.bicg
+                key = "rtol" if "rtol" in inspect.signature(solver).parameters else "tol"
+                x, info = solver(L, b, x0=x0, maxiter=maxiter, callback=callback,
+                                 M=Minv if use_preconditioning else None, **{key: tol})
+            if info < 0:
+                raise AssertionError("Error on input or breakdown of biconjugate gradient "
+                                     "algorithm (info = {})".format(info))
+            if verbose:
+                print("Time to solve the linear system: {} s".format(time.time() - t1))
+                if info > 0:
+                    print("The biconjugate gradient (step {}) algorithm did not converge after {} "
+                          "iterations.".format(i + 1, maxiter))
+            G[i, :] = x[:M]
+            if save_g is not None and i % save_each == 0:
+                np.save(save_g, G)
+        if save_g is not None:
+            np.save(save_g, G)
+        if np.max(np.abs(G - G.T)) >= 1e-4:
+            raise AssertionError("Error, the resulting one-phonon Green function is not Hermitian.")
+        return np.linalg.inv(0.5 * (G + G.T))
 
     def apply_L1_FT(self, transpose=False):
         """Harmonic part only, on self.psi (:2287-2445)."""

@@ -320,6 +320,62 @@ def no_mode_mixing_case(fname, M, seed, n_steps):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+@contextlib.contextmanager
+def _scipy_tol_adapter():
+    """The reference's run_biconjugate_gradient passes tol= to scipy's bicg /
+    bicgstab, a keyword recent scipy releases replaced by rtol; inside this
+    context (fixture generation only) tol is forwarded as rtol."""
+    import scipy.sparse.linalg as sla
+    saved = {k: getattr(sla, k) for k in ("bicg", "bicgstab")}
+
+    def wrap(fn):
+        def call(*a, tol=None, **kw):
+            if tol is not None:
+                kw["rtol"] = tol
+            return fn(*a, **kw)
+        return call
+    for k, fn in saved.items():
+        setattr(sla, k, wrap(fn))
+    try:
+        yield
+    finally:
+        for k, fn in saved.items():
+            setattr(sla, k, fn)
+
+
+def l1_inverse_case(fname, M, N, seed):
+    """apply_L1_inverse_FT (both directions, T > 0 and T = 0) and
+    run_biconjugate_gradient (bicgstab with the L1-inverse preconditioner)."""
+    import scipy.sparse.linalg
+    P = M + M * (M + 1)
+    rng = np.random.default_rng(seed + 1)
+    psi_r = rng.standard_normal(P)
+    # the harmonic inverse on thermally populated modes (50-500 cm^-1 at 300 K)
+    # and at T = 0
+    low = make_ensemble(M, N, seed=seed + 2, n_syms=1, rho_sigma=0.1)
+    lanc = make_reference_lanczos(low, use_wigner=False)
+    out = dict(w_low=low["w"], T_low=low["T"], psi_r=psi_r)
+    for tag, T in (("T", float(low["T"])), ("T0", 0.0)):
+        lanc.T = T
+        out["inv/" + tag] = lanc.apply_L1_inverse_FT(psi_r.copy())
+        out["invT/" + tag] = lanc.apply_L1_inverse_FT(psi_r.copy(), transpose=True)
+    # 0.36-1 Ry frequencies for the solve, as in static_case: the reference's absolute
+    # hermiticity assertion (|G - G^T| < 1e-4) needs G = O(1)
+    ens = make_ensemble(M, N, seed=seed, n_syms=1, rho_sigma=0.1, w_min_cm=40000.0,
+                        w_max_cm=110000.0)
+    lanc = make_reference_lanczos(ens, use_wigner=False)
+    out.update(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"])
+    lanc.M_linop = scipy.sparse.linalg.LinearOperator(
+        shape=(P, P), matvec=lanc.apply_L1_inverse_FT,
+        rmatvec=lambda v: lanc.apply_L1_inverse_FT(v, transpose=True), dtype=np.double)
+    with _scipy_tol_adapter(), contextlib.redirect_stdout(io.StringIO()):
+        out["G_inv/bicgstab"] = lanc.run_biconjugate_gradient(verbose=False, tol=1e-12,
+                                                              maxiter=3000, algorithm="bicgstab")
+        out["G_inv/cg-minimize"] = lanc.run_biconjugate_gradient(
+            verbose=False, tol=1e-10, maxiter=3000, algorithm="cg-minimize")
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -333,6 +389,7 @@ def main():
     input_files_case("input_files_m6_n5_s48.npz", 6, 5, 48, 51)
     host_helpers_case("host_helpers_m9.npz", 61)
     no_mode_mixing_case("no_mode_mixing_m5.npz", 5, 71, 12)
+    l1_inverse_case("l1_inverse_m6.npz", 6, 40, 81)
     print("fixtures written to", HERE)
 
 

@@ -188,3 +188,36 @@ def test_qspace_ir_and_raman_at_gamma():
     np.testing.assert_allclose(ql.psi[:6], proj(rv(1, 1) - rv(2, 2)), rtol=1e-12, atol=1e-300)
     # the rest of psi stays zero: a Gamma perturbation of the R sector only
     assert not np.any(ql.psi[6:])
+
+
+@pytest.mark.parametrize("tag", ["T", "T0"])
+def test_l1_inverse_matches_reference(golden, tag):
+    d = golden("l1_inverse_m6.npz")
+    M = d["w_low"].size
+    lanc = Lanczos.from_arrays(np.zeros((2, M)), np.zeros((2, M)), d["w_low"], np.ones(2),
+                               float(d["T_low"]) if tag == "T" else 0.0, use_wigner=False)
+    np.testing.assert_array_equal(lanc.apply_L1_inverse_FT(d["psi_r"]), d["inv/" + tag])
+    np.testing.assert_array_equal(lanc.apply_L1_inverse_FT(d["psi_r"], transpose=True),
+                                  d["invT/" + tag])
+    with pytest.raises(AssertionError):
+        lanc.apply_L1_inverse_FT(d["psi_r"][:-1])
+
+
+def test_biconjugate_gradient_matches_reference(golden):
+    """run_biconjugate_gradient's solves through L_linop / M_linop, with the
+    operator applied by the oracle (the product applies it on the GPU), against
+    the reference's own run on the same ensemble."""
+    d = golden("l1_inverse_m6.npz")
+    ens = dict(X=d["X"], Y=d["Y"], w=d["w"], rho=d["rho"], T=float(d["T"]))
+    lanc = Lanczos.from_arrays(d["X"], d["Y"], d["w"], d["rho"], float(d["T"]), use_wigner=False)
+    lanc.initialized = True
+    ol = oracle.OracleLanczos(ens, use_wigner=False)
+    lanc._apply_dev = lambda psi, transpose, **kw: ol.apply_full_L(np.asarray(psi), transpose)
+    G_inv = lanc.run_biconjugate_gradient(verbose=False, tol=1e-12, maxiter=3000)
+    np.testing.assert_allclose(G_inv, d["G_inv/bicgstab"], rtol=1e-7, atol=1e-10)
+    # the BFGS form stops where the reference's does (short of the bicgstab solution)
+    G_min = lanc.run_biconjugate_gradient(verbose=False, tol=1e-10, maxiter=3000,
+                                          algorithm="cg-minimize")
+    np.testing.assert_allclose(G_min, d["G_inv/cg-minimize"], rtol=1e-6, atol=1e-9)
+    with pytest.raises(ValueError):
+        lanc.run_biconjugate_gradient(verbose=False, algorithm="gmres")
