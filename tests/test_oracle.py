@@ -118,3 +118,48 @@ def test_continued_fraction_known_answers():
     n1 = _cf(a2, b2, b2, w2, False, use_terminator=False, smearing=0.01, smooth_ramp=0)
     n2 = _cf(a2, b2, b2, w2, False, use_terminator=False, smearing=0.01, smooth_ramp=5)
     np.testing.assert_allclose(n1, n2, rtol=1e-14)
+
+
+def _reference_module():
+    """The reference's own C module, compiled from its sources into oracle/_ref by
+    oracle/build_ref.sh (present only where the reference tree was available)."""
+    import importlib
+    import os
+    import sys
+    ref = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle",
+                       "_ref")
+    if not os.path.isdir(ref):
+        pytest.skip("oracle/_ref not built (no reference tree here)")
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    try:
+        return importlib.import_module("sscha_HP_odd")
+    except ImportError:
+        pytest.skip("oracle/_ref holds no importable reference module")
+
+
+@pytest.mark.parametrize("M,N,S", [(189, 6, 48), (573, 3, 1)])
+def test_oracle_matches_reference_module_at_config_shapes(M, N, S):
+    """The oracle against the reference's compiled module, run live, on slices of
+    the benchmark shapes (189 modes with 48 images; 573 modes): bit-exact."""
+    import contextlib
+    import io
+    from tdscha_gb300.synthetic import make_ensemble, random_R1, random_sym
+    ref = _reference_module()
+    ens = make_ensemble(M, N, seed=7 + M, n_syms=S, rho_sigma=0.1)
+    if S > 1:
+        syms, spaces, bid = ens["symmetries"], ens["degenerate_space"], ens["sym_block_id"]
+    else:
+        syms, spaces, bid = oracle.identity_symmetries(M)
+    R1, Y1 = random_R1(M, 3), random_sym(M, 4, scale=1e-3)
+    n_deg = np.array([len(b) for b in spaces], dtype=np.intc)
+    for d4 in (0, 1):
+        f_ref, d_ref = np.zeros(M), np.zeros((M, M))
+        with contextlib.redirect_stdout(io.StringIO()):
+            ref.GetPerturbAverageSym(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1, ens["T"],
+                                     d4, int(syms[0].shape[0]), syms, n_deg, spaces,
+                                     np.asarray(bid, dtype=np.intc), f_ref, d_ref)
+        f, d2v = oracle.perturb_averages(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                         ens["T"], d4, syms, spaces, bid)
+        np.testing.assert_array_equal(f, f_ref)
+        np.testing.assert_array_equal(d2v, d_ref)
