@@ -129,3 +129,47 @@ def test_continued_fraction_rejects_bad_args(lib):
     rc = lib.tdscha_continued_fraction(nat.dp(a), 0, nat.dp(a), 0, nat.dp(a), 0, nat.dp(a), 1,
                                        0, 1.0, 0, 0.0, 1, 1, 0.0, 0, nat.dp(g))
     assert rc == nat.ERR_ARG
+
+
+# entry points whose first argument is a context / network handle: NULL is rejected
+# with TDSCHA_ERR_ARG before any CUDA call (destroy of NULL is a no-op)
+_HANDLE_FIRST = [
+    "tdscha_ctx_layout", "tdscha_ctx_profile", "tdscha_ctx_profile_read", "tdscha_ctx_set_basis_ld",
+    "tdscha_ctx_set_options", "tdscha_ctx_set_translations", "tdscha_ctx_sync", "tdscha_ctx_tuning",
+    "tdscha_lanczos_run", "tdscha_lanczos_run_hostbuf", "tdscha_apply_full_L",
+    "tdscha_perturb_averages", "tdscha_static_L", "tdscha_static_hessian_expand",
+    "tdscha_static_hessian_collect", "tdscha_qapply_full_L", "tdscha_qctx_set_pert",
+    "tdscha_qctx_set_precision", "tdscha_qkpm_run", "tdscha_qlanczos_run",
+    "tdscha_qperturb_averages", "tdscha_mlp_forward", "tdscha_mlp_get_params",
+    "tdscha_mlp_set_params", "tdscha_mlp_loss_grad", "tdscha_mlp_train_step",
+    # no handle, but null output / input pointers
+    "tdscha_ctx_create", "tdscha_qctx_create", "tdscha_mlp_create", "tdscha_project_modes",
+    "tdscha_project_bloch", "tdscha_perturb_averages_noalloc", "tdscha_lanczos_run_batch"]
+
+
+def _null_args(fn):
+    args = []
+    for t in fn.argtypes:
+        if t in (ctypes.c_double, ctypes.c_float):
+            args.append(0.0)
+        elif t in (ctypes.c_int, ctypes.c_long, ctypes.c_longlong, ctypes.c_uint,
+                   ctypes.c_ulong, ctypes.c_ulonglong, ctypes.c_size_t):
+            args.append(0)
+        else:
+            args.append(None)
+    return args
+
+
+@pytest.mark.parametrize("name", _HANDLE_FIRST)
+def test_null_handles_and_pointers_rejected(lib, name):
+    fn = getattr(lib, name)
+    args = _null_args(fn)
+    if name == "tdscha_lanczos_run_batch":
+        args[1] = -1          # a negative run count with no runs
+    assert fn(*args) == nat.ERR_ARG, name
+    assert lib.tdscha_last_error()
+
+
+def test_null_destroy_is_noop(lib):
+    for name in ("tdscha_ctx_destroy", "tdscha_qctx_destroy", "tdscha_mlp_destroy"):
+        assert getattr(lib, name)(None) == nat.OK
