@@ -221,3 +221,51 @@ def test_biconjugate_gradient_matches_reference(golden):
     np.testing.assert_allclose(G_min, d["G_inv/cg-minimize"], rtol=1e-6, atol=1e-9)
     with pytest.raises(ValueError):
         lanc.run_biconjugate_gradient(verbose=False, algorithm="gmres")
+
+
+def test_ir_raman_modulus_real_space_equals_qspace():
+    """The reference's test_qspace/test_ir_modulus.py and test_raman_modulus.py in
+    synthetic form: a two-cell supercell whose modes are the Bloch combinations of
+    the q = 0 and q = 1/2 modes (Gamma translations dropped); with charges and a
+    Raman tensor obeying the acoustic sum rule, the real-space and q-space
+    perturbations have the same modulus."""
+    from tdscha_gb300.QSpaceLanczos import QSpaceLanczos
+    rng = np.random.default_rng(21)
+    nat, ncell = 2, 2
+    nb = 3 * nat
+    m_at = rng.uniform(1e3, 1e5, nat)
+    m = np.repeat(m_at, 3)
+    trans = np.zeros((nb, 3))
+    for d in range(3):
+        trans[d::3, d] = np.sqrt(m_at)
+    e0, _ = np.linalg.qr(np.hstack([trans, rng.standard_normal((nb, nb - 3))]))
+    e1, _ = np.linalg.qr(rng.standard_normal((nb, nb)))
+    pols_q = np.stack([e0, e1], axis=2).astype(np.complex128)
+    sc = np.hstack([np.vstack([e0, e0])[:, 3:], np.vstack([e1, -e1])]) / np.sqrt(ncell)
+    M = sc.shape[1]
+    N = 4
+    real = Lanczos.from_arrays(rng.standard_normal((N, M)), rng.standard_normal((N, M)),
+                               rng.uniform(1e-3, 3e-3, M), np.ones(N), 100.0, pols=sc,
+                               m=np.tile(m, ncell))
+    Xq = rng.standard_normal((ncell, N, nb)) + 0j
+    ql = QSpaceLanczos.from_arrays(Xq, Xq.copy(), rng.uniform(1e-3, 3e-3, (nb, ncell)),
+                                   np.ones(N), 100.0, q_points=np.array([[0, 0, 0], [0.5, 0, 0]]),
+                                   pols_q=pols_q, m=m)
+    A = rng.standard_normal((3, 3))
+    ec = np.stack([A, -A])                               # sum over atoms = 0
+    R = rng.standard_normal((3, 3, nat, 3))
+    R -= R.mean(axis=2, keepdims=True)                   # sum over atoms = 0
+    R = R.reshape(3, 3, nb)
+    for pol in (np.array([1.0, 0, 0]), np.array([0.3, -0.4, 0.8])):
+        real.prepare_ir(effective_charges=ec, pol_vec=pol)
+        ql.prepare_ir(effective_charges=ec, pol_vec=pol)
+        np.testing.assert_allclose(real.perturbation_modulus, ql.perturbation_modulus, rtol=1e-12)
+    e = np.eye(3)
+    real.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[1], raman_tensor=R)
+    ql.prepare_raman(pol_vec_in=e[0], pol_vec_out=e[1], raman_tensor=R)
+    np.testing.assert_allclose(real.perturbation_modulus, ql.perturbation_modulus, rtol=1e-12)
+    for k in range(7):
+        real.prepare_unpolarized_raman(index=k, raman_tensor=R)
+        ql.prepare_unpolarized_raman(index=k, raman_tensor=R)
+        np.testing.assert_allclose(real.perturbation_modulus, ql.perturbation_modulus,
+                                   rtol=1e-12)
