@@ -1,4 +1,5 @@
-"""Drop-in for the reference's compiled module `sscha_HP_odd` on the fast path.
+"""Drop-in for the reference's compiled module `sscha_HP_odd` on the fast path
+(`GetPerturbAverageSym`, and `GetPerturbAverage` without symmetry images).
 
 `GetPerturbAverageSym` keeps the reference's positional arguments
 (CModules/odd_corr_module.c:491-634, call site
@@ -39,3 +40,23 @@ def GetPerturbAverageSym(X, Y, w, rho, R1, Y1, T, apply_D4, N_syms, sym_list, n_
         int(apply_D4), s, len(ndeg_flat), nat.ip(ndeg_flat), nat.ip(deg), nat.dp(sym),
         nat.ip(bid), nat.dp(f_out), nat.dp(d2v_out)))
     return None
+
+
+def GetPerturbAverage(X, Y, w, rho, R1, Y1, T, apply_D4, f_out, d2v_out):
+    """The module's form without symmetry images (CModules/odd_corr_module.c:408-487,
+    LanczosFunctions.c:1731-1905): same outputs and in-place convention.  Y1 enters
+    those loops only through x^T Y1 x and x^T Y1 f, i.e. through its symmetric part,
+    so this is GetPerturbAverageSym with one-mode identity blocks on (Y1 + Y1^T) / 2
+    (the reference's two functions agree to rounding on such inputs)."""
+    X = nat.f64(X)
+    if X.ndim != 2:
+        raise ValueError("X must be an (N, n_modes) array")
+    M = X.shape[1]
+    Y1 = nat.f64(Y1)
+    if Y1.shape != (M, M):
+        raise ValueError("Y1 must have shape (%d, %d), got %s" % (M, M, Y1.shape))
+    one = np.ones((1, 1, 1))
+    return GetPerturbAverageSym(X, Y, w, rho, R1, 0.5 * (Y1 + Y1.T), T, apply_D4, 1, [one] * M,
+                                np.ones(M, dtype=np.intc),
+                                [np.array([i], dtype=np.intc) for i in range(M)],
+                                np.arange(M, dtype=np.intc), f_out, d2v_out)

@@ -134,3 +134,55 @@ def test_unsymmetrised_tables_match_general_path():
     for a, b in zip(fast, slow):
         np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
         assert np.asarray(a).dtype == np.asarray(b).dtype
+
+
+def test_unsymmetrised_shim_errors():
+    X = np.zeros((4, 3))
+    with pytest.raises(ValueError, match="N_modes"):
+        sscha_HP_odd.GetPerturbAverage(X, X, np.ones(4), np.ones(4), np.zeros(3),
+                                       np.zeros((3, 3)), 300.0, 1, np.zeros(3), np.zeros((3, 3)))
+    with pytest.raises(ValueError, match="apply_D4"):
+        sscha_HP_odd.GetPerturbAverage(X, X, np.ones(3), np.ones(4), np.zeros(3),
+                                       np.zeros((3, 3)), 300.0, 2, np.zeros(3), np.zeros((3, 3)))
+
+
+def test_unsymmetrised_shim_against_reference(monkeypatch):
+    """GetPerturbAverage forwards to GetPerturbAverageSym with one-mode identity
+    blocks and the symmetric part of Y1; the forwarded call, evaluated by the
+    oracle, equals the reference module's own GetPerturbAverage (run live where
+    oracle/_ref is built) on a non-symmetric Y1."""
+    import importlib
+    import os
+    import sys
+    import oracle
+    ref_dir = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "oracle", "_ref")
+    if not os.path.isdir(ref_dir):
+        pytest.skip("oracle/_ref not built (no reference tree here)")
+    sys.path.insert(0, ref_dir)
+    try:
+        ref = importlib.import_module("sscha_HP_odd")
+    except ImportError:
+        pytest.skip("oracle/_ref holds no importable reference module")
+    finally:
+        sys.path.remove(ref_dir)
+    M, N = 9, 30
+    ens = make_ensemble(M, N, seed=5, rho_sigma=0.1)
+    rng = np.random.default_rng(1)
+    R1, Y1 = random_R1(M, 2), rng.standard_normal((M, M)) * 1e-3
+
+    def forwarded(X, Y, w, rho, R1, Y1, T, d4, S, syms, n_deg, spaces, bid, f, d2v):
+        assert S == 1 and np.array_equal(Y1, Y1.T)
+        assert np.array_equal(n_deg, np.ones(M)) and np.array_equal(bid, np.arange(M))
+        f[:], d2v[:] = oracle.perturb_averages(X, Y, w, rho, R1, Y1, T, d4, syms, spaces, bid)
+
+    monkeypatch.setattr(sscha_HP_odd, "GetPerturbAverageSym", forwarded)
+    for d4 in (0, 1):
+        f, d2v = np.zeros(M), np.zeros((M, M))
+        sscha_HP_odd.GetPerturbAverage(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1,
+                                       ens["T"], d4, f, d2v)
+        f_ref, d_ref = np.zeros(M), np.zeros((M, M))
+        ref.GetPerturbAverage(ens["X"], ens["Y"], ens["w"], ens["rho"], R1, Y1, ens["T"], d4,
+                              f_ref, d_ref)
+        np.testing.assert_allclose(f, f_ref, rtol=0, atol=1e-14 * np.abs(f_ref).max())
+        np.testing.assert_allclose(d2v, d_ref, rtol=0, atol=1e-14 * np.abs(d_ref).max())
