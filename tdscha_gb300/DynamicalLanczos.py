@@ -1301,3 +1301,64 @@ class Lanczos(object):
         if "perturbation_modulus" in data:
             self.perturbation_modulus = float(data["perturbation_modulus"])
         self._invalidate()
+
+
+def is_julia_enabled():
+    """The reference's switch for its Julia kernels (:171-180); this build has none."""
+    return False
+
+
+def _run_length(b_row, n_steps):
+    """Steps of a run whose b_n table is zero-padded after it stopped: up to and
+    including the step before the first zero b_n."""
+    zeros = np.flatnonzero(np.asarray(b_row)[:n_steps - 1] == 0)
+    return n_steps if zeros.size == 0 else int(zeros[0]) + 1
+
+
+def GetFreeEnergyCurvatureFromContinuedFraction(a_ns, b_ns, pols_sc, masses, mode_mixing=True,
+                                                use_terminator=True, last_average=5, smearing=0,
+                                                reference_contraction=True):
+    """Free-energy curvature in the supercell from one symmetric Lanczos run per
+    mode (a_ns[i, i]) and, with mode_mixing, per pair of modes (a_ns[i, j], the run
+    started from e_i + e_j) (:7084-7192).  G_ij(0) comes from each run's continued
+    fraction (on the GPU); the pair runs give the off-diagonal terms as
+    (G_{i+j} - G_ii - G_jj) / 2; the curvature is G^-1 = F taken back to Cartesian
+    coordinates with E = sqrt(m) e.  Like the reference, writes gf_mat.dat and
+    fc_pols.dat in the working directory.
+
+    The reference's final contraction, einsum("ab, ca, da -> cd"), sums F over its
+    second index before the change of basis: sum_a (sum_b F_ab) E_ca E_da rather
+    than E F E^T.  That result is returned by default (parity);
+    reference_contraction=False returns E F E^T."""
+    a_ns, b_ns = np.asarray(a_ns), np.asarray(b_ns)
+    n_modes = np.shape(pols_sc)[1]
+    n_steps = np.shape(a_ns)[2]
+    if n_steps - 1 != np.shape(b_ns)[2]:
+        raise AssertionError("Error, an and bn has an incompatible size:\n a_n = {}, b_n = {}"
+                             .format(np.shape(a_ns), np.shape(b_ns)))
+
+    def g0(i, j, modulus):
+        n = _run_length(b_ns[i, j], n_steps)
+        lanc = Lanczos(None)
+        lanc.a_coeffs = a_ns[i, j, :n]
+        lanc.b_coeffs = b_ns[i, j, :n - 1]
+        lanc.perturbation_modulus = modulus
+        print("Computing ({},{}) ... n_steps = {}".format(i, j, n))
+        return np.real(lanc.get_green_function_continued_fraction(
+            np.array([0]), use_terminator=use_terminator, smearing=smearing,
+            last_average=last_average)[0])
+
+    G = np.zeros((n_modes, n_modes), dtype=np.double)
+    for i in range(n_modes):
+        G[i, i] = g0(i, i, 1)
+    if mode_mixing:
+        for i in range(n_modes):
+            for j in range(i + 1, n_modes):
+                G[i, j] = G[j, i] = (g0(i, j, 2) - G[i, i] - G[j, j]) / 2
+    np.savetxt("gf_mat.dat", G)
+    fc_pols = np.linalg.inv(G)
+    np.savetxt("fc_pols.dat", fc_pols)
+    e_m = np.asarray(pols_sc) * np.sqrt(np.asarray(masses))[:, None]
+    if reference_contraction:
+        return np.einsum("a, ca, da -> cd", fc_pols.sum(axis=1), e_m, e_m)
+    return e_m @ fc_pols @ e_m.T

@@ -376,6 +376,36 @@ def l1_inverse_case(fname, M, N, seed):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def curvature_case(fname, M, n_steps, seed):
+    """GetFreeEnergyCurvatureFromContinuedFraction on given coefficient tables
+    (diagonal and mixed-pair runs, some stopped early by a zero b_n)."""
+    import tempfile
+    DL = load_reference()
+    rng = np.random.default_rng(seed)
+    w2 = rng.uniform(1.0, 4.0, M)
+    a = w2[:, None, None] * rng.uniform(0.8, 1.2, (M, M, n_steps))
+    b = rng.uniform(0.1, 0.3, (M, M, n_steps - 1))
+    b[0, 0, 5:] = 0.0           # a run that stopped after 6 steps
+    b[1, 2, 3:] = 0.0
+    nat_sc = 2
+    pols, _ = np.linalg.qr(rng.standard_normal((3 * nat_sc, 3 * nat_sc)))
+    pols = pols[:, :M]
+    masses = np.repeat(rng.uniform(1e3, 1e5, nat_sc), 3)
+    out = dict(a_ns=a, b_ns=b, pols=pols, masses=masses)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            with contextlib.redirect_stdout(io.StringIO()):
+                out["fc_mixing"] = DL.GetFreeEnergyCurvatureFromContinuedFraction(
+                    a, b, pols, masses, mode_mixing=True, use_terminator=True, last_average=3)
+                out["fc_diag_noterm"] = DL.GetFreeEnergyCurvatureFromContinuedFraction(
+                    a, b, pols, masses, mode_mixing=False, use_terminator=False, smearing=1e-3)
+        finally:
+            os.chdir(cwd)
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -390,6 +420,7 @@ def main():
     host_helpers_case("host_helpers_m9.npz", 61)
     no_mode_mixing_case("no_mode_mixing_m5.npz", 5, 71, 12)
     l1_inverse_case("l1_inverse_m6.npz", 6, 40, 81)
+    curvature_case("curvature_m4.npz", 4, 12, 91)
     print("fixtures written to", HERE)
 
 

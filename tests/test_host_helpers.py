@@ -269,3 +269,39 @@ def test_ir_raman_modulus_real_space_equals_qspace():
         ql.prepare_unpolarized_raman(index=k, raman_tensor=R)
         np.testing.assert_allclose(real.perturbation_modulus, ql.perturbation_modulus,
                                    rtol=1e-12)
+
+
+def test_free_energy_curvature_from_continued_fractions(golden, monkeypatch, tmp_path):
+    """GetFreeEnergyCurvatureFromContinuedFraction against the reference's own
+    output on the same coefficient tables (runs of different lengths, with and
+    without mode mixing); the continued fractions come from the oracle here."""
+    import tdscha_gb300.DynamicalLanczos as DLg
+    d = golden("curvature_m4.npz")
+
+    def cf(self, w, use_terminator=True, last_average=1, smearing=0.0, smooth_ramp=0):
+        return oracle.continued_fraction(list(self.a_coeffs), list(self.b_coeffs),
+                                         list(self.c_coeffs), w, self.use_wigner,
+                                         self.perturbation_modulus,
+                                         use_terminator=use_terminator,
+                                         last_average=last_average, smearing=smearing)
+
+    monkeypatch.setattr(DLg.Lanczos, "get_green_function_continued_fraction", cf)
+    monkeypatch.chdir(tmp_path)
+    fc = DLg.GetFreeEnergyCurvatureFromContinuedFraction(d["a_ns"], d["b_ns"], d["pols"],
+                                                         d["masses"], mode_mixing=True,
+                                                         use_terminator=True, last_average=3)
+    np.testing.assert_allclose(fc, d["fc_mixing"], rtol=1e-10, atol=1e-10 * np.abs(fc).max())
+    fc = DLg.GetFreeEnergyCurvatureFromContinuedFraction(d["a_ns"], d["b_ns"], d["pols"],
+                                                         d["masses"], mode_mixing=False,
+                                                         use_terminator=False, smearing=1e-3)
+    np.testing.assert_allclose(fc, d["fc_diag_noterm"], rtol=1e-10,
+                               atol=1e-10 * np.abs(fc).max())
+    assert (tmp_path / "gf_mat.dat").exists() and (tmp_path / "fc_pols.dat").exists()
+    # the corrected contraction: E F E^T with F = G^-1 from the saved fc_pols.dat
+    fc_pols = np.loadtxt(tmp_path / "fc_pols.dat")
+    e_m = d["pols"] * np.sqrt(d["masses"])[:, None]
+    fix = DLg.GetFreeEnergyCurvatureFromContinuedFraction(
+        d["a_ns"], d["b_ns"], d["pols"], d["masses"], mode_mixing=False, use_terminator=False,
+        smearing=1e-3, reference_contraction=False)
+    np.testing.assert_allclose(fix, e_m @ fc_pols @ e_m.T, rtol=1e-12, atol=1e-12 * np.abs(fix).max())
+    assert DLg.is_julia_enabled() is False
