@@ -814,6 +814,18 @@ class Lanczos(object):
                                              torch.cuda.current_stream().cuda_stream))
         return Y[0].cpu().numpy()
 
+    def _static_unit_rows(self, i0, k, what):
+        """The static operator (what: 1 harmonic, 2 anharmonic, 3 both) on the unit
+        vectors e_i0 .. e_{i0+k-1}, one batched GPU call; rows of a (k, n) array."""
+        torch = _torch()
+        n = self._static_size()
+        E = torch.zeros((k, n), dtype=torch.float64, device="cuda")
+        E[torch.arange(k), torch.arange(i0, i0 + k)] = 1.0
+        Y = self._static_dev(E, what)
+        nat.check(nat.load().tdscha_ctx_sync(self._ctx.handle,
+                                             torch.cuda.current_stream().cuda_stream))
+        return Y.cpu().numpy()
+
     def apply_L1_static(self, psi, inverse=False, power=1):
         """Harmonic part of the static operator (:2562-2624): psi_R w^(2p) and
         psi_W / Lambda^p, p = -power when inverse."""
@@ -1362,3 +1374,38 @@ def GetFreeEnergyCurvatureFromContinuedFraction(a_ns, b_ns, pols_sc, masses, mod
     if reference_contraction:
         return np.einsum("a, ca, da -> cd", fc_pols.sum(axis=1), e_m, e_m)
     return e_m @ fc_pols @ e_m.T
+
+
+def get_full_L_matrix(lanczos, transpose=False, static=False, compute_anharm=True,
+                      compute_harm=True, chunk=1024):
+    """The dense operator, column by column, for checks on small systems (:7365-7418).
+    Dynamic: L e_i (or L^T e_i) through lanczos.L_linop, one GPU application per
+    column (which, like the reference's, leaves the last column in lanczos.psi).
+    static=True: the static operator on the M + M(M+1)/2 sector, harmonic and/or
+    anharmonic part, applied to `chunk` unit vectors per batched GPU call (the static
+    operator is symmetric, so transpose does not change it)."""
+    print()
+    print('Getting the full L matrix')
+    print('Are we using the Wigner representation = {}'.format(lanczos.use_wigner))
+    print()
+    if not static:
+        L_op = lanczos.L_linop
+        n = len(lanczos.psi)
+        L = np.zeros((n, n), dtype=np.double)
+        v = np.zeros(n, dtype=np.double)
+        for i in range(n):
+            print("Step {} out of {}".format(i + 1, n))
+            v[:] = 0.0
+            v[i] = 1.0
+            L[:, i] = L_op.rmatvec(v) if transpose else L_op.matvec(v)
+        return L
+    what = (1 if compute_harm else 0) | (2 if compute_anharm else 0)
+    n = lanczos._static_size()
+    L = np.zeros((n, n), dtype=np.double)
+    lanczos.psi = np.zeros(n, dtype=TYPE_DP)
+    if what == 0:
+        return L
+    for i0 in range(0, n, chunk):
+        k = min(chunk, n - i0)
+        L[:, i0:i0 + k] = lanczos._static_unit_rows(i0, k, what).T
+    return L

@@ -406,6 +406,23 @@ def curvature_case(fname, M, n_steps, seed):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def full_L_case(fname, M, N, seed):
+    """get_full_L_matrix: the dense dynamic L (normal representation, both
+    directions) and the dense static operator (through static_adapter)."""
+    ens = make_ensemble(M, N, seed=seed, n_syms=1, rho_sigma=0.1)
+    out = dict(X=ens["X"], Y=ens["Y"], w=ens["w"], rho=ens["rho"], T=ens["T"])
+    DL = load_reference()
+    lanc = make_reference_lanczos(ens, use_wigner=False)
+    with contextlib.redirect_stdout(io.StringIO()):
+        out["L"] = DL.get_full_L_matrix(lanc)
+        out["LT"] = DL.get_full_L_matrix(lanc, transpose=True)
+    lanc = make_reference_lanczos(ens, use_wigner=True)
+    with static_adapter(lanc), contextlib.redirect_stdout(io.StringIO()):
+        out["L_static"] = DL.get_full_L_matrix(lanc, static=True)
+        out["L_static_harm"] = DL.get_full_L_matrix(lanc, static=True, compute_anharm=False)
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -421,6 +438,7 @@ def main():
     no_mode_mixing_case("no_mode_mixing_m5.npz", 5, 71, 12)
     l1_inverse_case("l1_inverse_m6.npz", 6, 40, 81)
     curvature_case("curvature_m4.npz", 4, 12, 91)
+    full_L_case("full_L_m4.npz", 4, 30, 95)
     print("fixtures written to", HERE)
 
 

@@ -305,3 +305,41 @@ def test_free_energy_curvature_from_continued_fractions(golden, monkeypatch, tmp
         smearing=1e-3, reference_contraction=False)
     np.testing.assert_allclose(fix, e_m @ fc_pols @ e_m.T, rtol=1e-12, atol=1e-12 * np.abs(fix).max())
     assert DLg.is_julia_enabled() is False
+
+
+def test_full_L_matrix_against_reference(golden, monkeypatch):
+    """get_full_L_matrix against the reference's dense operators: dynamic (both
+    directions, L applied by the oracle) and static (the batched static
+    application replaced by the oracle's static operator)."""
+    import types
+    import tdscha_gb300.DynamicalLanczos as DLg
+    d = golden("full_L_m4.npz")
+    ens = dict(X=d["X"], Y=d["Y"], w=d["w"], rho=d["rho"], T=float(d["T"]))
+    lanc = Lanczos.from_arrays(d["X"], d["Y"], d["w"], d["rho"], float(d["T"]), use_wigner=False)
+    ol = oracle.OracleLanczos(ens, use_wigner=False)
+    lanc._apply_dev = lambda psi, transpose, **kw: ol.apply_full_L(np.asarray(psi), transpose)
+    np.testing.assert_allclose(DLg.get_full_L_matrix(lanc), d["L"], rtol=0,
+                               atol=1e-12 * np.abs(d["L"]).max())
+    np.testing.assert_allclose(DLg.get_full_L_matrix(lanc, transpose=True), d["LT"], rtol=0,
+                               atol=1e-12 * np.abs(d["LT"]).max())
+    ow = oracle.OracleLanczos(ens, use_wigner=True)
+
+    def unit_rows(self, i0, k, what):
+        n = self._static_size()
+        rows = []
+        for i in range(i0, i0 + k):
+            e = np.zeros(n)
+            e[i] = 1.0
+            out = np.zeros(n)
+            if what & 1:
+                out += oracle.static_L1(d["w"], float(d["T"]), e)
+            if what & 2:
+                out += oracle.static_anharmonic(ow, e)
+            rows.append(out)
+        return np.array(rows)
+
+    lanc.use_wigner = True
+    lanc._static_unit_rows = types.MethodType(unit_rows, lanc)
+    for key, kw in (("L_static", {}), ("L_static_harm", {"compute_anharm": False})):
+        got = DLg.get_full_L_matrix(lanc, static=True, chunk=5, **kw)
+        np.testing.assert_allclose(got, d[key], rtol=0, atol=1e-11 * np.abs(d[key]).max())
