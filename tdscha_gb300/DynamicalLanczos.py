@@ -1144,6 +1144,19 @@ class Lanczos(object):
         sign = -1 if self.reverse_L else 1
         return sign * matrix - sign * np.eye(n) * self.shift_value
 
+    def run_full_diag(self, number, discard_dyn=True, n_iter=100):
+        """The `number` largest eigenpairs of L by ARPACK (scipy eigsh on L_linop, every
+        application on the GPU) from the current psi (:6500-6543); eigvects keep only
+        the R sector when discard_dyn.  Like the reference, eigsh treats L as symmetric."""
+        import scipy.sparse.linalg
+        eigvals, eigvects = scipy.sparse.linalg.eigsh(self.L_linop, k=number, v0=self.psi,
+                                                      ncv=n_iter)
+        self.eigvals = eigvals
+        self.eigvects = eigvects
+        if discard_dyn:
+            eigvects = eigvects[:self.n_modes, :]
+        return eigvals, eigvects
+
     def run(self, n_iter, save_dir=".", verbose=True):
         """Deprecated in the reference (:4497-4517): use run_FT."""
         raise ValueError("Error, this run funciton has been deprecated, use run_FT instead.")

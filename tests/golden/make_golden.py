@@ -417,6 +417,12 @@ def full_L_case(fname, M, N, seed):
         out["L"] = DL.get_full_L_matrix(lanc)
         out["LT"] = DL.get_full_L_matrix(lanc, transpose=True)
     lanc = make_reference_lanczos(ens, use_wigner=True)
+    rng = np.random.default_rng(seed + 1)
+    v0 = rng.standard_normal(len(lanc.psi))
+    lanc.psi = v0.copy()
+    with contextlib.redirect_stdout(io.StringIO()):
+        ev, evec = lanc.run_full_diag(3, discard_dyn=True, n_iter=20)
+    out.update(diag_v0=v0, diag_eigvals=ev, diag_eigvects=evec)
     with static_adapter(lanc), contextlib.redirect_stdout(io.StringIO()):
         out["L_static"] = DL.get_full_L_matrix(lanc, static=True)
         out["L_static_harm"] = DL.get_full_L_matrix(lanc, static=True, compute_anharm=False)

@@ -323,6 +323,15 @@ def test_full_L_matrix_against_reference(golden, monkeypatch):
     np.testing.assert_allclose(DLg.get_full_L_matrix(lanc, transpose=True), d["LT"], rtol=0,
                                atol=1e-12 * np.abs(d["LT"]).max())
     ow = oracle.OracleLanczos(ens, use_wigner=True)
+    # ARPACK on L (Wigner) from the same start vector as the reference's run_full_diag
+    lw = Lanczos.from_arrays(d["X"], d["Y"], d["w"], d["rho"], float(d["T"]), use_wigner=True)
+    lw._apply_dev = lambda psi, transpose, **kw: ow.apply_full_L(np.asarray(psi), transpose)
+    lw.psi = d["diag_v0"].copy()
+    ev, evec = lw.run_full_diag(3, discard_dyn=True, n_iter=20)
+    np.testing.assert_allclose(ev, d["diag_eigvals"], rtol=1e-9)
+    # eigenvectors up to sign
+    sgn = np.sign(np.sum(evec * d["diag_eigvects"], axis=0))
+    np.testing.assert_allclose(evec * sgn, d["diag_eigvects"], atol=1e-7)
 
     def unit_rows(self, i0, k, what):
         n = self._static_size()
