@@ -1144,6 +1144,57 @@ class Lanczos(object):
         sign = -1 if self.reverse_L else 1
         return sign * matrix - sign * np.eye(n) * self.shift_value
 
+    # ------------------------- Lehmann representation on a stored Krylov basis
+    def _krylov_eigenpairs(self, use_arnoldi, drop_last):
+        """Eigenpairs of the Lanczos (or Arnoldi) matrix with the eigenvectors taken
+        back to psi space through the stored Krylov basis (krilov_basis, the vectors a
+        status saved by the reference's earlier symmetric Lanczos holds).  drop_last:
+        "always" drops the basis' last vector, "extra" only when it has one vector
+        more than the matrix (a run that did not converge)."""
+        matrix = self.build_lanczos_matrix_from_coeffs(use_arnoldi)
+        vals, vecs = np.linalg.eigh(matrix)
+        kb = np.array(self.krilov_basis)
+        if drop_last == "always" or (drop_last == "extra" and kb.shape[0] > len(vals)):
+            kb = kb[:-1, :]
+        return vals, kb.T @ vecs
+
+    def _to_modes(self, v):
+        return (np.asarray(v) / np.sqrt(self.m)) @ self.pols
+
+    def get_green_function_Lenmann(self, w_array, smearing, v_a, v_b, use_arnoldi=False):
+        """G_ab(w) = sum_j <v_a|j><j|v_b> / (lambda_j - w^2 + 2 i w smearing) over the
+        eigenpairs of the symmetric Lanczos matrix (:4696-4750); v_a, v_b Cartesian
+        (3 nat), mass-scaled into the mode basis."""
+        if not len(self.c_coeffs) < len(self.b_coeffs):
+            raise AssertionError("Lenmann cannot be used with non-symmetric Lanczos")
+        va, vb = self._to_modes(v_a), self._to_modes(v_b)
+        vals, vecs = self._krylov_eigenpairs(use_arnoldi, "always")
+        R = vecs[:self.n_modes, :]
+        weights = (va @ R) * (vb @ R)
+        w = np.asarray(w_array)
+        den = vals[None, :] - (w ** 2)[:, None] + 2j * (w * smearing)[:, None]
+        return np.sum(weights[None, :] / den, axis=1)
+
+    def get_spectral_function_from_Lenmann(self, w_array, smearing, use_arnoldi=True):
+        """-Im sum_j |<R|j>|^2 / (lambda_j - w^2 + 2 i w smearing), the R-sector weight
+        of every eigenvector (:4984-5030)."""
+        vals, vecs = self._krylov_eigenpairs(use_arnoldi, "extra")
+        R = vecs[:self.n_modes, :]
+        weights = np.sum(np.conj(R) * R, axis=0)
+        w = np.asarray(w_array)
+        den = vals[None, :] - (w ** 2)[:, None] + 2j * (w * smearing)[:, None]
+        return -np.imag(np.sum(weights[None, :] / den, axis=1))
+
+    def get_static_odd_fc(self, use_arnoldi=False):
+        """Static force constants from the Lanczos eigenpairs (:4752-4822):
+        D = sum_i lambda_i R_i R_i^T in the mode basis, taken to Cartesian coordinates
+        and scaled by sqrt(m_a m_b)."""
+        vals, vecs = self._krylov_eigenpairs(use_arnoldi, "extra")
+        R = vecs[:self.n_modes, :]
+        D = (R * vals[None, :]) @ R.T
+        fc = self.pols @ D @ self.pols.T
+        return fc * np.sqrt(np.outer(self.m, self.m))
+
     def run_full_diag(self, number, discard_dyn=True, n_iter=100):
         """The `number` largest eigenpairs of L by ARPACK (scipy eigsh on L_linop, every
         application on the GPU) from the current psi (:6500-6543); eigvects keep only

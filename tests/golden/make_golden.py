@@ -429,6 +429,42 @@ def full_L_case(fname, M, N, seed):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
+def lehmann_case(fname, M, n, seed):
+    """get_green_function_Lenmann, get_spectral_function_from_Lenmann and
+    get_static_odd_fc on a stored Krylov basis (the data a status saved by the
+    reference's earlier symmetric Lanczos holds), tridiagonal and Arnoldi forms."""
+    rng = np.random.default_rng(seed)
+    ens = make_ensemble(M, 5, seed=seed, n_syms=1, rho_sigma=0.0)
+    lanc = make_reference_lanczos(ens, use_wigner=True)
+    P = M + M * (M + 1)
+    nat = 2
+    pols, _ = np.linalg.qr(rng.standard_normal((3 * nat, 3 * nat)))
+    pols = pols[:, :M]
+    m = np.repeat(rng.uniform(1e3, 1e5, nat), 3)
+    kb, _ = np.linalg.qr(rng.standard_normal((P, n + 1)))
+    a = rng.uniform(1e-6, 4e-6, n)
+    b = rng.uniform(1e-7, 5e-7, n - 1)
+    arn = [list(rng.uniform(-1e-7, 1e-7, i)) + [a[i]] for i in range(n)]
+    lanc.pols, lanc.m, lanc.nat = pols, m, nat
+    lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs = list(a), list(b), []
+    lanc.krilov_basis = [kb[:, i].copy() for i in range(n + 1)]
+    lanc.arnoldi_matrix = arn
+    w = np.linspace(0, 3e-3, 40)
+    v_a = rng.standard_normal(3 * nat)
+    v_b = rng.standard_normal(3 * nat)
+    out = dict(pols=pols, m=m, kb=kb, a=a, b=b, w=ens["w"], T=ens["T"], wgrid=w, v_a=v_a, v_b=v_b,
+               arnoldi=np.array([np.pad(r, (0, n - len(r))) for r in arn]))
+    with contextlib.redirect_stdout(io.StringIO()):
+        out["gf"] = lanc.get_green_function_Lenmann(w, 1e-4, v_a, v_b)
+        out["gf_arnoldi"] = lanc.get_green_function_Lenmann(w, 1e-4, v_a, v_b, use_arnoldi=True)
+        out["spectral"] = lanc.get_spectral_function_from_Lenmann(w, 1e-4, use_arnoldi=False)
+        out["spectral_arnoldi"] = lanc.get_spectral_function_from_Lenmann(w, 1e-4)
+        out["fc"] = lanc.get_static_odd_fc()
+        lanc.krilov_basis = lanc.krilov_basis[:n]        # a converged run: n vectors
+        out["fc_n"] = lanc.get_static_odd_fc()
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 def main():
     perturb_cases()
     run_case("runft_m21_n1000.npz", 21, 1000, 1, 0.0, 21, 50,
@@ -445,6 +481,7 @@ def main():
     l1_inverse_case("l1_inverse_m6.npz", 6, 40, 81)
     curvature_case("curvature_m4.npz", 4, 12, 91)
     full_L_case("full_L_m4.npz", 4, 30, 95)
+    lehmann_case("lehmann_m3.npz", 3, 8, 97)
     print("fixtures written to", HERE)
 
 

@@ -352,3 +352,30 @@ def test_full_L_matrix_against_reference(golden, monkeypatch):
     for key, kw in (("L_static", {}), ("L_static_harm", {"compute_anharm": False})):
         got = DLg.get_full_L_matrix(lanc, static=True, chunk=5, **kw)
         np.testing.assert_allclose(got, d[key], rtol=0, atol=1e-11 * np.abs(d[key]).max())
+
+
+def test_lehmann_representation_against_reference(golden):
+    d = golden("lehmann_m3.npz")
+    M = d["w"].size
+    n = d["a"].size
+    lanc = Lanczos.from_arrays(np.zeros((2, M)), np.zeros((2, M)), d["w"], np.ones(2),
+                               float(d["T"]), pols=d["pols"], m=d["m"])
+    lanc.a_coeffs, lanc.b_coeffs, lanc.c_coeffs = list(d["a"]), list(d["b"]), []
+    lanc.krilov_basis = [d["kb"][:, i] for i in range(n + 1)]
+    lanc.arnoldi_matrix = [list(d["arnoldi"][i, :i + 1]) for i in range(n)]
+    w, va, vb = d["wgrid"], d["v_a"], d["v_b"]
+    tol = dict(rtol=1e-10)
+    np.testing.assert_allclose(lanc.get_green_function_Lenmann(w, 1e-4, va, vb), d["gf"], **tol)
+    np.testing.assert_allclose(lanc.get_green_function_Lenmann(w, 1e-4, va, vb, use_arnoldi=True),
+                               d["gf_arnoldi"], **tol)
+    np.testing.assert_allclose(lanc.get_spectral_function_from_Lenmann(w, 1e-4, use_arnoldi=False),
+                               d["spectral"], rtol=1e-10, atol=1e-10 * np.abs(d["spectral"]).max())
+    np.testing.assert_allclose(lanc.get_spectral_function_from_Lenmann(w, 1e-4),
+                               d["spectral_arnoldi"], rtol=1e-10,
+                               atol=1e-10 * np.abs(d["spectral_arnoldi"]).max())
+    np.testing.assert_allclose(lanc.get_static_odd_fc(), d["fc"], **tol)
+    lanc.krilov_basis = lanc.krilov_basis[:n]
+    np.testing.assert_allclose(lanc.get_static_odd_fc(), d["fc_n"], **tol)
+    lanc.c_coeffs = list(d["b"])
+    with pytest.raises(AssertionError):
+        lanc.get_green_function_Lenmann(w, 1e-4, va, vb)
