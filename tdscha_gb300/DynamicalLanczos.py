@@ -819,8 +819,9 @@ class Lanczos(object):
         vectors e_i0 .. e_{i0+k-1}, one batched GPU call; rows of a (k, n) array."""
         torch = _torch()
         n = self._static_size()
-        E = torch.zeros((k, n), dtype=torch.float64, device="cuda")
-        E[torch.arange(k), torch.arange(i0, i0 + k)] = 1.0
+        dev = torch.device("cuda")
+        E = torch.zeros((k, n), dtype=torch.float64, device=dev)
+        E[torch.arange(k, device=dev), torch.arange(i0, i0 + k, device=dev)] = 1.0
         Y = self._static_dev(E, what)
         nat.check(nat.load().tdscha_ctx_sync(self._ctx.handle,
                                              torch.cuda.current_stream().cuda_stream))
