@@ -163,3 +163,51 @@ def test_oracle_matches_reference_module_at_config_shapes(M, N, S):
                                          ens["T"], d4, syms, spaces, bid)
         np.testing.assert_array_equal(f, f_ref)
         np.testing.assert_array_equal(d2v, d_ref)
+
+
+@pytest.mark.parametrize("M,N,S,wig", [(60, 300, 1, False), (60, 300, 1, True),
+                                        (24, 60, 48, True)])
+def test_oracle_run_FT_matches_reference_live(M, N, S, wig):
+    """The oracle's Lanczos driver against the reference's own run_FT (its Python
+    driver with stubbed physics modules and its compiled C module), run live in
+    this test on shapes beyond the fixtures: coefficients bit-exact over 12 steps."""
+    import os
+    import sys
+    _reference_module()
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    before = set(sys.modules)
+    sys.path.insert(0, here)
+    try:
+        from ref_harness import load_reference, make_reference_lanczos
+        try:
+            load_reference()
+        except ImportError as e:
+            pytest.skip(str(e))
+        _live_run_FT(make_reference_lanczos, M, N, S, wig)
+    finally:
+        sys.path.remove(here)
+        # drop the reference modules and the physics stubs the harness installed
+        for name in set(sys.modules) - before:
+            if name.split(".")[0] in ("tdscha", "cellconstructor", "sscha", "spglib",
+                                      "ref_harness"):
+                del sys.modules[name]
+
+
+def _live_run_FT(make_reference_lanczos, M, N, S, wig):
+    import contextlib
+    import io
+    from tdscha_gb300.synthetic import make_ensemble, random_R1
+    ens = make_ensemble(M, N, seed=3 + M, n_syms=S, rho_sigma=0.1)
+    R1 = random_R1(M, 4)
+    lanc = make_reference_lanczos(ens, use_wigner=wig)
+    lanc.psi[:] = 0
+    lanc.psi[:M] = R1
+    lanc.perturbation_modulus = R1.dot(R1)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lanc.run_FT(12, verbose=False)
+    ol = oracle.OracleLanczos(ens, use_wigner=wig)
+    ol.prepare_perturbation_R(R1)
+    ol.run_FT(12)
+    for k in "abc":
+        np.testing.assert_array_equal(np.array(getattr(ol, k + "_coeffs")),
+                                      np.array(getattr(lanc, k + "_coeffs")))
